@@ -1,0 +1,223 @@
+/*
+ * wbc.h — C-ABI of libwbc_gb300.so, the GB300 (sm_103a) implementation of WarpBioCell's
+ * coupled cell step.
+ *
+ * Every entry point takes plain device pointers and sizes, launches asynchronously on the
+ * given CUDA stream (`stream` is a cudaStream_t passed as void*; NULL = legacy default stream)
+ * and returns WBC_OK or a negative WBC_ERR_* code. Nothing here allocates, frees or owns
+ * memory: the caller owns every buffer (capacity-sized, as in the reference's CellPopulation)
+ * and passes the scratch buffers whose sizes the *_workspace_bytes queries return.
+ *
+ * Layouts (all C order, little-endian):
+ *   position, velocity     float[capacity][3]   (x, y, z) per slot
+ *   per-cell scalars       float/int32/uint32[capacity]
+ *   fields                 float[nx][ny][nz]    (k fastest, as the reference's array3d)
+ *   deposit accumulator    int64[4][nx][ny][nz] (state layer, then node)
+ *   network states         uint64[capacity][n_words], node i at word i/64, bit i%64
+ *
+ * Each declaration names the reference function it replaces (paths inside the
+ * Gennappio/WarpBioCell project, src/warpbiocell/...).
+ */
+#ifndef WBC_H
+#define WBC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------------ */
+#define WBC_OK 0
+#define WBC_ERR_INVALID (-1)       /* bad argument (null pointer, negative size, bad geometry) */
+#define WBC_ERR_CAPACITY (-2)      /* more cells than the allocation holds */
+#define WBC_ERR_CUDA (-4)          /* a CUDA launch or runtime call failed; see wbc_last_error */
+#define WBC_ERR_TIMEOUT (-5)       /* a bounded device-side wait ran out */
+#define WBC_ERR_WORKSPACE (-6)     /* scratch buffer smaller than the *_workspace_bytes query */
+
+/* Cell states (cells/model.py:14-18) and network fate bits (kernels/network_kernels.py:29-32). */
+#define WBC_STATE_PROLIFERATIVE 0
+#define WBC_STATE_QUIESCENT 1
+#define WBC_STATE_HYPOXIC 2
+#define WBC_STATE_DEAD 3
+#define WBC_FATE_PROLIFERATION 1
+#define WBC_FATE_APOPTOSIS 2
+#define WBC_FATE_GROWTH_ARREST 4
+#define WBC_FATE_NECROSIS 8
+
+/* Library version and the last CUDA error message seen by this thread (never NULL). */
+int wbc_version(void);
+const char* wbc_last_error(void);
+/* Number of CUDA devices visible to the runtime (0 on a machine without a GPU). */
+int wbc_device_count(void);
+
+/* ---- per-cell random streams --------------------------------------------------------------- */
+/* rng_state[i] = stream start of slot i for every slot in [0, capacity).
+ * Replaces cells/state.py:25-28 (_init_rng) as launched at cells/state.py:110. */
+int wbc_rng_init(int32_t seed, uint32_t* rng_state, int64_t capacity, void* stream);
+/* Test hooks: draw `draws` uniform floats / unit-sphere directions from streams [0, n); the
+ * streams advance in place (same functions the lifecycle and placement kernels use). */
+int wbc_rng_uniform(int32_t n, int32_t draws, uint32_t* rng_state, float* out, void* stream);
+int wbc_rng_sphere(int32_t n, uint32_t* rng_state, float* out_xyz, void* stream);
+/* Test hook: the project's exp(x) on n floats (used for every death / division probability). */
+int wbc_expf_batch(int32_t n, const float* x, float* out, void* stream);
+
+/* ---- hash-grid binning + contact mechanics -------------------------------------------------- */
+typedef struct wbc_neighbor_grid {
+    int32_t dim;             /* buckets per axis; cells hash as (floor(x / bucket)) mod dim      */
+    float cell_size;         /* query radius [um]; the bucket edge is cell_size * (1 + 2^-10)   */
+    int32_t* bucket_count;   /* int32[dim^3]                                                     */
+    int32_t* bucket_start;   /* int32[dim^3] exclusive prefix sum of bucket_count                */
+    int32_t* cell_bucket;    /* int32[capacity] bucket of each slot                               */
+    int32_t* cell_rank;      /* int32[capacity] arrival rank inside the bucket (unordered)         */
+    int32_t* scatter;        /* int32[capacity] slots grouped by bucket, unordered inside one      */
+    int32_t* sorted_id;      /* int32[capacity] slots grouped by bucket, ascending inside one      */
+    float* sorted_xyzr;      /* float[capacity][4] (x, y, z, radius) in sorted_id order            */
+    int32_t* scan_partials;  /* scratch, wbc_scan_workspace_bytes(dim^3) bytes                     */
+    int64_t capacity;
+} wbc_neighbor_grid;
+
+size_t wbc_scan_workspace_bytes(int64_t n);
+/* Bin the active prefix [0, n): counting sort of slots into hashed buckets, stable in slot
+ * order, plus a coalesced float4 copy of (x, y, z, r). Replaces spatial/neighbors.py:33-37
+ * (NeighborGrid.build -> warp HashGrid.build). */
+int wbc_grid_build(const wbc_neighbor_grid* grid, int32_t n, const float* position, const float* radius,
+                   void* stream);
+/* One contact substep over a built grid: neighbour count (|x_i - x_j| < query_radius, j != i),
+ * overlap-repulsion velocity, and x += v dt, fused. Replaces kernels/mechanics_kernels.py:26-57
+ * (contact_velocities) + :60-67 (integrate_positions) as driven by cells/mechanics.py:75-109. */
+int wbc_contact_substep(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                        float* position, float* velocity, int32_t* neighbor_count, void* stream);
+
+/* ---- fields ------------------------------------------------------------------------------------ */
+typedef struct wbc_grid_geometry {
+    int32_t nx, ny, nz;
+    float origin_x, origin_y, origin_z;
+    float inv_dx;
+} wbc_grid_geometry;
+
+/* accumulator[state][node] += int64(w * 2^24 + 0.5) for the 8 trilinear corners of each living
+ * or dead cell with 0 <= state < 4; cells outside the trilinear support are skipped.
+ * Replaces kernels/field_kernels.py:78-116 (deposit_trilinear). The accumulator is not cleared. */
+int wbc_deposit(const wbc_grid_geometry* geom, int32_t n, const float* position, const int32_t* cell_state,
+                int64_t* accumulator, void* stream);
+/* density[s][node] = float(acc[s][node]) / 2^24 * inv_voxel_volume (kernels/field_kernels.py:119-126)
+ * and, when `combined` is non-NULL, combined[node] = sum_k weights[k] * density[k][node] in the
+ * reference's order (kernels/field_kernels.py:129-142). `clear` != 0 zeroes the accumulator as it
+ * is read. `density` may be NULL when only the combination is wanted. */
+int wbc_density_convert(int64_t nodes, int64_t* accumulator, float inv_voxel_volume, float* density,
+                        const float* weights4, float* combined, int32_t clear, void* stream);
+/* out = sum_k weights[k] * density[k] (kernels/field_kernels.py:129-142, fields/densities.py:45-50). */
+int wbc_density_combine(int64_t nodes, const float* weights4, const float* density, float* out, void* stream);
+/* Clamped trilinear interpolation at each cell (kernels/field_kernels.py:153-182). */
+int wbc_sample(const wbc_grid_geometry* geom, const float* field, int32_t n, const float* position,
+               float* out, void* stream);
+
+typedef struct wbc_sor_params {
+    int32_t nx, ny, nz;
+    int32_t bc_x, bc_y, bc_z;    /* 0 = Dirichlet face (never written), 1 = Neumann (mirror)      */
+    float omega;
+    float dx2_over_D;            /* h = dx^2 / D                                                    */
+    float uptake_max;
+    float michaelis_k;
+    float reference;             /* residual scale: boundary value, or 1 when it is 0               */
+    int32_t has_source;
+    float source_k;
+} wbc_sor_params;
+
+/* `sweeps` red-black SOR sweeps in place (kernels/field_kernels.py:185-212 launched as in
+ * fields/diffusion.py:103-112), then, when residual_out is non-NULL, the max-norm residual of
+ * the result (kernels/field_kernels.py:215-243) written to residual_out[0] (device float).
+ * `fixed` int32[nodes] (non-zero = pinned); `production` and `source` may be NULL. */
+int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed, const float* density,
+                   const float* production, const float* source, float* field, float* residual_out,
+                   void* stream);
+/* Explicit FTCS step field_out = field_in + dt (D lap - uptake + production) (validation only;
+ * kernels/field_kernels.py:246-273). `p->dx2_over_D` carries D/dx^2 here. */
+int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,
+                  const float* production, const float* source, const float* field_in, float* field_out,
+                  void* stream);
+
+/* ---- lifecycle ----------------------------------------------------------------------------------- */
+typedef struct wbc_lifecycle_params {
+    float dt;
+    float death_rate;
+    float anoxic_death_rate;
+    float division_rate;
+    int32_t inhibition_threshold;
+    float hypoxia_threshold;
+    float death_threshold;
+    float glucose_threshold;
+    float glucose_death_threshold;
+    int32_t necrosis_requires_glucose;
+    int32_t phenotype_model;      /* 0 = rules, 1 = network                                        */
+    float apoptosis_rate;
+    float necrosis_rate;
+} wbc_lifecycle_params;
+
+/* Death / state / division intent per cell (kernels/cell_kernels.py:77-154, cells/lifecycle.py:96-132). */
+int wbc_lifecycle_decide(const wbc_lifecycle_params* p, int32_t n, int32_t* cell_state, float* age,
+                         const int32_t* neighbor_count, const float* oxygen_local, const float* glucose_local,
+                         const int32_t* fate_flags, uint32_t* rng_state, int32_t* divide_flag, void* stream);
+/* Inclusive prefix sum of divide_flag[0, n) into division_offset; total_out[0] (device int32)
+ * receives the last value. Replaces warp.utils.array_scan at cells/lifecycle.py:146. */
+int wbc_division_scan(int32_t n, const int32_t* divide_flag, int32_t* division_offset, int32_t* total_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+/* Daughter of the k-th dividing cell into slot count + k (kernels/cell_kernels.py:157-200). */
+int wbc_place_daughters(int32_t count, float placement_factor, const int32_t* divide_flag,
+                        const int32_t* division_offset, float* position, float* radius, int32_t* cell_state,
+                        int32_t* cell_type, float* age, float* oxygen_local, float* glucose_local,
+                        uint32_t* rng_state, float* velocity, int32_t* neighbor_count, int32_t* fate_flags,
+                        void* stream);
+/* counts[state] += cells in that state (kernels/cell_kernels.py:203-208). counts is int32[4]. */
+int wbc_count_states(int32_t n, const int32_t* cell_state, int32_t* counts, void* stream);
+
+/* ---- Boolean networks --------------------------------------------------------------------------- */
+typedef struct wbc_network_program {
+    int32_t n_nodes;
+    int32_t n_words;             /* ceil(n_nodes / 64), at most 4                                   */
+    int32_t n_ops;
+    int32_t n_updatable;
+    const int32_t* ops;          /* postfix opcodes: 0 VAR, 1 NOT, 2 AND, 3 OR, 4 CONST             */
+    const int32_t* args;
+    const int32_t* start;        /* per node                                                         */
+    const int32_t* length;       /* per node                                                         */
+    const int32_t* updatable;    /* node ids of the non-input nodes                                  */
+} wbc_network_program;
+
+/* Zero the words, then node i ON when randf < p_on[i] (kernels/network_kernels.py:81-95). */
+int wbc_network_initialize(const wbc_network_program* prog, int32_t n, const float* p_on, uint32_t* rng_state,
+                           uint64_t* states, void* stream);
+/* Input clamps from sampled fields or constants (kernels/network_kernels.py:98-132). */
+int wbc_network_clamp_inputs(int32_t n, int32_t n_words, int32_t n_clamps, const int32_t* clamp_node,
+                             const int32_t* clamp_source, const float* clamp_threshold, const int32_t* clamp_above,
+                             const float* oxygen_local, const float* glucose_local, const float* extra_a,
+                             const float* extra_b, uint64_t* states, void* stream);
+/* `sweeps` synchronous updates (kernels/network_kernels.py:157-175 launched as in
+ * network/runtime.py:170-172); the state words stay in registers across sweeps. */
+int wbc_network_update_sync(const wbc_network_program* prog, int32_t n, int32_t sweeps, uint64_t* states,
+                            void* stream);
+/* `n_updates` random single-node updates per cell (kernels/network_kernels.py:135-154). */
+int wbc_network_update_async(const wbc_network_program* prog, int32_t n, int32_t n_updates, uint32_t* rng_state,
+                             uint64_t* states, void* stream);
+/* Gillespie simulation of the MaBoSS chain for `duration` (kernels/network_kernels.py:178-245). */
+int wbc_network_update_maboss(const wbc_network_program* prog, int32_t n, float duration, int32_t max_events,
+                              const float* rate_up_true, const float* rate_up_false, const float* rate_down_true,
+                              const float* rate_down_false, uint32_t* rng_state, uint64_t* states, void* stream);
+/* Pack the four fate nodes (-1 = absent) into fate_flags (kernels/network_kernels.py:248-268). */
+int wbc_network_read_fates(int32_t n, int32_t n_words, int32_t node_proliferation, int32_t node_apoptosis,
+                           int32_t node_growth_arrest, int32_t node_necrosis, const uint64_t* states,
+                           int32_t* fate_flags, void* stream);
+/* Daughters copy their parent's words (kernels/network_kernels.py:271-284). */
+int wbc_network_inherit(int32_t count_before, int32_t n_words, const int32_t* divide_flag,
+                        const int32_t* division_offset, uint64_t* states, void* stream);
+/* counts[k] += (living) cells with node nodes[k] ON (kernels/network_kernels.py:287-302). */
+int wbc_network_count_on(int32_t n, int32_t n_words, int32_t n_query, const int32_t* nodes, int32_t living_only,
+                         const int32_t* cell_state, const uint64_t* states, int32_t* counts, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WBC_H */

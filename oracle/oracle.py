@@ -1,0 +1,417 @@
+"""Python face of the CPU oracle (test infrastructure only).
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` use this
+module, and only as the checker / the timed CPU restatement; the product never imports it.
+
+``liboracle.so`` (wbc_oracle.cpp) restates each reference kernel; this module binds it with
+ctypes and adds ``OracleSim``, a numpy mirror of a whole coupled cell step in the reference's
+operator-splitting order (simulation/simulator.py:58-81): field update (deposit -> combine ->
+SOR to tolerance with the reference's check cadence, fields/diffusion.py:79-123 -> sample),
+network step, lifecycle decide + inclusive scan + capacity check + placement
+(cells/lifecycle.py:96-179), network inheritance, mechanics substeps
+(cells/mechanics.py:112-122). Scalar parameters are rounded to float32 from the same double
+expressions the reference passes to its kernels.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from oracle.build import build as _build
+
+_lib = None
+
+
+class SorParams(ctypes.Structure):
+    _fields_ = [("nx", c_int32), ("ny", c_int32), ("nz", c_int32), ("bc_x", c_int32), ("bc_y", c_int32),
+                ("bc_z", c_int32), ("omega", c_float), ("dx2_over_D", c_float), ("uptake_max", c_float),
+                ("michaelis_k", c_float), ("reference", c_float), ("has_source", c_int32), ("source_k", c_float)]
+
+
+class LifecycleParamsC(ctypes.Structure):
+    _fields_ = [("dt", c_float), ("death_rate", c_float), ("anoxic_death_rate", c_float), ("division_rate", c_float),
+                ("inhibition_threshold", c_int32), ("hypoxia_threshold", c_float), ("death_threshold", c_float),
+                ("glucose_threshold", c_float), ("glucose_death_threshold", c_float),
+                ("necrosis_requires_glucose", c_int32), ("phenotype_model", c_int32), ("apoptosis_rate", c_float),
+                ("necrosis_rate", c_float)]
+
+
+class ProgramC(ctypes.Structure):
+    _fields_ = [("n_nodes", c_int32), ("n_words", c_int32), ("n_ops", c_int32), ("n_updatable", c_int32),
+                ("ops", c_void_p), ("args", c_void_p), ("start", c_void_p), ("length", c_void_p),
+                ("updatable", c_void_p)]
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(str(_build()))
+        _lib.orc_num_threads.restype = c_int32
+        _lib.orc_division_scan.restype = c_int32
+    return _lib
+
+
+def P(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"], "oracle arrays must be C-contiguous"
+    return a.ctypes.data_as(c_void_p)
+
+
+def f32(x) -> c_float:
+    return c_float(float(np.float32(x)))
+
+
+def set_threads(n: int) -> None:
+    lib().orc_set_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())
+
+
+# ---- per-kernel wrappers ------------------------------------------------------------------------------
+def rng_init(seed: int, capacity: int) -> np.ndarray:
+    out = np.zeros(capacity, dtype=np.uint32)
+    lib().orc_rng_init(c_int32(seed), P(out), c_int64(capacity))
+    return out
+
+
+def rng_uniform(state: np.ndarray, draws: int) -> np.ndarray:
+    out = np.zeros((state.size, draws), dtype=np.float32)
+    lib().orc_rng_uniform(c_int32(state.size), c_int32(draws), P(state), P(out))
+    return out
+
+
+def rng_sphere(state: np.ndarray) -> np.ndarray:
+    out = np.zeros((state.size, 3), dtype=np.float32)
+    lib().orc_rng_sphere(c_int32(state.size), P(state), P(out))
+    return out
+
+
+def expf(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    lib().orc_expf(c_int32(x.size), P(x), P(out))
+    return out
+
+
+def logf(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    lib().orc_logf(c_int32(x.size), P(x), P(out))
+    return out
+
+
+def contact_substep(pos: np.ndarray, radius: np.ndarray, cell_size: float, dim: int, query_radius: float, rate: float,
+                    dt: float, fp64: bool = False):
+    """One contact substep in place on ``pos`` (n, 3); returns (velocity, neighbor_count)."""
+    n = pos.shape[0]
+    nc = np.zeros(n, dtype=np.int32)
+    if fp64:
+        assert pos.dtype == np.float64
+        vel = np.zeros((n, 3), dtype=np.float64)
+        r = np.ascontiguousarray(radius, dtype=np.float64)
+        lib().orc_contact_substep_f64(c_int32(n), P(pos), P(r), f32(cell_size), c_int32(dim), c_double(query_radius),
+                                      c_double(rate), c_double(dt), P(vel), P(nc))
+    else:
+        assert pos.dtype == np.float32
+        vel = np.zeros((n, 3), dtype=np.float32)
+        r = np.ascontiguousarray(radius, dtype=np.float32)
+        lib().orc_contact_substep_f32(c_int32(n), P(pos), P(r), f32(cell_size), c_int32(dim), f32(query_radius),
+                                      f32(rate), f32(dt), P(vel), P(nc))
+    return vel, nc
+
+
+@dataclass(frozen=True)
+class Geometry:
+    origin: tuple
+    dx: float
+    shape: tuple
+
+    @property
+    def nodes(self) -> int:
+        return int(np.prod(self.shape))
+
+
+def deposit(geom: Geometry, pos: np.ndarray, state: np.ndarray, acc: np.ndarray | None = None) -> np.ndarray:
+    """int64 accumulator (4, nx, ny, nz) of trilinear fixed-point weights (added to ``acc``)."""
+    nx, ny, nz = geom.shape
+    if acc is None:
+        acc = np.zeros((4, nx, ny, nz), dtype=np.int64)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    state = np.ascontiguousarray(state, dtype=np.int32)
+    o = geom.origin
+    lib().orc_deposit(c_int32(nx), c_int32(ny), c_int32(nz), f32(o[0]), f32(o[1]), f32(o[2]), f32(1.0 / geom.dx),
+                      c_int32(pos.shape[0]), P(pos), P(state), P(acc))
+    return acc
+
+
+def density_convert(geom: Geometry, acc: np.ndarray, weights=None):
+    dens = np.zeros((4,) + tuple(geom.shape), dtype=np.float32)
+    comb = None
+    w = None
+    if weights is not None:
+        w = np.ascontiguousarray(weights, dtype=np.float32)
+        comb = np.zeros(tuple(geom.shape), dtype=np.float32)
+    lib().orc_density_convert(c_int64(geom.nodes), P(acc), f32(1.0 / geom.dx**3), P(dens), P(w), P(comb))
+    return dens, comb
+
+
+def combine(density: np.ndarray, weights) -> np.ndarray:
+    w = [np.float32(x) for x in weights]
+    return ((w[0] * density[0] + w[1] * density[1]) + w[2] * density[2]) + w[3] * density[3]
+
+
+def sample(geom: Geometry, field_values: np.ndarray, pos: np.ndarray, fp64: bool = False) -> np.ndarray:
+    nx, ny, nz = geom.shape
+    o = geom.origin
+    n = pos.shape[0]
+    if fp64:
+        f = np.ascontiguousarray(field_values, dtype=np.float64)
+        p = np.ascontiguousarray(pos, dtype=np.float64)
+        out = np.zeros(n, dtype=np.float64)
+        lib().orc_sample_f64(c_int32(nx), c_int32(ny), c_int32(nz), c_double(o[0]), c_double(o[1]), c_double(o[2]),
+                             c_double(1.0 / geom.dx), P(f), c_int32(n), P(p), P(out))
+    else:
+        f = np.ascontiguousarray(field_values, dtype=np.float32)
+        p = np.ascontiguousarray(pos, dtype=np.float32)
+        out = np.zeros(n, dtype=np.float32)
+        lib().orc_sample_f32(c_int32(nx), c_int32(ny), c_int32(nz), f32(o[0]), f32(o[1]), f32(o[2]),
+                             f32(1.0 / geom.dx), P(f), c_int32(n), P(p), P(out))
+    return out
+
+
+def sor_params(geom: Geometry, boundary, boundary_value: float, diffusion: float, uptake_max: float,
+               michaelis_k: float, omega: float, has_source: int = 0, source_k: float = 1.0) -> SorParams:
+    nx, ny, nz = geom.shape
+    reference = boundary_value if boundary_value > 0.0 else 1.0
+    return SorParams(nx=nx, ny=ny, nz=nz, bc_x=int(boundary[0]), bc_y=int(boundary[1]), bc_z=int(boundary[2]),
+                     omega=omega, dx2_over_D=geom.dx**2 / diffusion, uptake_max=uptake_max, michaelis_k=michaelis_k,
+                     reference=reference, has_source=has_source, source_k=source_k)
+
+
+def sor_sweeps(params: SorParams, sweeps: int, fixed: np.ndarray, density: np.ndarray, values: np.ndarray,
+               production: np.ndarray | None = None, source: np.ndarray | None = None, residual: bool = True,
+               fp64: bool = False) -> float | None:
+    """``sweeps`` red-black sweeps in place on ``values``; returns the residual when asked."""
+    fixed = np.ascontiguousarray(fixed, dtype=np.int32)
+    if fp64:
+        res = np.zeros(1, dtype=np.float64)
+        lib().orc_sor_sweeps_f64(ctypes.byref(params), c_int32(sweeps), P(fixed), P(density), P(production),
+                                 P(source), P(values), P(res) if residual else None)
+    else:
+        res = np.zeros(1, dtype=np.float32)
+        lib().orc_sor_sweeps_f32(ctypes.byref(params), c_int32(sweeps), P(fixed), P(density), P(production),
+                                 P(source), P(values), P(res) if residual else None)
+    return float(res[0]) if residual else None
+
+
+def ftcs_step(params: SorParams, dt: float, fixed: np.ndarray, density: np.ndarray, values: np.ndarray,
+              production=None, source=None) -> np.ndarray:
+    out = np.empty_like(values)
+    lib().orc_ftcs_step_f32(ctypes.byref(params), f32(dt), P(np.ascontiguousarray(fixed, dtype=np.int32)),
+                            P(density), P(production), P(source), P(values), P(out))
+    return out
+
+
+def solve_steady_state(params: SorParams, settings, fixed, density, values, production=None, source=None,
+                       fp64: bool = False):
+    """Reference stopping rule: chunks of ``check_every`` sweeps, residual after each chunk."""
+    sweeps = 0
+    residual = float("inf")
+    while sweeps < settings.max_sweeps:
+        chunk = min(settings.check_every, settings.max_sweeps - sweeps)
+        residual = sor_sweeps(params, chunk, fixed, density, values, production, source, True, fp64)
+        sweeps += chunk
+        if residual < settings.tolerance:
+            return sweeps, residual, True
+    return sweeps, residual, False
+
+
+def lifecycle_params(params, dt: float) -> LifecycleParamsC:
+    return LifecycleParamsC(dt=dt, death_rate=params.death_rate, anoxic_death_rate=params.anoxic_death_rate,
+                            division_rate=params.division_rate,
+                            inhibition_threshold=min(int(params.inhibition_threshold), 2**31 - 1),
+                            hypoxia_threshold=params.hypoxia_threshold, death_threshold=params.death_threshold,
+                            glucose_threshold=params.glucose_threshold,
+                            glucose_death_threshold=params.glucose_death_threshold,
+                            necrosis_requires_glucose=1 if params.necrosis_requires_glucose else 0,
+                            phenotype_model=1 if params.phenotype_model == "network" else 0,
+                            apoptosis_rate=params.apoptosis_rate, necrosis_rate=params.necrosis_rate)
+
+
+def program(arrays: dict, n_nodes: int) -> tuple[ProgramC, list]:
+    keep = [np.ascontiguousarray(arrays[k], dtype=np.int32) for k in ("ops", "args", "start", "length", "updatable")]
+    p = ProgramC(n_nodes=n_nodes, n_words=(n_nodes + 63) // 64, n_ops=keep[0].size, n_updatable=keep[4].size,
+                 ops=P(keep[0]), args=P(keep[1]), start=P(keep[2]), length=P(keep[3]), updatable=P(keep[4]))
+    return p, keep
+
+
+# ---- whole-step mirror --------------------------------------------------------------------------------
+@dataclass
+class OracleSim:
+    """numpy mirror of a population (capacity-sized arrays) plus its optional fields and network."""
+
+    capacity: int
+    count: int
+    seed: int
+    position: np.ndarray
+    radius: np.ndarray
+    cell_state: np.ndarray
+    cell_type: np.ndarray
+    age: np.ndarray
+    oxygen_local: np.ndarray
+    glucose_local: np.ndarray
+    rng_state: np.ndarray
+    velocity: np.ndarray
+    neighbor_count: np.ndarray
+    divide_flag: np.ndarray
+    division_offset: np.ndarray
+    fate_flags: np.ndarray
+    extra_local: dict = field(default_factory=dict)
+
+    @classmethod
+    def from_numpy(cls, positions, radii, capacity=None, seed=0, states=None) -> OracleSim:
+        positions = np.asarray(positions, dtype=np.float32)
+        n = positions.shape[0]
+        cap = n if capacity is None else int(capacity)
+
+        def padded(v, dtype, fill=0):
+            buf = np.full((cap,) + np.shape(v)[1:], fill, dtype=dtype)
+            buf[:n] = v
+            return buf
+
+        if states is None:
+            states = np.zeros(n, dtype=np.int32)
+        return cls(capacity=cap, count=n, seed=int(seed), position=padded(positions, np.float32),
+                   radius=padded(np.asarray(radii, np.float32), np.float32),
+                   cell_state=padded(np.asarray(states, np.int32), np.int32, 3),
+                   cell_type=np.zeros(cap, np.int32), age=np.zeros(cap, np.float32),
+                   oxygen_local=np.zeros(cap, np.float32), glucose_local=np.zeros(cap, np.float32),
+                   rng_state=rng_init(seed, cap), velocity=np.zeros((cap, 3), np.float32),
+                   neighbor_count=np.zeros(cap, np.int32), divide_flag=np.zeros(cap, np.int32),
+                   division_offset=np.zeros(cap, np.int32), fate_flags=np.zeros(cap, np.int32))
+
+    def local_field(self, name: str) -> np.ndarray:
+        if name == "oxygen":
+            return self.oxygen_local
+        if name == "glucose":
+            return self.glucose_local
+        if name not in self.extra_local:
+            self.extra_local[name] = np.zeros(self.capacity, np.float32)
+        return self.extra_local[name]
+
+    # mechanics (cells/mechanics.py:75-122)
+    def contact_substep(self, cell_size: float, dim: int, query_radius: float, rate: float, dt: float) -> None:
+        n = self.count
+        if n == 0:
+            return
+        pos = np.ascontiguousarray(self.position[:n])
+        vel, nc = contact_substep(pos, self.radius[:n], cell_size, dim, query_radius, rate, dt)
+        self.position[:n] = pos
+        self.velocity[:n] = vel
+        self.neighbor_count[:n] = nc
+
+    # lifecycle (cells/lifecycle.py:96-179)
+    def decide_lifecycle(self, params, dt: float) -> None:
+        n = self.count
+        if n == 0:
+            return
+        lib().orc_lifecycle_decide(ctypes.byref(lifecycle_params(params, dt)), c_int32(n), P(self.cell_state),
+                                   P(self.age), P(self.neighbor_count), P(self.oxygen_local), P(self.glucose_local),
+                                   P(self.fate_flags), P(self.rng_state), P(self.divide_flag))
+
+    def commit_divisions(self, params) -> int:
+        n = self.count
+        if n == 0:
+            return 0
+        total = int(lib().orc_division_scan(c_int32(n), P(self.divide_flag), P(self.division_offset)))
+        if total == 0:
+            return 0
+        if n + total > self.capacity:
+            raise OverflowError("capacity exceeded")
+        lib().orc_place_daughters(c_int32(n), f32(params.placement_factor), P(self.divide_flag),
+                                  P(self.division_offset), P(self.position), P(self.radius), P(self.cell_state),
+                                  P(self.cell_type), P(self.age), P(self.oxygen_local), P(self.glucose_local),
+                                  P(self.rng_state), P(self.velocity), P(self.neighbor_count), P(self.fate_flags))
+        self.count = n + total
+        return total
+
+
+@dataclass
+class OracleSpecies:
+    """Mirror of one SpeciesField (fields/species.py:95-195) on an OracleSim."""
+
+    geom: Geometry
+    boundary: tuple
+    boundary_value: float
+    diffusion: float
+    uptake_max: tuple
+    michaelis_k: float
+    settings: object
+    production: tuple = (0.0, 0.0, 0.0, 0.0)
+    name: str = "oxygen"
+    values: np.ndarray = None
+    fixed: np.ndarray = None
+
+    def __post_init__(self):
+        shape = tuple(self.geom.shape)
+        self.values = np.full(shape, np.float32(self.boundary_value), dtype=np.float32)
+        if self.fixed is None:
+            self.fixed = np.zeros(shape, dtype=np.int32)
+        self.density = np.zeros(shape, np.float32)
+        self.prod = np.zeros(shape, np.float32)
+
+    @property
+    def uptake_scale(self) -> float:
+        return max(self.uptake_max) if max(self.uptake_max) > 0.0 else 0.0
+
+    @property
+    def uptake_weights(self):
+        s = self.uptake_scale
+        return tuple(u / s if s > 0.0 else 0.0 for u in self.uptake_max)
+
+    @property
+    def produces(self) -> bool:
+        return max(self.production) > 0.0
+
+    def combine(self, densities: np.ndarray) -> None:
+        self.density = combine(densities, self.uptake_weights)
+        if self.produces:
+            self.prod = combine(densities, self.production)
+
+    def solve(self, source=None, source_k: float = 1.0):
+        p = sor_params(self.geom, self.boundary, self.boundary_value, self.diffusion, self.uptake_scale,
+                       self.michaelis_k, self.settings.omega, 1 if source is not None else 0, source_k)
+        return solve_steady_state(p, self.settings, self.fixed, self.density, self.values,
+                                  self.prod if self.produces else None, source)
+
+    def sample_into(self, sim: OracleSim, out: np.ndarray) -> None:
+        n = sim.count
+        out[:n] = sample(self.geom, self.values, sim.position[:n])
+
+
+def cell_step(sim: OracleSim, lifecycle, contact, dt_cells: float, dt_mechanics: float, species: OracleSpecies | None = None,
+              dim: int = 128):
+    """Mirror of simulation/simulator.py:58-81 (no network) on an OracleSim; returns
+    (daughters, (sweeps, residual, converged) or None). ``contact`` needs ``query_radius`` and
+    ``rate`` (a ContactParams)."""
+    report = None
+    if species is not None:
+        n = sim.count
+        acc = deposit(species.geom, sim.position[:n], sim.cell_state[:n])
+        dens, _ = density_convert(species.geom, acc)
+        species.combine(dens)
+        report = species.solve()
+        species.sample_into(sim, sim.oxygen_local)
+    sim.decide_lifecycle(lifecycle, dt_cells)
+    daughters = sim.commit_divisions(lifecycle)
+    substeps = max(1, int(round(dt_cells / dt_mechanics)))
+    for _ in range(substeps):
+        sim.contact_substep(contact.query_radius, dim, contact.query_radius, contact.rate, dt_mechanics)
+    return daughters, report

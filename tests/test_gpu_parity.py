@@ -1,0 +1,422 @@
+"""GPU parity: the CUDA path (Python drop-in API -> C-ABI -> sm_103a kernels) against the CPU
+oracle on the same seeded inputs, bit for bit where the reference's algorithm is order
+independent or its order is fixed (integer deposits, neighbour sets, lifecycle decisions,
+slots, network states, SOR sweeps, positions), and against the reference's golden vectors and
+closed forms with the reference's own tolerances. Every test is marked ``gpu``.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as orc
+from warpbiocell_gb300 import _lib
+from warpbiocell_gb300.cells.initialization import spherical_cluster, uniform_ball
+from warpbiocell_gb300.cells.lifecycle import CapacityError, LifecycleParams, lifecycle_step
+from warpbiocell_gb300.cells.mechanics import ContactParams, contact_substep, make_neighbor_grid, relax_contacts
+from warpbiocell_gb300.cells.model import CellState
+from warpbiocell_gb300.cells.state import CellPopulation
+from warpbiocell_gb300.fields.densities import CellDensities
+from warpbiocell_gb300.fields.diffusion import SolverSettings
+from warpbiocell_gb300.fields.oxygen import OxygenField, OxygenParams
+from warpbiocell_gb300.fields.scalar_field import Boundary, GridGeometry
+from warpbiocell_gb300.metrics.population import state_counts
+from warpbiocell_gb300.simulation.simulator import TimeStepping, cell_step
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda:0"
+R = 8.0
+MIXED = (Boundary.DIRICHLET, Boundary.NEUMANN, Boundary.DIRICHLET)
+
+
+def _t(a, dtype=None):
+    return torch.as_tensor(np.ascontiguousarray(a), device=DEV) if dtype is None else torch.as_tensor(
+        np.ascontiguousarray(a), dtype=dtype, device=DEV)
+
+
+def _stream():
+    return _lib.stream(torch.device(DEV))
+
+
+# ---- random streams, exp ------------------------------------------------------------------------------
+def test_streams_draws_and_directions_match_oracle():
+    pop = CellPopulation.from_numpy(np.zeros((1000, 3), np.float32), np.full(1000, R), capacity=4096, device=DEV, seed=17)
+    np.testing.assert_array_equal(pop.rng_state.cpu().numpy().view(np.uint32), orc.rng_init(17, 4096))
+    state = pop.rng_state.clone()
+    out = torch.zeros((4096, 8), dtype=torch.float32, device=DEV)
+    _lib.call("wbc_rng_uniform", 4096, 8, _lib.ptr(state), _lib.ptr(out), _stream())
+    ref_state = orc.rng_init(17, 4096)
+    np.testing.assert_array_equal(out.cpu().numpy(), orc.rng_uniform(ref_state, 8))
+    np.testing.assert_array_equal(state.cpu().numpy().view(np.uint32), ref_state)
+    dirs = torch.zeros((4096, 3), dtype=torch.float32, device=DEV)
+    _lib.call("wbc_rng_sphere", 4096, _lib.ptr(state), _lib.ptr(dirs), _stream())
+    np.testing.assert_array_equal(dirs.cpu().numpy(), orc.rng_sphere(ref_state))
+
+
+def test_project_exp_matches_oracle_and_cuda_expf():
+    x = np.concatenate([np.linspace(-103.9, 88.7, 100001), -np.logspace(-8, 3, 10001)]).astype(np.float32)
+    xt = _t(x)
+    out = torch.empty_like(xt)
+    _lib.call("wbc_expf_batch", x.size, _lib.ptr(xt), _lib.ptr(out), _stream())
+    got = out.cpu().numpy()
+    np.testing.assert_array_equal(got, orc.expf(x))
+    cuda = torch.exp(xt).cpu().numpy().astype(np.float64)  # CUDA's expf (max error 2 ulp)
+    normal = cuda > 1.2e-38
+    ulp = np.spacing(cuda[normal].astype(np.float32)).astype(np.float64)
+    assert (np.abs(got[normal] - cuda[normal]) / ulp).max() <= 3.0
+
+
+# ---- deposit / density / sample -------------------------------------------------------------------------
+def _pop_from(pos, states=None, capacity=None, seed=0, radii=None):
+    n = pos.shape[0]
+    radii = np.full(n, R, np.float32) if radii is None else radii
+    return CellPopulation.from_numpy(pos, radii, capacity=capacity, device=DEV, seed=seed, states=states)
+
+
+def test_deposit_bitwise_equals_oracle_and_golden(golden):
+    g = golden("deposit")
+    geom = GridGeometry(tuple(g["origin"]), float(g["dx"]), tuple(int(x) for x in g["shape"]))
+    pop = _pop_from(g["positions"], g["states"])
+    dens = CellDensities(geom, device=DEV)
+    dens.deposit_fixed_point(pop)
+    acc_gpu = dens.accumulator.cpu().numpy()
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    acc_ref = orc.deposit(ogeom, g["positions"], g["states"])
+    np.testing.assert_array_equal(acc_gpu, acc_ref)
+    dens.convert()
+    d_ref, _ = orc.density_convert(ogeom, acc_ref)
+    np.testing.assert_array_equal(dens.numpy(), d_ref)
+    np.testing.assert_allclose(dens.numpy(), g["density"], atol=1e-8)
+    assert int(dens.accumulator.abs().sum().item()) == 0  # cleared by the conversion
+
+
+def test_deposit_large_is_order_independent_and_reproducible():
+    pos = uniform_ball(200000, 600.0, seed=3)
+    states = np.random.default_rng(3).integers(0, 4, 200000).astype(np.int32)
+    geom = GridGeometry.centered_cube(1200.0, 15.0)
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    ref = orc.deposit(ogeom, pos, states)
+    for perm_seed in (None, 1):
+        p, s = pos, states
+        if perm_seed is not None:
+            perm = np.random.default_rng(perm_seed).permutation(len(states))
+            p, s = pos[perm], states[perm]
+        dens = CellDensities(geom, device=DEV)
+        dens.deposit_fixed_point(_pop_from(p, s))
+        np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), ref)
+
+
+def test_fused_convert_combine_equals_separate_passes():
+    pos = uniform_ball(20000, 200.0, seed=4)
+    states = np.random.default_rng(4).integers(0, 4, 20000).astype(np.int32)
+    geom = GridGeometry.centered_cube(500.0, 20.0)
+    ox = OxygenField(geom, OxygenParams(), device=DEV, uptake_state_factors={"hypoxic": 0.5})
+    pop = _pop_from(pos, states)
+    ox.deposit_uptake(pop)
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    d_ref, _ = orc.density_convert(ogeom, orc.deposit(ogeom, pos, states))
+    np.testing.assert_array_equal(ox.densities.numpy(), d_ref)
+    np.testing.assert_array_equal(ox.density.cpu().numpy(), orc.combine(d_ref, ox.species.uptake_weights))
+
+
+def test_sample_bitwise_equals_oracle_and_matches_golden(golden):
+    g = golden("sample")
+    geom = GridGeometry(tuple(g["origin"]), float(g["dx"]), g["field"].shape)
+    ox = OxygenField(geom, OxygenParams(), boundary=(Boundary.NEUMANN,) * 3, device=DEV)
+    ox.field.values.copy_(_t(g["field"]))
+    pop = _pop_from(g["positions"])
+    ox.sample_at_cells(pop)
+    got = pop.oxygen_numpy()
+    np.testing.assert_array_equal(got, orc.sample(orc.Geometry(geom.origin, geom.dx, geom.shape), g["field"], g["positions"]))
+    np.testing.assert_allclose(got, g["expected"], rtol=1e-5, atol=1e-5)
+
+
+def test_sampling_is_exact_for_linear_fields():
+    geom = GridGeometry.centered_cube(200.0, 25.0)
+    ox = OxygenField(geom, OxygenParams(), boundary=(Boundary.NEUMANN,) * 3, device=DEV)
+    x, y, z = np.meshgrid(*geom.node_coordinates(), indexing="ij")
+    ox.field.assign(3.0 + 0.1 * x - 0.05 * y + 0.02 * z)
+    pos = np.random.default_rng(1).uniform(-90.0, 90.0, size=(200, 3)).astype(np.float32)
+    pop = _pop_from(pos)
+    ox.sample_at_cells(pop)
+    np.testing.assert_allclose(pop.oxygen_numpy(), 3.0 + 0.1 * pos[:, 0] - 0.05 * pos[:, 1] + 0.02 * pos[:, 2], atol=1e-4)
+
+
+# ---- SOR ------------------------------------------------------------------------------------------------------
+def _oracle_params(field, kin, omega, has_source=0, source_k=1.0):
+    g = field.geometry
+    return orc.sor_params(orc.Geometry(g.origin, g.dx, g.shape), field.boundary_flags, field.boundary_value,
+                          kin.diffusion, kin.uptake_max, kin.michaelis_k, omega, has_source, source_k)
+
+
+@pytest.mark.parametrize("sweeps", [1, 7, 40])
+def test_sor_sweeps_bitwise_equal_oracle_with_production_source_and_pins(sweeps):
+    from warpbiocell_gb300.fields.diffusion import sor_chunk, sor_params
+
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=12.0, shape=(23, 19, 17))
+    ox = OxygenField(geom, OxygenParams(boundary_value=30.0), boundary=MIXED, device=DEV)
+    rng = np.random.default_rng(sweeps)
+    pins = rng.random(geom.shape) < 0.03
+    ox.field.set_fixed(pins)
+    ox.field.assign(rng.uniform(0.0, 40.0, geom.shape).astype(np.float32))
+    density = rng.uniform(0.0, 3e-3, geom.shape).astype(np.float32)
+    production = rng.uniform(0.0, 30.0, geom.shape).astype(np.float32)
+    source = rng.uniform(0.0, 5.0, geom.shape).astype(np.float32)
+    kin = ox.species.kinetics
+    start = ox.numpy()
+    res = torch.zeros(1, dtype=torch.float32, device=DEV)
+    p = sor_params(ox.field, kin, 1.8, 1, 0.04)
+    sor_chunk(ox.field, _t(density), p, sweeps, res, _t(production), _t(source))
+    values = start.copy()
+    r_ref = orc.sor_sweeps(_oracle_params(ox.field, kin, 1.8, 1, 0.04), sweeps, pins.astype(np.int32), density, values,
+                           production, source)
+    np.testing.assert_array_equal(ox.numpy(), values)
+    assert float(res.item()) == np.float32(r_ref)
+
+
+def test_steady_state_matches_exact_discrete_solution(golden):
+    g = golden("steady_state")
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=(8, 7, 6))
+    params = OxygenParams(diffusion_coefficient=2.0e3, uptake_max=5.0e4, michaelis_k=3.0, boundary_value=20.0)
+    settings = SolverSettings(omega=1.5, tolerance=1e-5, max_sweeps=20000, check_every=10)
+    ox = OxygenField(geom, params, settings, boundary=MIXED, device=DEV)
+    ox.density.copy_(_t(g["density1"]))
+    report = ox.solve_steady_state()
+    assert report.converged
+    np.testing.assert_allclose(ox.numpy(), g["exact1"], atol=2e-3)
+    values = np.full(geom.shape, np.float32(20.0))
+    sweeps, res, ok = orc.solve_steady_state(_oracle_params(ox.field, params.kinetics, 1.5), settings,
+                                             np.zeros(geom.shape, np.int32), g["density1"], values)
+    assert (report.sweeps, ok) == (sweeps, True) and report.residual == np.float32(res)
+    np.testing.assert_array_equal(ox.numpy(), values)
+
+
+def test_steady_state_field_within_1e5_relative_of_fp64():
+    """The converged float32 field against an FP64 solve of the same discrete problem."""
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=4000, check_every=10)
+    ox = OxygenField(geom, OxygenParams(), settings, device=DEV)
+    x, y, z = np.meshgrid(*geom.node_coordinates(), indexing="ij")
+    density = np.where(x**2 + y**2 + z**2 < 150.0**2, 2.4e-4, 0.0).astype(np.float32)
+    ox.density.copy_(_t(density))
+    ox.solve_steady_state()
+    v64 = np.full(geom.shape, 38.0)
+    orc.solve_steady_state(_oracle_params(ox.field, ox.species.kinetics, 1.8),
+                           SolverSettings(omega=1.8, tolerance=1e-13, max_sweeps=20000, check_every=10),
+                           np.zeros(geom.shape, np.int32), density.astype(np.float64), v64, fp64=True)
+    rel = np.abs(ox.numpy() - v64) / np.maximum(np.abs(v64), 1.0)
+    assert rel.max() < 1e-5, rel.max()
+
+
+def test_warm_start_needs_one_check_and_uniform_stays_uniform():
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    ox = OxygenField(geom, OxygenParams(), SolverSettings(omega=1.8, tolerance=1e-5, check_every=10), device=DEV)
+    x, y, z = np.meshgrid(*geom.node_coordinates(), indexing="ij")
+    ox.density.copy_(_t(np.where(x**2 + y**2 + z**2 < 150.0**2, 2.4e-4, 0.0).astype(np.float32)))
+    first, second = ox.solve_steady_state(), ox.solve_steady_state()
+    assert first.converged and second.converged and first.sweeps > 20 and second.sweeps == 10
+    flat = OxygenField(geom, OxygenParams(boundary_value=40.0), device=DEV)
+    flat.solve_steady_state()
+    np.testing.assert_array_equal(flat.numpy(), 40.0)
+
+
+# ---- mechanics ------------------------------------------------------------------------------------------------
+def test_neighbor_counts_match_brute_force_and_positions_match_oracle(golden):
+    g = golden("contact")
+    params = ContactParams(stiffness=10.0, damping=1.0, max_radius=9.0, margin=0.5)
+    pop = _pop_from(g["positions"], radii=g["radii"])
+    grid = make_neighbor_grid(params, DEV)
+    contact_substep(pop, grid, params, dt=0.0)
+    np.testing.assert_array_equal(pop.neighbor_counts_numpy(), g["counts"])
+    np.testing.assert_allclose(pop.velocity[: pop.count].cpu().numpy(), g["velocities"], atol=2e-4)
+    ref = g["positions"].copy()
+    pop = _pop_from(g["positions"], radii=g["radii"])
+    for step in range(1, 21):
+        contact_substep(pop, grid, params, dt=0.01)
+        orc.contact_substep(ref, g["radii"], params.query_radius, 128, params.query_radius, params.rate, 0.01)
+        np.testing.assert_array_equal(pop.positions_numpy(), ref)  # canonical order: same bits
+        np.testing.assert_allclose(pop.positions_numpy(), g["trajectory"][step], atol=2e-3)
+
+
+def test_mechanics_laws():
+    # single cell stays put; isolated cells have no contacts; only the active prefix is indexed
+    pos = np.array([[3.0, -2.0, 5.0]], np.float32)
+    pop = _pop_from(pos)
+    params = ContactParams(stiffness=10.0, damping=1.0, max_radius=8.0)
+    relax_contacts(pop, make_neighbor_grid(params, DEV), params, dt=0.01, substeps=50)
+    np.testing.assert_array_equal(pop.positions_numpy(), pos)
+    pop = _pop_from(np.array([[0.0, 0, 0], [1.0, 0, 0]], np.float32), capacity=50)
+    contact_substep(pop, make_neighbor_grid(params, DEV), params, dt=0.0)
+    np.testing.assert_array_equal(pop.neighbor_counts_numpy(), [1, 1])
+    # pair overlap decays as (1 - 2 rate dt)^n and the midpoint stays put
+    pop = _pop_from(np.array([[0.0, 0, 0], [13.0, 0, 0]], np.float32))
+    relax_contacts(pop, make_neighbor_grid(params, DEV), params, dt=0.01, substeps=15)
+    x = pop.positions_numpy()
+    assert 16.0 - np.linalg.norm(x[1] - x[0]) == pytest.approx(3.0 * (1.0 - 0.2) ** 15, rel=1e-3)
+    np.testing.assert_allclose(x[0] + x[1], [13.0, 0.0, 0.0], atol=1e-4)
+    # centre of mass conserved in a compressed cluster
+    pos = spherical_cluster(1500, R, spacing_factor=0.85, jitter=0.2, seed=2)
+    pop = _pop_from(pos)
+    com = pos.astype(np.float64).mean(0)
+    relax_contacts(pop, make_neighbor_grid(params, DEV), params, dt=0.01, substeps=100)
+    np.testing.assert_allclose(pop.positions_numpy().astype(np.float64).mean(0), com, atol=1e-3)
+
+
+def test_contact_displacement_within_1e5_um_of_fp64():
+    pos = uniform_ball(50000, 300.0, seed=5)
+    radii = np.clip(np.random.default_rng(5).normal(8.0, 0.8, 50000), 6, 10).astype(np.float32)
+    params = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0)
+    pop = _pop_from(pos, radii=radii)
+    grid = make_neighbor_grid(params, DEV)
+    for _ in range(3):
+        before = pop.positions_numpy()
+        contact_substep(pop, grid, params, dt=0.1)
+        after = pop.positions_numpy()
+        p64 = before.astype(np.float64)
+        vel64, nc = orc.contact_substep(p64, radii, params.query_radius, 128, params.query_radius, params.rate, 0.1,
+                                        fp64=True)
+        np.testing.assert_array_equal(pop.neighbor_counts_numpy(), nc)
+        v32 = pop.velocity[: pop.count].cpu().numpy().astype(np.float64)
+        assert np.abs(v32 * 0.1 - vel64 * 0.1).max() < 1e-5  # per-step displacement
+        ulp = np.spacing(np.abs(before)).astype(np.float64)
+        assert np.all(np.abs(after - (before + vel64 * 0.1)) <= 1e-5 + ulp)
+
+
+# ---- lifecycle --------------------------------------------------------------------------------------------
+def _lp(**kw):
+    return LifecycleParams(**kw)
+
+
+def _compare_pop(pop, sim):
+    n = pop.count
+    assert n == sim.count
+    np.testing.assert_array_equal(pop.positions_numpy(), sim.position[:n])
+    np.testing.assert_array_equal(pop.states_numpy(), sim.cell_state[:n])
+    np.testing.assert_array_equal(pop.ages_numpy(), sim.age[:n])
+    np.testing.assert_array_equal(pop.rng_numpy(), sim.rng_state[:n])
+    np.testing.assert_array_equal(pop.neighbor_counts_numpy(), sim.neighbor_count[:n])
+    np.testing.assert_array_equal(pop.oxygen_numpy(), sim.oxygen_local[:n])
+
+
+@pytest.mark.parametrize("mode", ["rules", "network"])
+def test_lifecycle_decide_scan_place_bitwise_equal_oracle(mode):
+    n = 30000
+    pos = uniform_ball(n, 400.0, seed=6)
+    rng = np.random.default_rng(6)
+    states = rng.integers(0, 4, n).astype(np.int32)
+    pop = _pop_from(pos, states, capacity=3 * n, seed=6)
+    sim = orc.OracleSim.from_numpy(pos, np.full(n, R), capacity=3 * n, seed=6, states=states)
+    o2 = rng.uniform(0.0, 12.0, n).astype(np.float32)
+    glc = rng.uniform(0.0, 6.0, n).astype(np.float32)
+    nc = rng.integers(0, 12, n).astype(np.int32)
+    flags = rng.integers(0, 16, n).astype(np.int32)
+    for t, a in ((pop.oxygen_local, o2), (pop.glucose_local, glc), (pop.neighbor_count, nc), (pop.fate_flags, flags)):
+        t[:n] = _t(a)
+    sim.oxygen_local[:n], sim.glucose_local[:n], sim.neighbor_count[:n], sim.fate_flags[:n] = o2, glc, nc, flags
+    params = _lp(division_rate=0.7, death_rate=0.05, anoxic_death_rate=0.5, inhibition_threshold=8,
+                 hypoxia_threshold=5.0, death_threshold=1.0, glucose_threshold=4.0, glucose_death_threshold=0.5,
+                 necrosis_requires_glucose=True, phenotype_model=mode, apoptosis_rate=0.3, necrosis_rate=2.0)
+    created = lifecycle_step(pop, params, dt=1.0)
+    sim.decide_lifecycle(params, 1.0)
+    assert created == sim.commit_divisions(params) and created > 1000
+    _compare_pop(pop, sim)
+    np.testing.assert_array_equal(pop.division_offset[:n].cpu().numpy(), sim.division_offset[:n])
+    np.testing.assert_array_equal(pop.fate_flags_numpy(), sim.fate_flags[: pop.count])
+
+
+def test_every_cell_divides_exactly_once_and_capacity_overflow_places_nothing():
+    n = 300
+    pos = spherical_cluster(n, R, spacing_factor=1.0, jitter=0.1, seed=0)
+    pop = _pop_from(pos, capacity=3 * n)
+    params = _lp(division_rate=1.0e3, inhibition_threshold=10**6)
+    assert lifecycle_step(pop, params, dt=1.0) == n and pop.count == 2 * n
+    x = pop.positions_numpy()
+    np.testing.assert_allclose(np.linalg.norm(x[n:] - x[:n], axis=1), R, rtol=1e-5)
+    np.testing.assert_allclose(0.5 * (x[n:] + x[:n]), pos, atol=1e-5)
+    assert np.all(pop.ages_numpy()[:n] == 1.0) and np.all(pop.ages_numpy()[n:] == 0.0)
+    assert np.all(pop.cell_state[2 * n:].cpu().numpy() == int(CellState.DEAD))
+    pop = _pop_from(pos[:50], capacity=60)
+    before = pop.positions_numpy()
+    with pytest.raises(CapacityError):
+        lifecycle_step(pop, params, dt=1.0)
+    assert pop.count == 50
+    np.testing.assert_array_equal(pop.positions_numpy(), before)
+    assert np.all(pop.position[50:].cpu().numpy() == 0.0)
+
+
+def test_certain_death_and_death_statistics():
+    pop = _pop_from(spherical_cluster(100, R, seed=0), capacity=300)
+    assert lifecycle_step(pop, _lp(division_rate=1e3, death_rate=1e3, inhibition_threshold=10**6), dt=1.0) == 0
+    assert state_counts(pop)[CellState.DEAD] == 100
+    n = 20000
+    pop = _pop_from(np.zeros((n, 3), np.float32))
+    lifecycle_step(pop, _lp(division_rate=0.0, death_rate=0.05, inhibition_threshold=10**6), dt=1.0)
+    p = 1.0 - np.exp(-0.05)
+    assert abs(state_counts(pop)[CellState.DEAD] / n - p) < 4.0 * np.sqrt(p * (1 - p) / n)
+
+
+def test_contact_inhibition_makes_crowded_cells_quiescent():
+    cluster = spherical_cluster(400, R, spacing_factor=1.0, jitter=0.05, seed=3)
+    pos = np.vstack([cluster, [[500.0, 0, 0], [0, 500.0, 0], [0, 0, 500.0]]]).astype(np.float32)
+    n = pos.shape[0]
+    pop = _pop_from(pos, capacity=3 * n)
+    contact = ContactParams(stiffness=10.0, damping=1.0, max_radius=R, margin=2.0)
+    contact_substep(pop, make_neighbor_grid(contact, DEV), contact, dt=0.0)
+    crowded = pop.neighbor_counts_numpy() >= 6
+    assert crowded.sum() > 100 and (~crowded).sum() >= 3
+    created = lifecycle_step(pop, _lp(division_rate=1e3, inhibition_threshold=6), dt=1.0)
+    states = pop.states_numpy()[:n]
+    assert np.all(states[crowded] == int(CellState.QUIESCENT)) and np.all(states[~crowded] == 0)
+    assert created == int((~crowded).sum())
+
+
+# ---- whole coupled step ----------------------------------------------------------------------------------------
+def _coupled(seed=0, capacity=12000, n=3000, steps=6):
+    pos = uniform_ball(n, 120.0, seed=seed)
+    radii = np.clip(np.random.default_rng(seed).normal(8.0, 0.8, n), 6, 10).astype(np.float32)
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=2000, check_every=20)
+    oparams = OxygenParams(diffusion_coefficient=7.2e6, uptake_max=5.54e7, michaelis_k=1.0, boundary_value=12.0)
+    lifecycle = LifecycleParams(division_rate=0.2, death_rate=0.01, anoxic_death_rate=0.5, inhibition_threshold=14,
+                                hypoxia_threshold=5.0, death_threshold=1.0)
+    contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0)
+    stepping = TimeStepping(dt_cells=0.25, dt_mechanics=0.125)
+    return pos, radii, geom, settings, oparams, lifecycle, contact, stepping
+
+
+def test_coupled_cell_steps_bitwise_equal_oracle():
+    pos, radii, geom, settings, oparams, lifecycle, contact, stepping = _coupled()
+    pop = CellPopulation.from_numpy(pos, radii, capacity=12000, device=DEV, seed=0)
+    ox = OxygenField(geom, oparams, settings, device=DEV)
+    grid = make_neighbor_grid(contact, DEV)
+    sim = orc.OracleSim.from_numpy(pos, radii, capacity=12000, seed=0)
+    sp = orc.OracleSpecies(orc.Geometry(geom.origin, geom.dx, geom.shape), (0, 0, 0), 12.0, 7.2e6,
+                           ox.species.uptake_max, 1.0, settings)
+    for _ in range(6):
+        rep = cell_step(pop, grid, lifecycle, contact, stepping, oxygen=ox)
+        daughters, (sweeps, residual, ok) = orc.cell_step(sim, lifecycle, contact, stepping.dt_cells,
+                                                          stepping.dt_mechanics, sp)
+        assert rep.daughters == daughters and rep.field_sweeps == sweeps and rep.field_converged == ok
+        assert rep.field_residual == np.float32(residual)
+        np.testing.assert_array_equal(ox.numpy(), sp.values)
+        _compare_pop(pop, sim)
+    assert pop.count > 3000 and state_counts(pop)[CellState.HYPOXIC] > 0
+
+
+def test_coupled_run_is_reproducible_and_independent_of_capacity():
+    pos, radii, geom, settings, oparams, lifecycle, contact, stepping = _coupled(seed=1)
+    snaps = []
+    for capacity in (12000, 12000, 20000):
+        pop = CellPopulation.from_numpy(pos, radii, capacity=capacity, device=DEV, seed=1)
+        ox = OxygenField(geom, oparams, settings, device=DEV)
+        grid = make_neighbor_grid(contact, DEV)
+        for _ in range(4):
+            cell_step(pop, grid, lifecycle, contact, stepping, oxygen=ox)
+        snaps.append((pop.count, pop.positions_numpy(), pop.states_numpy(), ox.numpy()))
+    for s in snaps[1:]:
+        assert s[0] == snaps[0][0]
+        for a, b in zip(s[1:], snaps[0][1:]):
+            np.testing.assert_array_equal(a, b)

@@ -1,0 +1,307 @@
+// Cell <-> grid transfer and the Michaelis-Menten reaction-diffusion solver.
+//
+//   deposit    int64 fixed-point trilinear weights, atomically added (order independent, so the
+//              accumulator is bit-exact whatever the thread order)        field_kernels.py:78-116
+//   convert    acc / 2^24 / dx^3 per state, optional per-species combination and clearing of the
+//              accumulator in the same pass                             field_kernels.py:119-142
+//   sample     clamped trilinear interpolation at the cells             field_kernels.py:153-182
+//   SOR        red-black colour half-sweeps, in place                   field_kernels.py:185-212
+//   residual   max-norm of the dimensionless residual, block-reduced    field_kernels.py:215-243
+//   FTCS       explicit reference step (validation only)                field_kernels.py:246-273
+//
+// Layout: fields are float[nx][ny][nz] with k fastest; the accumulator is int64[4][nodes].
+// Every float expression is evaluated in the reference's order (no contraction, see
+// wbc_common.cuh), so the field after a given number of sweeps is bit-identical to the oracle's.
+#include "wbc_common.cuh"
+
+namespace wbc {
+
+constexpr float kFixedOne = 16777216.0f;  // 2^24
+
+__global__ void k_deposit(wbc_grid_geometry g, int32_t n, const float* __restrict__ position,
+                          const int32_t* __restrict__ cell_state, unsigned long long* __restrict__ acc) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const int s = cell_state[c];
+    if (s < 0 || s >= 4) return;
+    const float* p = position + 3 * static_cast<int64_t>(c);
+    const float ux = (p[0] - g.origin_x) * g.inv_dx;
+    const float uy = (p[1] - g.origin_y) * g.inv_dx;
+    const float uz = (p[2] - g.origin_z) * g.inv_dx;
+    const int i0 = static_cast<int>(floorf(ux));
+    const int j0 = static_cast<int>(floorf(uy));
+    const int k0 = static_cast<int>(floorf(uz));
+    if (i0 < 0 || j0 < 0 || k0 < 0) return;
+    if (i0 + 1 >= g.nx || j0 + 1 >= g.ny || k0 + 1 >= g.nz) return;
+    const float fx = ux - static_cast<float>(i0);
+    const float fy = uy - static_cast<float>(j0);
+    const float fz = uz - static_cast<float>(k0);
+    const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
+    unsigned long long* layer = acc + s * nodes;
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+        const float wx = di == 0 ? 1.0f - fx : fx;
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) {
+            const float wy = dj == 0 ? 1.0f - fy : fy;
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const float wz = dk == 0 ? 1.0f - fz : fz;
+                const float w = wx * wy * wz;
+                const int q = static_cast<int>(w * kFixedOne + 0.5f);
+                const int64_t node = (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + (k0 + dk);
+                atomicAdd(layer + node, static_cast<unsigned long long>(static_cast<long long>(q)));
+            }
+        }
+    }
+}
+
+__global__ void k_convert(int64_t nodes, long long* __restrict__ acc, float inv_vol, float* __restrict__ density,
+                          float w0, float w1, float w2, float w3, float* __restrict__ combined, int clear) {
+    int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (node >= nodes) return;
+    float d[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const long long a = acc[s * nodes + node];
+        d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
+        if (density) density[s * nodes + node] = d[s];
+        if (clear) acc[s * nodes + node] = 0;
+    }
+    if (combined) combined[node] = w0 * d[0] + w1 * d[1] + w2 * d[2] + w3 * d[3];
+}
+
+__global__ void k_combine(int64_t nodes, float w0, float w1, float w2, float w3, const float* __restrict__ density,
+                          float* __restrict__ out) {
+    int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (node >= nodes) return;
+    out[node] = w0 * density[node] + w1 * density[nodes + node] + w2 * density[2 * nodes + node] +
+                w3 * density[3 * nodes + node];
+}
+
+__global__ void k_sample(wbc_grid_geometry g, const float* __restrict__ field, int32_t n,
+                         const float* __restrict__ position, float* __restrict__ out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float* p = position + 3 * static_cast<int64_t>(c);
+    const float ux = (p[0] - g.origin_x) * g.inv_dx;
+    const float uy = (p[1] - g.origin_y) * g.inv_dx;
+    const float uz = (p[2] - g.origin_z) * g.inv_dx;
+    const float cx = fminf(fmaxf(ux, 0.0f), static_cast<float>(g.nx - 1));
+    const float cy = fminf(fmaxf(uy, 0.0f), static_cast<float>(g.ny - 1));
+    const float cz = fminf(fmaxf(uz, 0.0f), static_cast<float>(g.nz - 1));
+    const int i0 = min(static_cast<int>(floorf(cx)), g.nx - 2);
+    const int j0 = min(static_cast<int>(floorf(cy)), g.ny - 2);
+    const int k0 = min(static_cast<int>(floorf(cz)), g.nz - 2);
+    const float fx = cx - static_cast<float>(i0);
+    const float fy = cy - static_cast<float>(j0);
+    const float fz = cz - static_cast<float>(k0);
+    const int64_t sy = g.nz, sx = static_cast<int64_t>(g.ny) * g.nz;
+    const int64_t b = i0 * sx + j0 * sy + k0;
+    const float gx = 1.0f - fx;
+    const float c00 = field[b] * gx + field[b + sx] * fx;
+    const float c10 = field[b + sy] * gx + field[b + sx + sy] * fx;
+    const float c01 = field[b + 1] * gx + field[b + sx + 1] * fx;
+    const float c11 = field[b + sy + 1] * gx + field[b + sx + sy + 1] * fx;
+    const float c0 = c00 * (1.0f - fy) + c10 * fy;
+    const float c1 = c01 * (1.0f - fy) + c11 * fy;
+    out[c] = c0 * (1.0f - fz) + c1 * fz;
+}
+
+// ---- SOR -----------------------------------------------------------------------------------------
+__device__ __forceinline__ bool on_dirichlet_face(const wbc_sor_params& p, int i, int j, int k) {
+    if (p.bc_x == 0 && (i == 0 || i == p.nx - 1)) return true;
+    if (p.bc_y == 0 && (j == 0 || j == p.ny - 1)) return true;
+    if (p.bc_z == 0 && (k == 0 || k == p.nz - 1)) return true;
+    return false;
+}
+
+// Sum of the six neighbours, mirrored at every edge (only reached on Neumann faces).
+__device__ __forceinline__ float neighbor_sum(const float* __restrict__ f, const wbc_sor_params& p, int i, int j,
+                                              int k) {
+    const int im = i - 1 < 0 ? 1 : i - 1;
+    const int ip = i + 1 > p.nx - 1 ? p.nx - 2 : i + 1;
+    const int jm = j - 1 < 0 ? 1 : j - 1;
+    const int jp = j + 1 > p.ny - 1 ? p.ny - 2 : j + 1;
+    const int km = k - 1 < 0 ? 1 : k - 1;
+    const int kp = k + 1 > p.nz - 1 ? p.nz - 2 : k + 1;
+    const int64_t sx = static_cast<int64_t>(p.ny) * p.nz;
+    const int64_t sy = p.nz;
+    const int64_t row = j * sy;
+    const int64_t base = i * sx;
+    return f[im * sx + row + k] + f[ip * sx + row + k] + f[base + jm * sy + k] + f[base + jp * sy + k] +
+           f[base + row + km] + f[base + row + kp];
+}
+
+__device__ __forceinline__ float production_at(const wbc_sor_params& p, const float* __restrict__ production,
+                                               const float* __restrict__ source, int64_t idx) {
+    const float prod = production ? production[idx] : 0.0f;
+    if (!p.has_source) return prod * 1.0f;
+    const float v = source[idx];
+    return prod * (v / (p.source_k + v));
+}
+
+// One colour: thread (i, j, m) updates k = 2m + ((colour + i + j) & 1).
+__global__ void k_sor_colour(wbc_sor_params p, int colour, const int32_t* __restrict__ fixed,
+                             const float* __restrict__ density, const float* __restrict__ production,
+                             const float* __restrict__ source, float* __restrict__ field) {
+    const int half = (p.nz + 1) >> 1;
+    int64_t t = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t total = static_cast<int64_t>(p.nx) * p.ny * half;
+    if (t >= total) return;
+    const int m = static_cast<int>(t % half);
+    const int64_t ij = t / half;
+    const int j = static_cast<int>(ij % p.ny);
+    const int i = static_cast<int>(ij / p.ny);
+    const int k = 2 * m + ((colour + i + j) & 1);
+    if (k >= p.nz) return;
+    const int64_t idx = (static_cast<int64_t>(i) * p.ny + j) * p.nz + k;
+    if (fixed[idx] != 0 || on_dirichlet_face(p, i, j, k)) return;
+    const float o = field[idx];
+    const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
+    const float prod = production_at(p, production, source, idx);
+    const float gs = (neighbor_sum(field, p, i, j, k) + p.dx2_over_D * prod) / (6.0f + p.dx2_over_D * c);
+    field[idx] = fmaxf((1.0f - p.omega) * o + p.omega * gs, 0.0f);
+}
+
+__global__ void k_residual(wbc_sor_params p, const int32_t* __restrict__ fixed, const float* __restrict__ density,
+                           const float* __restrict__ production, const float* __restrict__ source,
+                           const float* __restrict__ field, unsigned int* __restrict__ residual_bits) {
+    const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
+    int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    float val = 0.0f;
+    if (idx < nodes) {
+        const int k = static_cast<int>(idx % p.nz);
+        const int64_t ij = idx / p.nz;
+        const int j = static_cast<int>(ij % p.ny);
+        const int i = static_cast<int>(ij / p.ny);
+        if (fixed[idx] == 0 && !on_dirichlet_face(p, i, j, k)) {
+            const float o = field[idx];
+            const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
+            const float prod = production_at(p, production, source, idx);
+            const float r = neighbor_sum(field, p, i, j, k) + p.dx2_over_D * prod - (6.0f + p.dx2_over_D * c) * o;
+            val = fabsf(r) / fmaxf(6.0f * o, p.reference);
+        }
+    }
+    // Max of non-negative floats = max of their bit patterns; NaN (0x7fc00000) dominates.
+    unsigned int bits = __float_as_uint(val);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
+    __shared__ unsigned int warp_max[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) warp_max[warp] = bits;
+    __syncthreads();
+    if (warp == 0) {
+        bits = lane < (blockDim.x >> 5) ? warp_max[lane] : 0u;
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
+        if (lane == 0) atomicMax(residual_bits, bits);
+    }
+}
+
+__global__ void k_ftcs(wbc_sor_params p, float dt, const int32_t* __restrict__ fixed, const float* __restrict__ density,
+                       const float* __restrict__ production, const float* __restrict__ source,
+                       const float* __restrict__ in, float* __restrict__ out) {
+    const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
+    int64_t idx = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (idx >= nodes) return;
+    const int k = static_cast<int>(idx % p.nz);
+    const int64_t ij = idx / p.nz;
+    const int j = static_cast<int>(ij % p.ny);
+    const int i = static_cast<int>(ij / p.ny);
+    const float o = in[idx];
+    if (fixed[idx] != 0 || on_dirichlet_face(p, i, j, k)) {
+        out[idx] = o;
+        return;
+    }
+    const float D_over_dx2 = p.dx2_over_D;
+    const float lap = D_over_dx2 * (neighbor_sum(in, p, i, j, k) - 6.0f * o);
+    const float uptake = density[idx] * p.uptake_max * o / (p.michaelis_k + o);
+    const float prod = production_at(p, production, source, idx);
+    out[idx] = o + dt * (lap - uptake + prod);
+}
+
+static bool geom_ok(const wbc_grid_geometry* g) { return g && g->nx >= 2 && g->ny >= 2 && g->nz >= 2; }
+
+static bool sor_ok(const wbc_sor_params* p) { return p && p->nx >= 3 && p->ny >= 3 && p->nz >= 3; }
+
+}  // namespace wbc
+
+using namespace wbc;
+
+extern "C" {
+
+int wbc_deposit(const wbc_grid_geometry* geom, int32_t n, const float* position, const int32_t* cell_state,
+                int64_t* accumulator, void* stream) {
+    if (!geom_ok(geom) || n < 0 || !accumulator || (n > 0 && (!position || !cell_state))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_deposit<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(*geom, n, position, cell_state,
+                                                               reinterpret_cast<unsigned long long*>(accumulator));
+    return check_launch("wbc_deposit");
+}
+
+int wbc_density_convert(int64_t nodes, int64_t* accumulator, float inv_voxel_volume, float* density,
+                        const float* weights4, float* combined, int32_t clear, void* stream) {
+    if (nodes < 0 || !accumulator || (combined && !weights4)) return WBC_ERR_INVALID;
+    if (nodes == 0) return WBC_OK;
+    float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (weights4)
+        for (int s = 0; s < 4; ++s) w[s] = weights4[s];
+    k_convert<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, reinterpret_cast<long long*>(accumulator),
+                                                                   inv_voxel_volume, density, w[0], w[1], w[2], w[3],
+                                                                   combined, clear);
+    return check_launch("wbc_density_convert");
+}
+
+int wbc_density_combine(int64_t nodes, const float* weights4, const float* density, float* out, void* stream) {
+    if (nodes < 0 || !weights4 || (nodes > 0 && (!density || !out))) return WBC_ERR_INVALID;
+    if (nodes == 0) return WBC_OK;
+    k_combine<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, weights4[0], weights4[1], weights4[2],
+                                                                   weights4[3], density, out);
+    return check_launch("wbc_density_combine");
+}
+
+int wbc_sample(const wbc_grid_geometry* geom, const float* field, int32_t n, const float* position, float* out,
+               void* stream) {
+    if (!geom_ok(geom) || n < 0 || (n > 0 && (!field || !position || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_sample<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(*geom, field, n, position, out);
+    return check_launch("wbc_sample");
+}
+
+int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed, const float* density,
+                   const float* production, const float* source, float* field, float* residual_out, void* stream) {
+    if (!sor_ok(p) || sweeps < 0 || !fixed || !density || !field || (p->has_source && !source))
+        return WBC_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
+    const int64_t half_nodes = static_cast<int64_t>(p->nx) * p->ny * ((p->nz + 1) >> 1);
+    for (int sweep = 0; sweep < sweeps; ++sweep) {
+        for (int colour = 0; colour < 2; ++colour)
+            k_sor_colour<<<grid_for(half_nodes), kThreads, 0, s>>>(*p, colour, fixed, density, production, source,
+                                                                   field);
+    }
+    if (residual_out) {
+        cudaError_t err = cudaMemsetAsync(residual_out, 0, sizeof(float), s);
+        if (err != cudaSuccess) {
+            set_error("wbc_sor_sweeps: cudaMemsetAsync", err);
+            return WBC_ERR_CUDA;
+        }
+        k_residual<<<grid_for(nodes), kThreads, 0, s>>>(*p, fixed, density, production, source, field,
+                                                        reinterpret_cast<unsigned int*>(residual_out));
+    }
+    return check_launch("wbc_sor_sweeps");
+}
+
+int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,
+                  const float* production, const float* source, const float* field_in, float* field_out,
+                  void* stream) {
+    if (!sor_ok(p) || !fixed || !density || !field_in || !field_out || (p->has_source && !source))
+        return WBC_ERR_INVALID;
+    const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
+    k_ftcs<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(*p, dt, fixed, density, production, source, field_in,
+                                                                field_out);
+    return check_launch("wbc_ftcs_step");
+}
+
+}  // extern "C"

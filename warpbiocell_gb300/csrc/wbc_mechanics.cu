@@ -1,0 +1,183 @@
+// Hash-grid binning and the fused contact substep (neighbour count + overlap repulsion + Euler
+// integration).
+//
+// Binning: a counting sort of the active slots into dim^3 hashed buckets of edge
+// cell_size * (1 + 2^-10) (the 0.1% widening keeps every pair closer than cell_size in adjacent
+// buckets despite the rounding of x / edge). Within a bucket the slots are put in ascending
+// order, so the order in which a cell visits its candidates — 27 buckets in (x, y, z) offset
+// order, ascending slot inside each — is fixed by the positions alone. That fixes the float
+// summation order of the velocity, which is what lets the CPU oracle reproduce positions bit
+// for bit and keeps same-device runs bitwise reproducible.
+//
+// Reference: spatial/neighbors.py:33-37 (HashGrid build over the active prefix) and
+// kernels/mechanics_kernels.py:26-67 (contact_velocities, integrate_positions).
+#include "wbc_common.cuh"
+
+namespace wbc {
+
+struct BucketMap {
+    float inv_edge;
+    int dim;
+
+    __device__ __forceinline__ int coord(float x) const {
+        float q = x * inv_edge;
+        q = fminf(fmaxf(q, -1.0e9f), 1.0e9f);
+        return static_cast<int>(floorf(q));
+    }
+    __device__ __forceinline__ int wrap(int c) const {
+        int m = c % dim;
+        return m < 0 ? m + dim : m;
+    }
+    __device__ __forceinline__ int bucket(int cx, int cy, int cz) const {
+        return (wrap(cx) * dim + wrap(cy)) * dim + wrap(cz);
+    }
+};
+
+// Host-side: the bucket edge and its inverse, rounded exactly as the oracle rounds them.
+static BucketMap make_map(float cell_size, int dim) {
+    float edge = cell_size * 1.0009765625f;
+    BucketMap m;
+    m.inv_edge = 1.0f / edge;
+    m.dim = dim;
+    return m;
+}
+
+__global__ void k_bin_assign(BucketMap map, int32_t n, const float* __restrict__ position,
+                             int32_t* __restrict__ bucket_count, int32_t* __restrict__ cell_bucket,
+                             int32_t* __restrict__ cell_rank) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = position + 3 * static_cast<int64_t>(i);
+    int b = map.bucket(map.coord(p[0]), map.coord(p[1]), map.coord(p[2]));
+    cell_bucket[i] = b;
+    cell_rank[i] = atomicAdd(bucket_count + b, 1);
+}
+
+__global__ void k_bin_scatter(int32_t n, const int32_t* __restrict__ cell_bucket, const int32_t* __restrict__ cell_rank,
+                              const int32_t* __restrict__ bucket_start, int32_t* __restrict__ scatter) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    scatter[bucket_start[cell_bucket[i]] + cell_rank[i]] = i;
+}
+
+// Each slot finds its place among the members of its bucket in ascending slot order.
+__global__ void k_bin_order(int32_t n, const float* __restrict__ position, const float* __restrict__ radius,
+                            const int32_t* __restrict__ cell_bucket, const int32_t* __restrict__ bucket_start,
+                            const int32_t* __restrict__ bucket_count, const int32_t* __restrict__ scatter,
+                            int32_t* __restrict__ sorted_id, float4* __restrict__ sorted_xyzr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = cell_bucket[i];
+    const int s = bucket_start[b];
+    const int c = bucket_count[b];
+    int rank = 0;
+    for (int u = s; u < s + c; ++u) rank += scatter[u] < i ? 1 : 0;
+    const float* p = position + 3 * static_cast<int64_t>(i);
+    sorted_id[s + rank] = i;
+    sorted_xyzr[s + rank] = make_float4(p[0], p[1], p[2], radius[i]);
+}
+
+// One thread per sorted slot t (so a warp works on neighbouring cells and shares buckets).
+__global__ void __launch_bounds__(256) k_contact(BucketMap map, int32_t n, const int32_t* __restrict__ bucket_start,
+                                                 const int32_t* __restrict__ bucket_count,
+                                                 const int32_t* __restrict__ sorted_id,
+                                                 const float4* __restrict__ sorted_xyzr, float query_radius, float rate,
+                                                 float dt, float* __restrict__ position, float* __restrict__ velocity,
+                                                 int32_t* __restrict__ neighbor_count) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4 me = sorted_xyzr[t];
+    const int i = sorted_id[t];
+    const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    float vx = 0.0f, vy = 0.0f, vz = 0.0f;
+    int count = 0;
+    for (int ox = -1; ox <= 1; ++ox) {
+        for (int oy = -1; oy <= 1; ++oy) {
+            for (int oz = -1; oz <= 1; ++oz) {
+                const int b = map.bucket(cx + ox, cy + oy, cz + oz);
+                const int s = bucket_start[b];
+                const int e = s + bucket_count[b];
+                for (int u = s; u < e; ++u) {
+                    if (u == t) continue;
+                    const float4 q = sorted_xyzr[u];
+                    const float dx = me.x - q.x;
+                    const float dy = me.y - q.y;
+                    const float dz = me.z - q.z;
+                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    if (d < query_radius) {
+                        ++count;
+                        const float overlap = me.w + q.w - d;
+                        if (overlap > 0.0f && d > 1.0e-6f) {
+                            const float f = rate * overlap / d;
+                            vx = vx + f * dx;
+                            vy = vy + f * dy;
+                            vz = vz + f * dz;
+                        }
+                    }
+                }
+            }
+        }
+    }
+    const int64_t o = 3 * static_cast<int64_t>(i);
+    velocity[o + 0] = vx;
+    velocity[o + 1] = vy;
+    velocity[o + 2] = vz;
+    neighbor_count[i] = count;
+    position[o + 0] = me.x + vx * dt;
+    position[o + 1] = me.y + vy * dt;
+    position[o + 2] = me.z + vz * dt;
+}
+
+static bool grid_ok(const wbc_neighbor_grid* g) {
+    return g && g->dim >= 3 && g->dim <= 1290 && g->cell_size > 0.0f && g->bucket_count && g->bucket_start &&
+           g->cell_bucket && g->cell_rank && g->scatter && g->sorted_id && g->sorted_xyzr && g->scan_partials;
+}
+
+}  // namespace wbc
+
+using namespace wbc;
+
+extern "C" {
+
+int wbc_grid_build(const wbc_neighbor_grid* grid, int32_t n, const float* position, const float* radius,
+                   void* stream) {
+    if (!grid_ok(grid) || n < 0 || n > grid->capacity || (n > 0 && (!position || !radius))) return WBC_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    const int64_t buckets = static_cast<int64_t>(grid->dim) * grid->dim * grid->dim;
+    cudaError_t err = cudaMemsetAsync(grid->bucket_count, 0, buckets * sizeof(int32_t), s);
+    if (err != cudaSuccess) {
+        set_error("wbc_grid_build: cudaMemsetAsync", err);
+        return WBC_ERR_CUDA;
+    }
+    if (n == 0) return scan_i32(grid->bucket_count, grid->bucket_start, buckets, false, grid->scan_partials, nullptr, s);
+    BucketMap map = make_map(grid->cell_size, grid->dim);
+    k_bin_assign<<<grid_for(n), kThreads, 0, s>>>(map, n, position, grid->bucket_count, grid->cell_bucket,
+                                                  grid->cell_rank);
+    int rc = scan_i32(grid->bucket_count, grid->bucket_start, buckets, false, grid->scan_partials, nullptr, s);
+    if (rc != WBC_OK) return rc;
+    k_bin_scatter<<<grid_for(n), kThreads, 0, s>>>(n, grid->cell_bucket, grid->cell_rank, grid->bucket_start,
+                                                   grid->scatter);
+    k_bin_order<<<grid_for(n), kThreads, 0, s>>>(n, position, radius, grid->cell_bucket, grid->bucket_start,
+                                                 grid->bucket_count, grid->scatter, grid->sorted_id,
+                                                 reinterpret_cast<float4*>(grid->sorted_xyzr));
+    return check_launch("wbc_grid_build");
+}
+
+int wbc_contact_substep(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                        float* position, float* velocity, int32_t* neighbor_count, void* stream) {
+    if (!grid_ok(grid) || n < 0 || n > grid->capacity || (n > 0 && (!position || !velocity || !neighbor_count)))
+        return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    if (!(query_radius <= grid->cell_size)) {
+        set_error_msg("wbc_contact_substep: query_radius exceeds the grid's cell_size");
+        return WBC_ERR_INVALID;
+    }
+    BucketMap map = make_map(grid->cell_size, grid->dim);
+    k_contact<<<grid_for(n), 256, 0, as_stream(stream)>>>(
+        map, n, grid->bucket_start, grid->bucket_count, grid->sorted_id,
+        reinterpret_cast<const float4*>(grid->sorted_xyzr), query_radius, rate, dt, position, velocity,
+        neighbor_count);
+    return check_launch("wbc_contact_substep");
+}
+
+}  // extern "C"

@@ -1,0 +1,223 @@
+// Library plumbing: error bookkeeping, version, device count, the multi-block int32 scan used by
+// the hash-grid binning and the division slots, and the test hooks of the random streams.
+#include <cstdio>
+#include <cstring>
+
+#include "wbc_common.cuh"
+
+namespace wbc {
+
+namespace {
+thread_local char g_error[512] = "no error";
+}
+
+void set_error(const char* where, cudaError_t err) {
+    std::snprintf(g_error, sizeof(g_error), "%s: %s (%s)", where, cudaGetErrorString(err), cudaGetErrorName(err));
+}
+
+void set_error_msg(const char* msg) { std::snprintf(g_error, sizeof(g_error), "%s", msg); }
+
+int check_launch(const char* where) {
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) {
+        set_error(where, err);
+        return WBC_ERR_CUDA;
+    }
+    return WBC_OK;
+}
+
+// ---- scan --------------------------------------------------------------------------------------
+// Tile = kScanThreads x kScanItems consecutive elements. Phase 1 reduces every tile to one
+// partial; phase 2 (one block) turns the partials into exclusive tile offsets with a running
+// carry, so any number of tiles works; phase 3 rescans each tile from its offset. Pure integer
+// work, so the result does not depend on the launch shape.
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+int64_t scan_partials_count(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+__device__ __forceinline__ int32_t warp_inclusive(int32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        int32_t o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+
+// Block-wide exclusive scan of one value per thread; returns the exclusive prefix, *total the sum.
+__device__ __forceinline__ int32_t block_exclusive(int32_t v, int32_t* total) {
+    __shared__ int32_t warp_sums[kScanThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    int32_t inc = warp_inclusive(v);
+    if (lane == 31) warp_sums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        int32_t s = (lane < kScanThreads / 32) ? warp_sums[lane] : 0;
+        s = warp_inclusive(s);
+        if (lane < kScanThreads / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    int32_t warp_offset = warp > 0 ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[kScanThreads / 32 - 1];
+    __syncthreads();
+    return warp_offset + inc - v;
+}
+
+__global__ void scan_reduce_tiles(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ partials) {
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t idx = base + k;
+        if (idx < n) s += in[idx];
+    }
+    int32_t total;
+    block_exclusive(s, &total);
+    if (threadIdx.x == 0) partials[blockIdx.x] = total;
+}
+
+__global__ void scan_partials(int32_t* __restrict__ partials, int64_t tiles, int32_t* __restrict__ total_out) {
+    int32_t carry = 0;
+    for (int64_t base = 0; base < tiles; base += kScanThreads) {
+        int64_t idx = base + threadIdx.x;
+        int32_t v = idx < tiles ? partials[idx] : 0;
+        int32_t chunk_total;
+        int32_t ex = block_exclusive(v, &chunk_total);
+        if (idx < tiles) partials[idx] = carry + ex;
+        carry += chunk_total;
+    }
+    if (threadIdx.x == 0) {
+        partials[tiles] = carry;
+        if (total_out) *total_out = carry;
+    }
+}
+
+__global__ void scan_tiles(const int32_t* __restrict__ in, int32_t* __restrict__ out, int64_t n,
+                           const int32_t* __restrict__ partials, bool inclusive) {
+    const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+    int32_t vals[kScanItems];
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t idx = base + k;
+        vals[k] = idx < n ? in[idx] : 0;
+        s += vals[k];
+    }
+    int32_t total;
+    int32_t run = block_exclusive(s, &total) + partials[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t idx = base + k;
+        if (inclusive) run += vals[k];
+        if (idx < n) out[idx] = run;
+        if (!inclusive) run += vals[k];
+    }
+}
+
+int scan_i32(const int32_t* in, int32_t* out, int64_t n, bool inclusive, int32_t* partials, int32_t* total,
+             cudaStream_t stream) {
+    if (n <= 0) {
+        if (total) {
+            cudaError_t err = cudaMemsetAsync(total, 0, sizeof(int32_t), stream);
+            if (err != cudaSuccess) {
+                set_error("scan: cudaMemsetAsync", err);
+                return WBC_ERR_CUDA;
+            }
+        }
+        return WBC_OK;
+    }
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    scan_reduce_tiles<<<static_cast<unsigned>(tiles), kScanThreads, 0, stream>>>(in, n, partials);
+    scan_partials<<<1, kScanThreads, 0, stream>>>(partials, tiles, total);
+    scan_tiles<<<static_cast<unsigned>(tiles), kScanThreads, 0, stream>>>(in, out, n, partials, inclusive);
+    return check_launch("scan_i32");
+}
+
+// ---- random-stream test hooks ----------------------------------------------------------------------
+__global__ void k_rng_init(int32_t seed, uint32_t* __restrict__ rng_state, int64_t capacity) {
+    int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i < capacity) rng_state[i] = rng_start(seed, static_cast<uint32_t>(i));
+}
+
+__global__ void k_rng_uniform(int32_t n, int32_t draws, uint32_t* __restrict__ rng_state, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = rng_state[i];
+    const uint32_t inc = rng_increment(static_cast<uint32_t>(i));
+    for (int k = 0; k < draws; ++k) out[static_cast<int64_t>(i) * draws + k] = randf(s, inc);
+    rng_state[i] = s;
+}
+
+__global__ void k_rng_sphere(int32_t n, uint32_t* __restrict__ rng_state, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t s = rng_state[i];
+    float x, y, z;
+    unit_sphere(s, rng_increment(static_cast<uint32_t>(i)), x, y, z);
+    rng_state[i] = s;
+    out[3 * static_cast<int64_t>(i) + 0] = x;
+    out[3 * static_cast<int64_t>(i) + 1] = y;
+    out[3 * static_cast<int64_t>(i) + 2] = z;
+}
+
+__global__ void k_expf(int32_t n, const float* __restrict__ x, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = wbc_expf(x[i]);
+}
+
+}  // namespace wbc
+
+using namespace wbc;
+
+extern "C" {
+
+int wbc_version(void) { return 1; }
+
+const char* wbc_last_error(void) { return g_error; }
+
+int wbc_device_count(void) {
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return count;
+}
+
+size_t wbc_scan_workspace_bytes(int64_t n) {
+    return static_cast<size_t>(scan_partials_count(n < 1 ? 1 : n)) * sizeof(int32_t);
+}
+
+int wbc_rng_init(int32_t seed, uint32_t* rng_state, int64_t capacity, void* stream) {
+    if (capacity < 0 || (capacity > 0 && !rng_state)) return WBC_ERR_INVALID;
+    if (capacity == 0) return WBC_OK;
+    k_rng_init<<<grid_for(capacity), kThreads, 0, as_stream(stream)>>>(seed, rng_state, capacity);
+    return check_launch("wbc_rng_init");
+}
+
+int wbc_rng_uniform(int32_t n, int32_t draws, uint32_t* rng_state, float* out, void* stream) {
+    if (n < 0 || draws < 0 || (n > 0 && (!rng_state || !out))) return WBC_ERR_INVALID;
+    if (n == 0 || draws == 0) return WBC_OK;
+    k_rng_uniform<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, draws, rng_state, out);
+    return check_launch("wbc_rng_uniform");
+}
+
+int wbc_rng_sphere(int32_t n, uint32_t* rng_state, float* out_xyz, void* stream) {
+    if (n < 0 || (n > 0 && (!rng_state || !out_xyz))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_rng_sphere<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, rng_state, out_xyz);
+    return check_launch("wbc_rng_sphere");
+}
+
+int wbc_expf_batch(int32_t n, const float* x, float* out, void* stream) {
+    if (n < 0 || (n > 0 && (!x || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_expf<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, x, out);
+    return check_launch("wbc_expf_batch");
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+"""Reaction-diffusion solvers on a ScalarField with Michaelis-Menten uptake
+(reference: fields/diffusion.py:18-154).
+
+``solve_steady_state`` is the production path: red-black SOR sweeps in place from the field's
+current values (warm start), ``check_every`` sweeps per native call (``wbc_sor_sweeps``, which
+also reduces the max-norm residual on the device), one host read of the residual per check,
+exactly the reference's cadence and stopping rule. ``explicit_step`` (FTCS) is for validation.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import torch
+
+from warpbiocell_gb300 import _lib
+from warpbiocell_gb300.fields.scalar_field import ScalarField
+
+
+@dataclass(frozen=True)
+class UptakeKinetics:
+    """``q(O) = uptake_max * O / (michaelis_k + O)`` per consuming cell; ``diffusion`` D [um^2/h]."""
+
+    diffusion: float
+    uptake_max: float
+    michaelis_k: float
+
+    def __post_init__(self):
+        if self.diffusion <= 0.0:
+            raise ValueError("diffusion coefficient must be positive")
+        if self.uptake_max < 0.0 or self.michaelis_k <= 0.0:
+            raise ValueError("uptake_max must be non-negative and michaelis_k positive")
+
+
+@dataclass(frozen=True)
+class SolverSettings:
+    """Red-black SOR settings: relaxation ``omega`` in (0, 2), a hard ``max_sweeps`` budget, the
+    dimensionless max-norm residual ``tolerance`` and ``check_every`` sweeps between residual
+    checks (each check is one host sync). In float32 the residual bottoms out near
+    1e-7 * omega / (2 - omega), so tolerances below ~1e-6 may never be met."""
+
+    omega: float = 1.5
+    max_sweeps: int = 2000
+    tolerance: float = 1.0e-5
+    check_every: int = 20
+
+    def __post_init__(self):
+        if not 0.0 < self.omega < 2.0:
+            raise ValueError("omega must lie in (0, 2)")
+        if self.max_sweeps < 1 or self.check_every < 1:
+            raise ValueError("max_sweeps and check_every must be positive")
+        if self.tolerance <= 0.0:
+            raise ValueError("tolerance must be positive")
+
+
+@dataclass(frozen=True)
+class SolveReport:
+    sweeps: int
+    residual: float
+    converged: bool
+
+
+def _source_args(field: ScalarField, production, source, source_k):
+    prod = production if production is not None else None
+    has_source = 1 if source is not None else 0
+    return prod, has_source, source, float(source_k)
+
+
+def sor_params(field: ScalarField, kinetics: UptakeKinetics, omega: float, has_source: int = 0,
+               source_k: float = 1.0) -> _lib.SorParamsC:
+    """Kernel parameters, each rounded to float32 from the same double expression the reference uses."""
+    geom = field.geometry
+    nx, ny, nz = geom.shape
+    bc_x, bc_y, bc_z = field.boundary_flags
+    reference = field.boundary_value if field.boundary_value > 0.0 else 1.0
+    return _lib.SorParamsC(nx=nx, ny=ny, nz=nz, bc_x=bc_x, bc_y=bc_y, bc_z=bc_z, omega=omega,
+                           dx2_over_D=geom.dx**2 / kinetics.diffusion, uptake_max=kinetics.uptake_max,
+                           michaelis_k=kinetics.michaelis_k, reference=reference, has_source=has_source,
+                           source_k=source_k)
+
+
+def sor_chunk(field: ScalarField, density: torch.Tensor, params: _lib.SorParamsC, sweeps: int,
+              residual_buffer: torch.Tensor | None, production=None, source=None) -> None:
+    """``sweeps`` red-black sweeps (and the residual into ``residual_buffer[0]`` when given)."""
+    _lib.call("wbc_sor_sweeps", ctypes.byref(params), int(sweeps), _lib.ptr(field.fixed), _lib.ptr(density),
+              _lib.ptr(production), _lib.ptr(source), _lib.ptr(field.values), _lib.ptr(residual_buffer),
+              _lib.stream(field.device))
+
+
+def solve_steady_state(
+    field: ScalarField,
+    density: torch.Tensor,
+    kinetics: UptakeKinetics,
+    settings: SolverSettings,
+    residual_buffer: torch.Tensor,
+    production: torch.Tensor | None = None,
+    source: torch.Tensor | None = None,
+    source_k: float = 1.0,
+) -> SolveReport:
+    """Iterate SOR sweeps in place, starting from the field's current values (warm start).
+
+    ``production`` [conc/h] is an optional zero-order source per node, scaled by
+    ``S/(source_k + S)`` of the ``source`` field when one is given.
+    """
+    prod, has_source, src, source_k = _source_args(field, production, source, source_k)
+    params = sor_params(field, kinetics, settings.omega, has_source, source_k)
+    sweeps = 0
+    residual = float("inf")
+    while sweeps < settings.max_sweeps:
+        chunk = min(settings.check_every, settings.max_sweeps - sweeps)
+        sor_chunk(field, density, params, chunk, residual_buffer, prod, src)
+        sweeps += chunk
+        residual = float(residual_buffer[0].item())
+        if residual < settings.tolerance:
+            return SolveReport(sweeps=sweeps, residual=residual, converged=True)
+    return SolveReport(sweeps=sweeps, residual=residual, converged=False)
+
+
+def max_stable_dt(field: ScalarField, kinetics: UptakeKinetics) -> float:
+    """Explicit-scheme stability limit ``dx^2 / (6 D)`` [h]."""
+    return field.geometry.dx**2 / (6.0 * kinetics.diffusion)
+
+
+def explicit_step(
+    field: ScalarField,
+    density: torch.Tensor,
+    kinetics: UptakeKinetics,
+    dt: float,
+    scratch: torch.Tensor,
+    production: torch.Tensor | None = None,
+    source: torch.Tensor | None = None,
+    source_k: float = 1.0,
+) -> None:
+    """One FTCS step into ``scratch``, copied back so ``field.values`` stays the same tensor."""
+    limit = max_stable_dt(field, kinetics)
+    if dt > limit * (1.0 + 1.0e-6):
+        raise ValueError(f"dt = {dt:.3g} h exceeds the explicit stability limit dx^2/(6D) = {limit:.3g} h")
+    prod, has_source, src, source_k = _source_args(field, production, source, source_k)
+    geom = field.geometry
+    nx, ny, nz = geom.shape
+    bc_x, bc_y, bc_z = field.boundary_flags
+    params = _lib.SorParamsC(nx=nx, ny=ny, nz=nz, bc_x=bc_x, bc_y=bc_y, bc_z=bc_z, omega=1.0,
+                             dx2_over_D=kinetics.diffusion / geom.dx**2, uptake_max=kinetics.uptake_max,
+                             michaelis_k=kinetics.michaelis_k, reference=1.0, has_source=has_source,
+                             source_k=source_k)
+    _lib.call("wbc_ftcs_step", ctypes.byref(params), float(dt), _lib.ptr(field.fixed), _lib.ptr(density),
+              _lib.ptr(prod), _lib.ptr(src), _lib.ptr(field.values), _lib.ptr(scratch), _lib.stream(field.device))
+    field.values.copy_(scratch)

@@ -1,0 +1,1 @@
+"""Drop-in counterpart of the reference package of the same name."""
