@@ -1,0 +1,490 @@
+"""Benchmark of the coupled cell step: cell-steps/s on the 1M-cell / 161^3-node spheroid.
+
+One step = one ``cell_step`` of the drop-in API: deposit of the cells' O2 uptake (int64 fixed
+point) -> red-black SOR to the residual tolerance (warm start, residual checked every
+``check_every`` sweeps) -> trilinear sampling -> lifecycle (decide, inclusive scan, one host read,
+placement) -> one mechanics substep (hash-grid binning, contact forces + integration).
+
+Workload "spheroid_1M_161" (default): 1,000,000 cells uniform in a 1,200 um ball, radii
+N(8, 0.8) clipped to [6, 10] um, 161^3 grid at 15 um (boundary 100 mmHg), D = 2000 um^2/s,
+Vmax = 20 amol/s = 5.54e7 mmHg um^3/h, Km = 1 mmHg, SOR omega 1.8 to residual 1e-6, hypoxia
+below 5 mmHg, necrosis below 1 mmHg, division ln2/24 per h, k/gamma = 1/h, 20 um hash cells,
+dt = 6 min (one mechanics substep). Synthetic seeded inputs (numpy default_rng(0)).
+
+Arms:
+  (default)          GB300 kernels through the public API; device-timed K steps (CUDA events,
+                     inputs already in HBM), per-stage event timers, an end-to-end pass through
+                     host buffers, a CPU baseline sample (the oracle on the host cores) and a
+                     full-size bitwise parity check of one step against the oracle.
+  --impl reference   the reference's algorithm on the host CPU: WarpBioCell's own Warp CPU path
+                     cannot run here (warp-lang is not installed), so this times the C++
+                     restatement (oracle/) with every host thread, on the same workload.
+
+Multi-GPU (torchrun, --gpus N): independent replicas, one per GPU (no data-path collective; the
+only collectives are the timing barrier and the max/sum reductions of the result).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+if str(ROOT) not in sys.path:
+    sys.path.insert(0, str(ROOT))
+
+METRIC = "cell-steps/s @1M cells+161^3 O2 (coupled cell step)"
+UNIT = "cell-steps/s"
+
+WORKLOADS = {
+    "spheroid_1M_161": dict(cells=1_000_000, ball_um=1200.0, box_um=2400.0, dx_um=15.0, boundary=100.0),
+    "spheroid_10k_41": dict(cells=10_000, ball_um=250.0, box_um=800.0, dx_um=20.0, boundary=38.0),
+    "spheroid_100k_81": dict(cells=100_000, ball_um=600.0, box_um=1600.0, dx_um=20.0, boundary=38.0),
+}
+
+DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
+VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
+KM = 1.0
+DT = 0.1  # h (6 min)
+
+
+def make_params(w: dict):
+    from warpbiocell_gb300.cells.lifecycle import LifecycleParams
+    from warpbiocell_gb300.cells.mechanics import ContactParams
+    from warpbiocell_gb300.fields.diffusion import SolverSettings
+    from warpbiocell_gb300.fields.oxygen import OxygenParams
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+    from warpbiocell_gb300.simulation.simulator import TimeStepping
+
+    return dict(
+        geom=GridGeometry.centered_cube(w["box_um"], w["dx_um"]),
+        oxygen=OxygenParams(diffusion_coefficient=DIFFUSION, uptake_max=VMAX, michaelis_k=KM,
+                            boundary_value=w["boundary"]),
+        settings=SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=2000, check_every=20),
+        lifecycle=LifecycleParams(division_rate=math.log(2.0) / 24.0, death_rate=0.0, anoxic_death_rate=0.5,
+                                  inhibition_threshold=8, hypoxia_threshold=5.0, death_threshold=1.0),
+        contact=ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, margin=0.0),
+        stepping=TimeStepping(dt_cells=DT, dt_mechanics=DT),
+    )
+
+
+def make_cells(w: dict, seed: int):
+    from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball
+
+    pos = uniform_ball(w["cells"], w["ball_um"], seed=seed)
+    radii = clipped_normal_radii(w["cells"], 8.0, 0.8, 6.0, 10.0, seed=seed + 1)
+    return pos, radii
+
+
+# ---- clocks ------------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu_index = gpu_index
+        self.proc = None
+        self.path = Path(tempfile.mkstemp(prefix="wbc_clocks_", suffix=".csv")[1])
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu_index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, sm_max, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                sm_max.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        self.path.unlink(missing_ok=True)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(sm_max)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- roofline bookkeeping --------------------------------------------------------------------------------
+def stage_bytes(stage: str, cells: float, nodes: float, launches: int, daughters: float = 0.0) -> float:
+    """Algorithmic (compulsory) bytes a stage moves, summed over its launches."""
+    if stage == "sor":  # per colour launch: read the field once, n_eff and write the colour's half
+        return launches * 8.0 * nodes
+    if stage == "deposit":  # position + state per cell (the atomics stay in L2)
+        return 16.0 * cells
+    if stage == "convert":  # read + clear 4 int64 layers, write 4 float layers + n_eff
+        return (32.0 + 32.0 + 16.0 + 4.0) * nodes
+    if stage == "contact":  # xyzr + id read, position/velocity/count write
+        return (16.0 + 4.0 + 12.0 + 12.0 + 4.0) * cells
+    if stage == "bin":  # position/radius read, ids + xyzr written
+        return (12.0 + 4.0 + 4.0 + 16.0) * cells
+    if stage == "sample":
+        return (12.0 + 4.0) * cells + 4.0 * nodes
+    if stage == "decide":
+        return 40.0 * cells
+    if stage == "scan":
+        return 8.0 * cells
+    if stage == "place":
+        return 8.0 * cells + 64.0 * daughters
+    return 0.0
+
+
+def load_peaks() -> dict:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        try:
+            return json.loads(path.read_text())
+        except ValueError:
+            pass
+    return {}
+
+
+# ---- GB300 arm ---------------------------------------------------------------------------------------------
+def run_gpu(args, rank: int, world: int) -> dict | None:
+    import torch
+
+    from warpbiocell_gb300 import _lib, profiling
+    from warpbiocell_gb300.cells.mechanics import contact_substep, make_neighbor_grid
+    from warpbiocell_gb300.cells.state import CellPopulation
+    from warpbiocell_gb300.fields.oxygen import OxygenField
+    from warpbiocell_gb300.simulation.simulator import cell_step
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]
+    P = make_params(w)
+    pos, radii = make_cells(w, seed=args.seed + rank)
+    capacity = int(w["cells"] * 1.5)
+    pop = CellPopulation.from_numpy(pos, radii, capacity=capacity, device=dev, seed=args.seed + rank)
+    ox = OxygenField(P["geom"], P["oxygen"], P["settings"], device=dev)
+    grid = make_neighbor_grid(P["contact"], dev)
+    # As the reference's Experiment.run: initial neighbour counts and an initial field solve.
+    contact_substep(pop, grid, P["contact"], dt=0.0)
+    first = ox.update(pop)
+
+    def step():
+        return cell_step(pop, grid, P["lifecycle"], P["contact"], P["stepping"], oxygen=ox)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = _lib.launch_count()
+    profiling.enable(True)
+    barrier()
+    start_ev = torch.cuda.Event(enable_timing=True)
+    end_ev = torch.cuda.Event(enable_timing=True)
+    cell_steps = 0
+    sweeps = []
+    daughters = 0
+    start_ev.record()
+    for _ in range(args.steps):
+        cell_steps += pop.count
+        rep = step()
+        sweeps.append(rep.field_sweeps)
+        daughters += rep.daughters
+    end_ev.record()
+    barrier()
+    elapsed_ms = start_ev.elapsed_time(end_ev)
+    stages = profiling.summary()
+    profiling.enable(False)
+    launches = _lib.launch_count() - launches0
+    clocks = sampler.stop()
+
+    # End to end: every step uploads the population from pinned host buffers, runs the step
+    # through the public API and reads the updated population back.
+    names = ["position", "radius", "cell_state", "cell_type", "age", "oxygen_local", "glucose_local", "rng_state",
+             "velocity", "neighbor_count", "fate_flags"]
+    host = {k: torch.empty_like(getattr(pop, k), device="cpu").pin_memory() for k in names}
+    for k in names:
+        host[k].copy_(getattr(pop, k))
+    e2e_steps = max(1, args.steps)
+    torch.cuda.synchronize()
+    h2d = d2h = 0
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_end = torch.cuda.Event(enable_timing=True)
+    e2e_cells = 0
+    barrier()
+    e_start.record()
+    for _ in range(e2e_steps):
+        n = pop.count
+        for k in names:
+            getattr(pop, k)[:n].copy_(host[k][:n], non_blocking=True)
+            h2d += host[k][:n].numel() * host[k].element_size()
+        e2e_cells += n
+        step()
+        n = pop.count
+        for k in names:
+            host[k][:n].copy_(getattr(pop, k)[:n], non_blocking=True)
+            d2h += host[k][:n].numel() * host[k].element_size()
+    e_end.record()
+    barrier()
+    e2e_ms = e_start.elapsed_time(e_end)
+
+    result = {
+        "rank": rank,
+        "elapsed_ms": elapsed_ms,
+        "cell_steps": cell_steps,
+        "e2e_ms": e2e_ms,
+        "e2e_cell_steps": e2e_cells,
+        "h2d": h2d / e2e_steps,
+        "d2h": d2h / e2e_steps,
+        "launches": launches,
+        "stages": stages,
+        "sweeps": sweeps,
+        "initial_sweeps": first.sweeps,
+        "daughters": daughters,
+        "clocks": clocks,
+        "count": pop.count,
+        "nodes": P["geom"].node_count,
+    }
+    if rank == 0 and not args.skip_cpu:
+        result["cpu_baseline"], result["parity_full_size"] = cpu_sample_and_parity(pop, ox, grid, P, step)
+    return result
+
+
+def _population_to_oracle(pop):
+    from oracle import oracle as orc
+
+    arrays = {k: getattr(pop, k).cpu().numpy().copy() for k in
+              ("position", "radius", "cell_state", "cell_type", "age", "oxygen_local", "glucose_local", "velocity",
+               "neighbor_count", "divide_flag", "division_offset", "fate_flags")}
+    sim = orc.OracleSim(capacity=pop.capacity, count=pop.count, seed=pop.seed,
+                        rng_state=pop.rng_state.cpu().numpy().view(np.uint32).copy(), **arrays)
+    return sim
+
+
+def cpu_sample_and_parity(pop, ox, grid, P, step):
+    """Time one full-size cell step of the oracle on the host cores from the GPU's current state,
+    then run the same step on the GPU and compare the two bit for bit."""
+    from oracle import oracle as orc
+
+    sim = _population_to_oracle(pop)
+    g = P["geom"]
+    sp = orc.OracleSpecies(orc.Geometry(g.origin, g.dx, g.shape), tuple(int(b) for b in ox.field.boundary_flags),
+                           ox.field.boundary_value, ox.species.diffusion, ox.species.uptake_max,
+                           ox.species.michaelis_k, P["settings"])
+    sp.values = ox.numpy()
+    threads = orc.num_threads()
+    cells = sim.count
+    t0 = time.perf_counter()
+    daughters, report = orc.cell_step(sim, P["lifecycle"], P["contact"], P["stepping"].dt_cells,
+                                      P["stepping"].dt_mechanics, sp, dim=grid.dim)
+    cpu_s = time.perf_counter() - t0
+    rep = step()
+    n = pop.count
+    same = (rep.daughters == daughters and n == sim.count and rep.field_sweeps == report[0]
+            and np.array_equal(ox.numpy(), sp.values)
+            and np.array_equal(pop.position[:n].cpu().numpy(), sim.position[:n])
+            and np.array_equal(pop.cell_state[:n].cpu().numpy(), sim.cell_state[:n])
+            and np.array_equal(pop.neighbor_count[:n].cpu().numpy(), sim.neighbor_count[:n])
+            and np.array_equal(pop.rng_state[:n].cpu().numpy().view(np.uint32), sim.rng_state[:n]))
+    baseline = {"value": cells / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                "sample": f"one full cell step of the same workload ({cells} cells, {report[0]} SOR sweeps) by the "
+                          f"C++ restatement with {threads} OpenMP threads, from the GPU run's state; {cpu_s:.2f} s"}
+    return baseline, bool(same)
+
+
+def report_gpu(args, results: list[dict], world: int) -> dict:
+    peaks = load_peaks()
+    r0 = results[0]
+    max_ms = max(r["elapsed_ms"] for r in results)
+    total_cells = sum(r["cell_steps"] for r in results)
+    value = total_cells / (max_ms / 1e3)
+    e2e_ms = max(r["e2e_ms"] for r in results)
+    e2e_value = sum(r["e2e_cell_steps"] for r in results) / (e2e_ms / 1e3)
+    stages = r0["stages"]
+    steps = max(1, args.steps)
+    cells_per_step = r0["cell_steps"] / steps
+    nodes = r0["nodes"]
+    dominant = max(stages, key=lambda k: stages[k]["ms"]) if stages else None
+    roofline = None
+    if dominant:
+        s = stages[dominant]
+        if dominant == "sor":  # per colour launch (the residual launches are counted as launches too)
+            per_launch_ms = s["ms"] / max(1, s["launches"])
+            nbytes = stage_bytes("sor", cells_per_step, nodes, 1)
+        else:  # per call of the stage
+            per_launch_ms = s["ms"] / max(1, s["calls"])
+            nbytes = stage_bytes(dominant, cells_per_step, nodes, 1)
+        achieved = nbytes / (per_launch_ms / 1e3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "traffic": None,
+                    "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                    "bytes_per_launch": nbytes, "launch_ms": per_launch_ms}
+    breakdown = {k: {"ms_per_step": round(v["ms"] / steps, 4), "launches_per_step": v["launches"] / steps,
+                     "GB/s": round(stage_bytes(k, cells_per_step, nodes, int(v["launches"] / steps)) /
+                                   (v["ms"] / steps / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                 for k, v in sorted(stages.items(), key=lambda kv: -kv[1]["ms"])}
+    out = {
+        "metric": METRIC,
+        "value": round(value, 1),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(max_ms / steps, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
+        "data": "synthetic (seeded uniform ball, clipped-normal radii)",
+        "config": {"workload": args.workload, **WORKLOADS[args.workload], "grid_nodes": nodes,
+                   "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT, "mechanics_substeps": 1,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2: per-step working set (cells ~60 MB + int64 accumulator "
+                         f"{4 * 8 * nodes / 1e6:.0f} MB + fields) exceeds the 129 MB L2"},
+        "gpu_launches": int(r0["launches"]),
+        "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(r0["h2d"]),
+                "d2h_bytes_per_step": int(r0["d2h"])},
+        "roofline": roofline,
+        "stages": breakdown,
+        "sor_sweeps_per_step": r0["sweeps"],
+        "initial_solve_sweeps": r0["initial_sweeps"],
+        "clocks": r0["clocks"],
+        "cells_final": r0["count"],
+    }
+    if "cpu_baseline" in r0:
+        out["cpu_baseline"] = r0["cpu_baseline"]
+        out["parity_full_size_bitwise"] = r0["parity_full_size"]
+    return out
+
+
+# ---- reference arm (CPU) ---------------------------------------------------------------------------------------
+def run_reference(args) -> dict:
+    from oracle import oracle as orc
+
+    w = WORKLOADS[args.workload]
+    P = make_params(w)
+    pos, radii = make_cells(w, seed=args.seed)
+    sim = orc.OracleSim.from_numpy(pos, radii, capacity=int(w["cells"] * 1.5), seed=args.seed)
+    g = P["geom"]
+    sp = orc.OracleSpecies(orc.Geometry(g.origin, g.dx, g.shape), (0, 0, 0), w["boundary"], DIFFUSION,
+                           (VMAX, VMAX, VMAX, 0.0), KM, P["settings"])
+    threads = orc.num_threads()
+    contact, stepping = P["contact"], P["stepping"]
+    sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
+    # initial field solve as in the reference's Experiment.run
+    n = sim.count
+    acc = orc.deposit(sp.geom, sim.position[:n], sim.cell_state[:n])
+    dens, _ = orc.density_convert(sp.geom, acc)
+    sp.combine(dens)
+    sp.solve()
+    sp.sample_into(sim, sim.oxygen_local)
+    for _ in range(args.warmup):
+        orc.cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, sp)
+    cells = 0
+    t0 = time.perf_counter()
+    done = 0
+    budget_s = args.reference_budget_s
+    for _ in range(args.steps):
+        cells += sim.count
+        orc.cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, sp)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    elapsed = time.perf_counter() - t0
+    value = cells / elapsed
+    sample = (f"{done} full cell steps of the workload by the C++ restatement of the reference kernels "
+              f"(WarpBioCell's Warp CPU path cannot run here: warp-lang is absent) on {threads} OpenMP threads")
+    return {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": done, "warmup": args.warmup,
+        "ms_per_step": round(elapsed * 1e3 / max(1, done), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
+        "data": "synthetic (seeded uniform ball, clipped-normal radii)",
+        "config": {"workload": args.workload, **w, "grid_nodes": g.node_count},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="spheroid_1M_161")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline sample and parity check")
+    ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "gb300":
+        print("note: fewer than 3 warm-up steps", file=sys.stderr)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    result = run_gpu(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+
+        gathered = [None] * world
+        dist.all_gather_object(gathered, result)
+        results = gathered
+    else:
+        results = [result]
+    if rank == 0:
+        print(json.dumps(report_gpu(args, results, world)))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -51,6 +51,8 @@ int wbc_version(void);
 const char* wbc_last_error(void);
 /* Number of CUDA devices visible to the runtime (0 on a machine without a GPU). */
 int wbc_device_count(void);
+/* Kernels launched by this library in this process so far (all threads and devices). */
+int64_t wbc_launch_count(void);
 
 /* ---- per-cell random streams --------------------------------------------------------------- */
 /* rng_state[i] = stream start of slot i for every slot in [0, capacity).
@@ -129,7 +131,8 @@ typedef struct wbc_sor_params {
 /* `sweeps` red-black SOR sweeps in place (kernels/field_kernels.py:185-212 launched as in
  * fields/diffusion.py:103-112), then, when residual_out is non-NULL, the max-norm residual of
  * the result (kernels/field_kernels.py:215-243) written to residual_out[0] (device float).
- * `fixed` int32[nodes] (non-zero = pinned); `production` and `source` may be NULL. */
+ * `fixed` int32[nodes] (non-zero = pinned) may be NULL when no node is pinned; `production` and
+ * `source` may be NULL. */
 int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed, const float* density,
                    const float* production, const float* source, float* field, float* residual_out,
                    void* stream);

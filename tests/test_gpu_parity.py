@@ -275,10 +275,15 @@ def test_contact_displacement_within_1e5_um_of_fp64():
         before = pop.positions_numpy()
         contact_substep(pop, grid, params, dt=0.1)
         after = pop.positions_numpy()
+        p32 = before.copy()
+        _, nc32 = orc.contact_substep(p32, radii, params.query_radius, 128, params.query_radius, params.rate, 0.1)
+        np.testing.assert_array_equal(pop.neighbor_counts_numpy(), nc32)
+        np.testing.assert_array_equal(after, p32)
+        # FP64 re-run of the same step (its neighbour counts may differ at d == query_radius by
+        # rounding; velocities only involve overlapping pairs, far inside that radius)
         p64 = before.astype(np.float64)
-        vel64, nc = orc.contact_substep(p64, radii, params.query_radius, 128, params.query_radius, params.rate, 0.1,
-                                        fp64=True)
-        np.testing.assert_array_equal(pop.neighbor_counts_numpy(), nc)
+        vel64, _ = orc.contact_substep(p64, radii, params.query_radius, 128, params.query_radius, params.rate, 0.1,
+                                       fp64=True)
         v32 = pop.velocity[: pop.count].cpu().numpy().astype(np.float64)
         assert np.abs(v32 * 0.1 - vel64 * 0.1).max() < 1e-5  # per-step displacement
         ulp = np.spacing(np.abs(before)).astype(np.float64)

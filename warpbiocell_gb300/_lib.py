@@ -114,6 +114,7 @@ SIGNATURES: dict[str, list] = {
     "wbc_version": [],
     "wbc_last_error": [],
     "wbc_device_count": [],
+    "wbc_launch_count": [],
     "wbc_scan_workspace_bytes": [c_int64],
     "wbc_rng_init": [_I, _P, c_int64, _P],
     "wbc_rng_uniform": [_I, _I, _P, _P, _P],
@@ -140,7 +141,7 @@ SIGNATURES: dict[str, list] = {
     "wbc_network_inherit": [_I, _I, _P, _P, _P, _P],
     "wbc_network_count_on": [_I, _I, _I, _P, _I, _P, _P, _P, _P],
 }
-_RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t}
+_RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None
@@ -167,6 +168,11 @@ def load(path: str | Path | None = None) -> ctypes.CDLL:
             fn.restype = _RESTYPE.get(name, c_int32)
         _lib = lib
         return lib
+
+
+def launch_count() -> int:
+    """Kernels launched by libwbc_gb300 in this process so far."""
+    return int(load().wbc_launch_count())
 
 
 def last_error() -> str:

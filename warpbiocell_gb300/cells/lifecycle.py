@@ -12,7 +12,7 @@ from __future__ import annotations
 import ctypes
 from dataclasses import dataclass
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 
 
 class CapacityError(RuntimeError):
@@ -93,6 +93,11 @@ def decide_lifecycle(population, params: LifecycleParams, dt: float) -> None:
     if n == 0:
         return
     p = population
+    with profiling.stage("decide"):
+        _decide(p, params, dt, n)
+
+
+def _decide(p, params: LifecycleParams, dt: float, n: int) -> None:
     _lib.call(
         "wbc_lifecycle_decide",
         ctypes.byref(params.native(dt)),
@@ -114,6 +119,11 @@ def scan_divisions(population) -> None:
     total into the population's device counter (no host sync)."""
     n = population.count
     workspace, total = population.scan_workspace()
+    with profiling.stage("scan", launches=3):
+        _scan(population, n, workspace, total)
+
+
+def _scan(population, n, workspace, total) -> None:
     _lib.call(
         "wbc_division_scan",
         n,
@@ -128,7 +138,11 @@ def scan_divisions(population) -> None:
 
 def place_daughters(population, params: LifecycleParams) -> None:
     """Launch the placement over the current prefix (after :func:`scan_divisions`)."""
-    p = population
+    with profiling.stage("place"):
+        _place(population, params)
+
+
+def _place(p, params: LifecycleParams) -> None:
     _lib.call(
         "wbc_place_daughters",
         p.count,

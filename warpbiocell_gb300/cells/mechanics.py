@@ -12,7 +12,7 @@ from __future__ import annotations
 import ctypes
 from dataclasses import dataclass
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 from warpbiocell_gb300.spatial.neighbors import NeighborGrid
 
 # Explicit Euler on one overlapping pair contracts the overlap by (1 - 2 rate dt) per substep;
@@ -73,18 +73,10 @@ def contact_substep(population, grid: NeighborGrid, params: ContactParams, dt: f
     if n == 0:
         return
     grid.build(population)
-    _lib.call(
-        "wbc_contact_substep",
-        ctypes.byref(grid.struct),
-        n,
-        float(params.query_radius),
-        float(params.rate),
-        float(dt),
-        _lib.ptr(population.position),
-        _lib.ptr(population.velocity),
-        _lib.ptr(population.neighbor_count),
-        _lib.stream(population.device),
-    )
+    with profiling.stage("contact"):
+        _lib.call("wbc_contact_substep", ctypes.byref(grid.struct), n, float(params.query_radius), float(params.rate),
+                  float(dt), _lib.ptr(population.position), _lib.ptr(population.velocity),
+                  _lib.ptr(population.neighbor_count), _lib.stream(population.device))
 
 
 def relax_contacts(population, grid: NeighborGrid, params: ContactParams, dt: float, substeps: int, region=None) -> None:

@@ -156,7 +156,7 @@ __global__ void k_sor_colour(wbc_sor_params p, int colour, const int32_t* __rest
     const int k = 2 * m + ((colour + i + j) & 1);
     if (k >= p.nz) return;
     const int64_t idx = (static_cast<int64_t>(i) * p.ny + j) * p.nz + k;
-    if (fixed[idx] != 0 || on_dirichlet_face(p, i, j, k)) return;
+    if ((fixed && fixed[idx] != 0) || on_dirichlet_face(p, i, j, k)) return;
     const float o = field[idx];
     const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
     const float prod = production_at(p, production, source, idx);
@@ -175,7 +175,7 @@ __global__ void k_residual(wbc_sor_params p, const int32_t* __restrict__ fixed, 
         const int64_t ij = idx / p.nz;
         const int j = static_cast<int>(ij % p.ny);
         const int i = static_cast<int>(ij / p.ny);
-        if (fixed[idx] == 0 && !on_dirichlet_face(p, i, j, k)) {
+        if ((!fixed || fixed[idx] == 0) && !on_dirichlet_face(p, i, j, k)) {
             const float o = field[idx];
             const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
             const float prod = production_at(p, production, source, idx);
@@ -271,7 +271,7 @@ int wbc_sample(const wbc_grid_geometry* geom, const float* field, int32_t n, con
 
 int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed, const float* density,
                    const float* production, const float* source, float* field, float* residual_out, void* stream) {
-    if (!sor_ok(p) || sweeps < 0 || !fixed || !density || !field || (p->has_source && !source))
+    if (!sor_ok(p) || sweeps < 0 || !density || !field || (p->has_source && !source))
         return WBC_ERR_INVALID;
     cudaStream_t s = as_stream(stream);
     const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
@@ -290,7 +290,7 @@ int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed
         k_residual<<<grid_for(nodes), kThreads, 0, s>>>(*p, fixed, density, production, source, field,
                                                         reinterpret_cast<unsigned int*>(residual_out));
     }
-    return check_launch("wbc_sor_sweeps");
+    return check_launch("wbc_sor_sweeps", 2 * static_cast<int64_t>(sweeps) + (residual_out ? 1 : 0));
 }
 
 int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,

@@ -160,7 +160,7 @@ int wbc_grid_build(const wbc_neighbor_grid* grid, int32_t n, const float* positi
     k_bin_order<<<grid_for(n), kThreads, 0, s>>>(n, position, radius, grid->cell_bucket, grid->bucket_start,
                                                  grid->bucket_count, grid->scatter, grid->sorted_id,
                                                  reinterpret_cast<float4*>(grid->sorted_xyzr));
-    return check_launch("wbc_grid_build");
+    return check_launch("wbc_grid_build", 3);
 }
 
 int wbc_contact_substep(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,

@@ -1,5 +1,6 @@
 // Library plumbing: error bookkeeping, version, device count, the multi-block int32 scan used by
 // the hash-grid binning and the division slots, and the test hooks of the random streams.
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 
@@ -9,6 +10,7 @@ namespace wbc {
 
 namespace {
 thread_local char g_error[512] = "no error";
+std::atomic<int64_t> g_launches{0};
 }
 
 void set_error(const char* where, cudaError_t err) {
@@ -17,7 +19,8 @@ void set_error(const char* where, cudaError_t err) {
 
 void set_error_msg(const char* msg) { std::snprintf(g_error, sizeof(g_error), "%s", msg); }
 
-int check_launch(const char* where) {
+int check_launch(const char* where, int64_t launches) {
+    g_launches.fetch_add(launches, std::memory_order_relaxed);
     cudaError_t err = cudaGetLastError();
     if (err != cudaSuccess) {
         set_error(where, err);
@@ -134,7 +137,7 @@ int scan_i32(const int32_t* in, int32_t* out, int64_t n, bool inclusive, int32_t
     scan_reduce_tiles<<<static_cast<unsigned>(tiles), kScanThreads, 0, stream>>>(in, n, partials);
     scan_partials<<<1, kScanThreads, 0, stream>>>(partials, tiles, total);
     scan_tiles<<<static_cast<unsigned>(tiles), kScanThreads, 0, stream>>>(in, out, n, partials, inclusive);
-    return check_launch("scan_i32");
+    return check_launch("scan_i32", 3);
 }
 
 // ---- random-stream test hooks ----------------------------------------------------------------------
@@ -178,6 +181,8 @@ extern "C" {
 int wbc_version(void) { return 1; }
 
 const char* wbc_last_error(void) { return g_error; }
+
+int64_t wbc_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int wbc_device_count(void) {
     int count = 0;

@@ -13,7 +13,7 @@ import ctypes
 import numpy as np
 import torch
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 from warpbiocell_gb300.cells.model import NUM_STATES
 from warpbiocell_gb300.fields.scalar_field import GridGeometry
 
@@ -41,17 +41,19 @@ class CellDensities:
         if population.device != self.device:
             raise RuntimeError("population and CellDensities must live on the same device")
         if population.count > 0:
-            _lib.call("wbc_deposit", ctypes.byref(self._native), population.count, _lib.ptr(population.position),
-                      _lib.ptr(population.cell_state), _lib.ptr(self._accumulator), _lib.stream(self.device))
+            with profiling.stage("deposit"):
+                _lib.call("wbc_deposit", ctypes.byref(self._native), population.count, _lib.ptr(population.position),
+                          _lib.ptr(population.cell_state), _lib.ptr(self._accumulator), _lib.stream(self.device))
 
     def convert(self, weights=None, combined: torch.Tensor | None = None) -> None:
         """density = acc / 2^24 / dx^3 (and optionally combined = sum_k w_k density_k); clears acc."""
         w = None
         if weights is not None:
             w = (ctypes.c_float * 4)(*[float(x) for x in weights])
-        _lib.call("wbc_density_convert", self.geometry.node_count, _lib.ptr(self._accumulator),
-                  1.0 / self.geometry.voxel_volume, _lib.ptr(self.density), w, _lib.ptr(combined), 1,
-                  _lib.stream(self.device))
+        with profiling.stage("convert"):
+            _lib.call("wbc_density_convert", self.geometry.node_count, _lib.ptr(self._accumulator),
+                      1.0 / self.geometry.voxel_volume, _lib.ptr(self.density), w, _lib.ptr(combined), 1,
+                      _lib.stream(self.device))
 
     def deposit(self, population) -> None:
         self.deposit_fixed_point(population)

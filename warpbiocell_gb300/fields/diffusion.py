@@ -14,7 +14,7 @@ from dataclasses import dataclass
 
 import torch
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 from warpbiocell_gb300.fields.scalar_field import ScalarField
 
 
@@ -83,9 +83,10 @@ def sor_params(field: ScalarField, kinetics: UptakeKinetics, omega: float, has_s
 def sor_chunk(field: ScalarField, density: torch.Tensor, params: _lib.SorParamsC, sweeps: int,
               residual_buffer: torch.Tensor | None, production=None, source=None) -> None:
     """``sweeps`` red-black sweeps (and the residual into ``residual_buffer[0]`` when given)."""
-    _lib.call("wbc_sor_sweeps", ctypes.byref(params), int(sweeps), _lib.ptr(field.fixed), _lib.ptr(density),
-              _lib.ptr(production), _lib.ptr(source), _lib.ptr(field.values), _lib.ptr(residual_buffer),
-              _lib.stream(field.device))
+    with profiling.stage("sor", launches=2 * int(sweeps) + (1 if residual_buffer is not None else 0)):
+        _lib.call("wbc_sor_sweeps", ctypes.byref(params), int(sweeps), _lib.ptr(field.fixed_or_none()),
+                  _lib.ptr(density), _lib.ptr(production), _lib.ptr(source), _lib.ptr(field.values),
+                  _lib.ptr(residual_buffer), _lib.stream(field.device))
 
 
 def solve_steady_state(

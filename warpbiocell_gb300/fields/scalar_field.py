@@ -96,12 +96,23 @@ class ScalarField:
         """Pin the nodes where ``mask`` is true to ``boundary_value`` (``None`` clears the mask)."""
         if mask is None:
             self.fixed.zero_()
+            object.__setattr__(self, "_any_fixed", False)
             return
         mask = np.asarray(mask, dtype=bool)
         if mask.shape != tuple(self.geometry.shape):
             raise ValueError(f"mask shape {mask.shape} does not match the grid {self.geometry.shape}")
         self.fixed.copy_(torch.from_numpy(mask.astype(np.int32)))
+        object.__setattr__(self, "_any_fixed", bool(mask.any()))
         self.apply_dirichlet()
+
+    @property
+    def any_fixed(self) -> bool:
+        """True once a node has been pinned with ``set_fixed`` (solvers then read the mask)."""
+        return getattr(self, "_any_fixed", False)
+
+    def fixed_or_none(self) -> torch.Tensor | None:
+        """The pin mask for the kernels, or None when nothing is pinned (the mask is not read)."""
+        return self.fixed if self.any_fixed else None
 
     def fixed_mask(self) -> np.ndarray:
         return self.fixed.cpu().numpy().astype(bool)

@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 from warpbiocell_gb300.cells.model import NUM_STATES, CellState
 from warpbiocell_gb300.fields.densities import CellDensities
 from warpbiocell_gb300.fields.diffusion import (
@@ -150,8 +150,9 @@ class SpeciesField:
         if population.count == 0:
             return
         target = out if out is not None else population.local_field(self.name)
-        _lib.call("wbc_sample", ctypes.byref(self.geometry.native()), _lib.ptr(self.field.values), population.count,
-                  _lib.ptr(population.position), _lib.ptr(target), _lib.stream(self.device))
+        with profiling.stage("sample"):
+            _lib.call("wbc_sample", ctypes.byref(self.geometry.native()), _lib.ptr(self.field.values),
+                      population.count, _lib.ptr(population.position), _lib.ptr(target), _lib.stream(self.device))
 
     # ---- solvers --------------------------------------------------------------------------
     def solve_steady_state(self, source: SpeciesField | None = None) -> SolveReport:

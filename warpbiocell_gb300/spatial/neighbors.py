@@ -15,7 +15,7 @@ import ctypes
 
 import torch
 
-from warpbiocell_gb300 import _lib
+from warpbiocell_gb300 import _lib, profiling
 
 
 class NeighborGrid:
@@ -76,11 +76,6 @@ class NeighborGrid:
         if population.device != self.device:
             raise RuntimeError("population and NeighborGrid must live on the same device")
         self.reserve(max(population.capacity, 1))
-        _lib.call(
-            "wbc_grid_build",
-            ctypes.byref(self._struct),
-            population.count,
-            _lib.ptr(population.position),
-            _lib.ptr(population.radius),
-            _lib.stream(self.device),
-        )
+        with profiling.stage("bin", launches=6):
+            _lib.call("wbc_grid_build", ctypes.byref(self._struct), population.count, _lib.ptr(population.position),
+                      _lib.ptr(population.radius), _lib.stream(self.device))
