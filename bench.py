@@ -72,7 +72,7 @@ def make_params(w: dict):
         settings=SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=2000, check_every=20),
         lifecycle=LifecycleParams(division_rate=math.log(2.0) / 24.0, death_rate=0.0, anoxic_death_rate=0.5,
                                   inhibition_threshold=8, hypoxia_threshold=5.0, death_threshold=1.0),
-        contact=ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, margin=0.0),
+        contact=ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, margin=0.0, wall_rate=4.0),
         stepping=TimeStepping(dt_cells=DT, dt_mechanics=DT),
     )
 

@@ -326,7 +326,7 @@ def test_lifecycle_decide_scan_place_bitwise_equal_oracle(mode):
                  necrosis_requires_glucose=True, phenotype_model=mode, apoptosis_rate=0.3, necrosis_rate=2.0)
     created = lifecycle_step(pop, params, dt=1.0)
     sim.decide_lifecycle(params, 1.0)
-    assert created == sim.commit_divisions(params) and created > 1000
+    assert created == sim.commit_divisions(params) and created > 500
     _compare_pop(pop, sim)
     np.testing.assert_array_equal(pop.division_offset[:n].cpu().numpy(), sim.division_offset[:n])
     np.testing.assert_array_equal(pop.fate_flags_numpy(), sim.fate_flags[: pop.count])
@@ -387,7 +387,7 @@ def _coupled(seed=0, capacity=12000, n=3000, steps=6):
     oparams = OxygenParams(diffusion_coefficient=7.2e6, uptake_max=5.54e7, michaelis_k=1.0, boundary_value=12.0)
     lifecycle = LifecycleParams(division_rate=0.2, death_rate=0.01, anoxic_death_rate=0.5, inhibition_threshold=14,
                                 hypoxia_threshold=5.0, death_threshold=1.0)
-    contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0)
+    contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, wall_rate=4.0)
     stepping = TimeStepping(dt_cells=0.25, dt_mechanics=0.125)
     return pos, radii, geom, settings, oparams, lifecycle, contact, stepping
 
