@@ -136,6 +136,27 @@ typedef struct wbc_sor_params {
 int wbc_sor_sweeps(const wbc_sor_params* p, int32_t sweeps, const int32_t* fixed, const float* density,
                    const float* production, const float* source, float* field, float* residual_out,
                    void* stream);
+typedef struct wbc_sor_report {
+    int32_t sweeps;              /* sweeps performed (a multiple of check_every, or max_sweeps)     */
+    float residual;              /* max-norm residual after the last check                          */
+    int32_t converged;           /* residual < tolerance                                             */
+    int32_t path;                /* 2 = shared-memory resident solver, 1 = streaming colour launches */
+    int32_t tiles;               /* CTAs of the resident solver (0 for the streaming path)           */
+} wbc_sor_report;
+
+/* Scratch bytes wbc_sor_solve needs for this grid (control block + halo exchange buffer). */
+size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p);
+/* Solve to the residual tolerance from the field's current values (warm start), checking the
+ * residual every `check_every` sweeps and stopping at `max_sweeps`: the sweep count, residual and
+ * stopping rule of fields/diffusion.py:79-123 (kernels/field_kernels.py:185-243). path 0 = auto:
+ * one persistent cooperative launch with the field tile resident in shared memory when the grid
+ * fits on chip, otherwise streaming colour launches with a host check per chunk; 1 = streaming;
+ * 2 = resident only. Synchronises `stream` and fills the host-side `report`. The field after the
+ * solve is bit-identical on both paths. Returns WBC_ERR_TIMEOUT if a grid barrier timed out. */
+int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
+                  const int32_t* fixed, const float* density, const float* production, const float* source,
+                  float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
+                  void* stream);
 /* Explicit FTCS step field_out = field_in + dt (D lap - uptake + production) (validation only;
  * kernels/field_kernels.py:246-273). `p->dx2_over_D` carries D/dx^2 here. */
 int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,

@@ -425,3 +425,77 @@ def test_coupled_run_is_reproducible_and_independent_of_capacity():
         assert s[0] == snaps[0][0]
         for a, b in zip(s[1:], snaps[0][1:]):
             np.testing.assert_array_equal(a, b)
+
+
+# ---- the shared-memory resident solver against the streaming colour launches and the oracle ------------
+def _solve_with_path(path, geom, boundary, start, density, pins=None, production=None, source=None, settings=None):
+    from warpbiocell_gb300.fields import diffusion
+    from warpbiocell_gb300.fields.diffusion import solve_steady_state
+    from warpbiocell_gb300.fields.scalar_field import ScalarField
+    from warpbiocell_gb300.fields.diffusion import UptakeKinetics
+
+    f = ScalarField.create(geom, 30.0, boundary=boundary, device=DEV)
+    if pins is not None:
+        f.set_fixed(pins)
+    f.assign(start)
+    kin = UptakeKinetics(2.0e3, 5.0e4, 3.0)
+    res = torch.zeros(1, dtype=torch.float32, device=DEV)
+    old = diffusion.solver_path
+    diffusion.solver_path = path
+    try:
+        rep = solve_steady_state(f, _t(density), kin, settings, res,
+                                 production=None if production is None else _t(production),
+                                 source=None if source is None else _t(source), source_k=0.04)
+        info = dict(diffusion.last_solve)
+    finally:
+        diffusion.solver_path = old
+    return f.numpy(), rep, info
+
+
+@pytest.mark.parametrize("shape, boundary, extras", [
+    ((37, 29, 23), MIXED, False),
+    ((41, 41, 41), (Boundary.DIRICHLET,) * 3, False),
+    ((33, 27, 31), (Boundary.NEUMANN, Boundary.DIRICHLET, Boundary.NEUMANN), True),
+    ((97, 89, 101), (Boundary.DIRICHLET,) * 3, True),
+])
+def test_resident_solver_bitwise_equals_streaming_and_oracle(shape, boundary, extras):
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
+    rng = np.random.default_rng(sum(shape))
+    start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
+    density = rng.uniform(0.0, 2.0e-3, shape).astype(np.float32)
+    pins = (rng.random(shape) < 0.02) if extras else None
+    production = rng.uniform(0.0, 40.0, shape).astype(np.float32) if extras else None
+    source = rng.uniform(0.0, 5.0, shape).astype(np.float32) if extras else None
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=300, check_every=20)
+    a, ra, ia = _solve_with_path(1, geom, boundary, start, density, pins, production, source, settings)
+    b, rb, ib = _solve_with_path(2, geom, boundary, start, density, pins, production, source, settings)
+    assert ia["path"] == 1 and ib["path"] == 2 and ib["tiles"] >= 1
+    assert (ra.sweeps, ra.converged, ra.residual) == (rb.sweeps, rb.converged, rb.residual)
+    np.testing.assert_array_equal(a, b)
+    # oracle: same start (Dirichlet faces / pins re-imposed as ScalarField.assign does)
+    from warpbiocell_gb300.fields.scalar_field import ScalarField
+
+    f = ScalarField.create(geom, 30.0, boundary=boundary, device=DEV)
+    if pins is not None:
+        f.set_fixed(pins)
+    f.assign(start)
+    values = f.numpy()
+    p = orc.sor_params(orc.Geometry(geom.origin, geom.dx, geom.shape), f.boundary_flags, 30.0, 2.0e3, 5.0e4, 3.0, 1.8,
+                       1 if source is not None else 0, 0.04)
+    fixed = pins.astype(np.int32) if pins is not None else np.zeros(shape, np.int32)
+    sweeps, residual, ok = orc.solve_steady_state(p, settings, fixed, density, values, production, source)
+    assert (sweeps, ok) == (rb.sweeps, rb.converged) and np.float32(residual) == rb.residual
+    np.testing.assert_array_equal(b, values)
+
+
+def test_resident_solver_runs_the_benchmark_grid():
+    geom = GridGeometry.centered_cube(2400.0, 15.0)
+    x, y, z = np.meshgrid(*geom.node_coordinates(), indexing="ij")
+    density = np.where(x**2 + y**2 + z**2 < 1100.0**2, 1.5e-4, 0.0).astype(np.float32)
+    start = np.full(geom.shape, 100.0, np.float32)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=100, check_every=20)
+    a, ra, ia = _solve_with_path(1, geom, (Boundary.DIRICHLET,) * 3, start, density, settings=settings)
+    b, rb, ib = _solve_with_path(2, geom, (Boundary.DIRICHLET,) * 3, start, density, settings=settings)
+    assert ib["path"] == 2 and ib["tiles"] > 100
+    assert (ra.sweeps, ra.residual) == (rb.sweeps, rb.residual)
+    np.testing.assert_array_equal(a, b)

@@ -74,6 +74,16 @@ class SorParamsC(ctypes.Structure):
     ]
 
 
+class SorReportC(ctypes.Structure):
+    _fields_ = [
+        ("sweeps", c_int32),
+        ("residual", c_float),
+        ("converged", c_int32),
+        ("path", c_int32),
+        ("tiles", c_int32),
+    ]
+
+
 class LifecycleParamsC(ctypes.Structure):
     _fields_ = [
         ("dt", c_float),
@@ -128,6 +138,9 @@ SIGNATURES: dict[str, list] = {
     "wbc_sample": [POINTER(GridGeometryC), _P, _I, _P, _P, _P],
     "wbc_sor_sweeps": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P],
     "wbc_ftcs_step": [POINTER(SorParamsC), _F, _P, _P, _P, _P, _P, _P, _P],
+    "wbc_sor_solve_workspace_bytes": [POINTER(SorParamsC)],
+    "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, POINTER(SorReportC), _P,
+                      c_size_t, _I, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
     "wbc_place_daughters": [_I, _F, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
@@ -141,7 +154,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_network_inherit": [_I, _I, _P, _P, _P, _P],
     "wbc_network_count_on": [_I, _I, _I, _P, _I, _P, _P, _P, _P],
 }
-_RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64}
+_RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64,
+            "wbc_sor_solve_workspace_bytes": c_size_t}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

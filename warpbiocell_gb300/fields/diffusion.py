@@ -106,16 +106,33 @@ def solve_steady_state(
     """
     prod, has_source, src, source_k = _source_args(field, production, source, source_k)
     params = sor_params(field, kinetics, settings.omega, has_source, source_k)
-    sweeps = 0
-    residual = float("inf")
-    while sweeps < settings.max_sweeps:
-        chunk = min(settings.check_every, settings.max_sweeps - sweeps)
-        sor_chunk(field, density, params, chunk, residual_buffer, prod, src)
-        sweeps += chunk
-        residual = float(residual_buffer[0].item())
-        if residual < settings.tolerance:
-            return SolveReport(sweeps=sweeps, residual=residual, converged=True)
-    return SolveReport(sweeps=sweeps, residual=residual, converged=False)
+    workspace = _workspace(field, params)
+    report = _lib.SorReportC()
+    with profiling.stage("sor"):
+        _lib.call("wbc_sor_solve", ctypes.byref(params), int(settings.check_every), int(settings.max_sweeps),
+                  float(settings.tolerance), _lib.ptr(field.fixed_or_none()), _lib.ptr(density), _lib.ptr(prod),
+                  _lib.ptr(src), _lib.ptr(field.values), ctypes.byref(report), _lib.ptr(workspace),
+                  workspace.numel(), int(solver_path), _lib.stream(field.device))
+    residual_buffer.fill_(float(report.residual))
+    last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles)
+    return SolveReport(sweeps=int(report.sweeps), residual=float(report.residual), converged=bool(report.converged))
+
+
+# 0: the shared-memory resident solver when the grid fits on chip, else streaming colour launches;
+# 1: streaming colour launches only; 2: resident only (an error if the grid does not fit).
+solver_path = 0
+# sweeps / path / CTA count of the most recent solve (for benchmarks and tests)
+last_solve: dict = {}
+
+
+def _workspace(field: ScalarField, params: _lib.SorParamsC) -> torch.Tensor:
+    """Scratch of the solver (control block, halo exchange and coefficient planes), per field."""
+    nbytes = int(_lib.load().wbc_sor_solve_workspace_bytes(ctypes.byref(params)))
+    ws = getattr(field, "_sor_workspace", None)
+    if ws is None or ws.numel() < nbytes:
+        ws = torch.empty(nbytes, dtype=torch.uint8, device=field.device)
+        object.__setattr__(field, "_sor_workspace", ws)
+    return ws
 
 
 def max_stable_dt(field: ScalarField, kinetics: UptakeKinetics) -> float:
