@@ -3,20 +3,21 @@
 //
 // Decomposition: the (i, j) plane is cut into tx x ty tiles of ti x tj columns; each CTA (one
 // per SM) owns one tile with the full z extent. Shared memory holds the tile plus a one-column
-// halo ring, split by k parity (E[col][m] = f(k = 2m), O[col][m] = f(k = 2m + 1)) so a warp
-// updating consecutive nodes of one colour reads consecutive words. At the start each CTA
+// halo ring, split by k parity (E[col][m] = f(k = 2m), O[col][m] = f(k = 2m + 1)): within a
+// column all nodes of one colour share a k parity, so a warp that owns a column updates its
+// colour with 32 consecutive words per access and no bank conflicts. At the start each CTA
 // writes the uptake coefficients density * uptake_max of its columns, split the same way, to an
 // L2-resident scratch copy (a negative value marks the nodes that are never updated: Dirichlet
-// faces and pinned nodes), so a colour reads only its own coefficients, contiguously.
+// faces and pinned nodes); a colour reads only its own coefficients, contiguously.
 //
-// One colour half-sweep = update the owned nodes of that colour from shared memory, publish the
-// updated colour of the columns within one column of the tile edge to a parity-split exchange
-// buffer in global memory (L2 resident, bypassing L1), a grid barrier, then pull the halo
-// ring's updated colour back into shared memory. Every `check_every` sweeps the max-norm
-// residual is reduced (warp shuffles, one atomicMax per CTA) and all CTAs stop together once it
-// is below the tolerance: the reference's sweep count, residual and stopping rule, with no host
-// round trip. Each node's update is the reference kernel's float expression in the same order,
-// so the field after n sweeps is bit-identical to the oracle's and to the streaming kernels'.
+// One colour half-sweep = every warp updates its columns' nodes of that colour from shared
+// memory; the tile-edge columns' updated colour is published to a parity-split exchange buffer
+// in global memory (L2, bypassing L1); a grid barrier; then the halo ring's updated colour is
+// pulled back into shared memory. Every `check_every` sweeps the max-norm residual is reduced
+// (warp shuffles, one atomicMax per CTA) and all CTAs stop together once it is below the
+// tolerance: the reference's sweep count, residual and stopping rule, with no host round trip.
+// Each node's update is the reference kernel's float expression in the same order, so the field
+// after n sweeps is bit-identical to the oracle's and to the streaming kernels'.
 //
 // The grid barrier polls a bounded number of times (about a second); on timeout the CTA raises
 // an abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
@@ -56,8 +57,8 @@ struct SorArgs {
     const float* production;
     const float* source;
     float* field;
-    float* xchg;    // [2][nx][ny][M] halo exchange
-    float* coeff;   // [2][nx][ny][M] density * uptake_max, -1 where not updated
+    float* xchg;   // [2][nx][ny][M] halo exchange
+    float* coeff;  // [2][nx][ny][M] density * uptake_max, -1 where not updated
     SorControl* ctl;
     int check_every;
     int max_sweeps;
@@ -65,6 +66,7 @@ struct SorArgs {
 };
 
 constexpr unsigned kBarrierPolls = 1u << 24;  // x ~64 ns sleep: about a second
+constexpr int kMaxLanesPerColumn = 8;         // M <= 256 (nz <= 511)
 
 __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n - 1 ? n - 2 : i); }
 
@@ -86,7 +88,7 @@ __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned nblocks, 
                     atomicExch(&ctl->abort, 1u);
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __threadfence();
@@ -102,40 +104,6 @@ struct TileGeom {
     int stride_i;        // columns per smem row (tj + 2)
     int ncm;             // (ti + 2) * (tj + 2) * M: floats per parity plane in shared memory
 };
-
-// Slot walker: the thread's slots are linear indices t, t + T, ... over (li, lj, m) in
-// [0,ai) x [0,aj) x [0,M), advanced incrementally (no division inside the sweep loops).
-struct Walker {
-    int li, lj, m;
-    int dli, dlj, dm;
-    __device__ __forceinline__ void step(int M, int aj) {
-        m += dm;
-        lj += dlj;
-        li += dli;
-        if (m >= M) {
-            m -= M;
-            lj += 1;
-        }
-        if (lj >= aj) {
-            lj -= aj;
-            li += 1;
-        }
-    }
-};
-
-__device__ __forceinline__ Walker make_walker(int M, int aj) {
-    Walker w;
-    const int t = threadIdx.x, T = blockDim.x;
-    const int lc = t / M;
-    w.m = t - lc * M;
-    w.li = lc / aj;
-    w.lj = lc - w.li * aj;
-    const int dlc = T / M;
-    w.dm = T - dlc * M;
-    w.dli = dlc / aj;
-    w.dlj = dlc - w.dli * aj;
-    return w;
-}
 
 // Sum of the six neighbours (im, ip, jm, jp, km, kp in the reference's order), mirrored in k.
 __device__ __forceinline__ float neighbour_sum(const float* s, int ncm, int M, int nz, int stride_i, int c2, int k) {
@@ -155,56 +123,37 @@ __device__ __forceinline__ float prod_term(const SorArgs& a, int64_t idx) {
     return prod * (v / (a.p.source_k + v));
 }
 
-// Publish the updated colour of the columns within one column of the tile edge (pull = false),
-// or pull the halo ring's updated colour from the exchange buffer (pull = true).
-__device__ __forceinline__ void exchange(float* s, const SorArgs& a, const TileGeom& g, int colour, bool pull) {
-    const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
-    const int perim = pull ? 2 * (g.ai + g.aj) : 4 * (g.ai + g.aj);
-    const int total = perim * M;
-    for (int e = threadIdx.x; e < total; e += blockDim.x) {
-        const int r = e / M;
-        const int m = e - r * M;
-        int li, lj;
-        if (pull) {
-            if (r < g.aj) {
-                li = -1;
-                lj = r;
-            } else if (r < 2 * g.aj) {
-                li = g.ai;
-                lj = r - g.aj;
-            } else if (r < 2 * g.aj + g.ai) {
-                li = r - 2 * g.aj;
-                lj = -1;
-            } else {
-                li = r - 2 * g.aj - g.ai;
-                lj = g.aj;
-            }
-        } else {
-            // rows li in {0, 1, ai-2, ai-1} x all lj, then columns lj in {0, 1, aj-2, aj-1} x all li
-            if (r < 4 * g.aj) {
-                const int which = r / g.aj;
-                lj = r - which * g.aj;
-                li = which < 2 ? which : g.ai - 4 + which;
-            } else {
-                const int q = r - 4 * g.aj;
-                const int which = q / g.ai;
-                li = q - which * g.ai;
-                lj = which < 2 ? which : g.aj - 4 + which;
-            }
-            if (li < 0 || li >= g.ai || lj < 0 || lj >= g.aj) continue;
-        }
-        const int gi_u = g.i0 + li, gj_u = g.j0 + lj;
-        const int kpar = (colour + gi_u + gj_u) & 1;  // mirroring moves i, j by 2: parity kept
-        if (2 * m + kpar >= nz) continue;
-        const int c2 = (li + 1) * g.stride_i + (lj + 1);
-        const int gi = mirror(gi_u, nx), gj = mirror(gj_u, ny);
-        float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M + m;
-        float* sm = s + kpar * g.ncm + c2 * M + m;
-        if (pull)
-            *sm = __ldcg(x);
-        else
-            __stcg(x, *sm);
+// Column r of the halo ring (pull) as tile coordinates.
+__device__ __forceinline__ void ring_column(const TileGeom& g, int r, int& li, int& lj) {
+    if (r < g.aj) {
+        li = -1;
+        lj = r;
+    } else if (r < 2 * g.aj) {
+        li = g.ai;
+        lj = r - g.aj;
+    } else if (r < 2 * g.aj + g.ai) {
+        li = r - 2 * g.aj;
+        lj = -1;
+    } else {
+        li = r - 2 * g.aj - g.ai;
+        lj = g.aj;
     }
+}
+
+// Column r of the published set: rows rows[0..nrow) x all lj, then cols[0..ncol) x all li.
+__device__ __forceinline__ bool publish_column(const TileGeom& g, const int* rows, int nrow, const int* cols, int r,
+                                               int& li, int& lj) {
+    if (r < nrow * g.aj) {
+        const int q = r / g.aj;
+        li = rows[q];
+        lj = r - q * g.aj;
+    } else {
+        const int rr = r - nrow * g.aj;
+        const int q = rr / g.ai;
+        lj = cols[q];
+        li = rr - q * g.ai;
+    }
+    return li >= 0 && li < g.ai && lj >= 0 && lj < g.aj;
 }
 
 template <bool HAS_PROD>
@@ -213,6 +162,7 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     __shared__ unsigned int s_red[32];
     __shared__ int s_abort;
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     TileGeom g;
     {
         const int bx = blockIdx.x / a.t.ty;
@@ -225,29 +175,46 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         g.ncm = (a.t.ti + 2) * (a.t.tj + 2) * M;
     }
     const int64_t sx = static_cast<int64_t>(ny) * nz;
+    // Columns other tiles read: the edge rows / columns, plus the second one on a Neumann face
+    // (its mirror image is the halo of this very tile).
+    int rows[4], cols[4], nrow = 0, ncol = 0;
+    rows[nrow++] = 0;
+    if (g.ai > 1) rows[nrow++] = g.ai - 1;
+    if (a.p.bc_x == 1 && g.i0 == 0 && g.ai > 1) rows[nrow++] = 1;
+    if (a.p.bc_x == 1 && g.i0 + g.ai == nx && g.ai > 2) rows[nrow++] = g.ai - 2;
+    cols[ncol++] = 0;
+    if (g.aj > 1) cols[ncol++] = g.aj - 1;
+    if (a.p.bc_y == 1 && g.j0 == 0 && g.aj > 1) cols[ncol++] = 1;
+    if (a.p.bc_y == 1 && g.j0 + g.aj == ny && g.aj > 2) cols[ncol++] = g.aj - 2;
+    const int n_publish = nrow * g.aj + ncol * g.ai;
+    const int n_ring = 2 * (g.ai + g.aj);
+    const int ncolumns = g.ai * g.aj;
+    const int lanes_m = (M + 31) >> 5;
 
     // Tile + halo ring (mirrored at the domain faces) into shared memory; the owned columns'
     // coefficients into the parity-split scratch copy.
     {
-        const int cols = (g.ai + 2) * (g.aj + 2);
-        for (int e = threadIdx.x; e < cols * nz; e += blockDim.x) {
-            const int col = e / nz;
-            const int k = e - col * nz;
-            const int lrow = col / (g.aj + 2);
-            const int li = lrow - 1, lj = col - lrow * (g.aj + 2) - 1;
-            const int gi_u = g.i0 + li, gj_u = g.j0 + lj;
-            const int gi = mirror(gi_u, nx), gj = mirror(gj_u, ny);
+        const int span = g.aj + 2;
+        const int cols_all = (g.ai + 2) * span;
+        for (int col = warp; col < cols_all; col += nwarps) {
+            const int lrow = col / span;
+            const int li = lrow - 1, lj = col - lrow * span - 1;
+            const int gi = mirror(g.i0 + li, nx), gj = mirror(g.j0 + lj, ny);
             const int c2 = (li + 1) * g.stride_i + (lj + 1);
-            const int64_t idx = gi * sx + static_cast<int64_t>(gj) * nz + k;
-            s[(k & 1) * g.ncm + c2 * M + (k >> 1)] = a.field[idx];
-            if (li >= 0 && li < g.ai && lj >= 0 && lj < g.aj) {
-                const wbc_sor_params& p = a.p;
-                const bool face = (p.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
-                                  (p.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
-                                  (p.bc_z == 0 && (k == 0 || k == nz - 1));
-                float v = -1.0f;
-                if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
-                a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+            const bool owned = li >= 0 && li < g.ai && lj >= 0 && lj < g.aj;
+            const int64_t base = gi * sx + static_cast<int64_t>(gj) * nz;
+            for (int k = lane; k < nz; k += 32) {
+                const int64_t idx = base + k;
+                s[(k & 1) * g.ncm + c2 * M + (k >> 1)] = a.field[idx];
+                if (owned) {
+                    const wbc_sor_params& p = a.p;
+                    const bool face = (p.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
+                                      (p.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
+                                      (p.bc_z == 0 && (k == 0 || k == nz - 1));
+                    float v = -1.0f;
+                    if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
+                    a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+                }
             }
         }
     }
@@ -257,7 +224,6 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     const float one_minus_omega = 1.0f - omega;
     const float h = a.p.dx2_over_D;
     const float K = a.p.michaelis_k;
-    const int slots = g.ai * g.aj * M;
     unsigned gen = 0;
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
@@ -268,28 +234,62 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         const int chunk = min(a.check_every, a.max_sweeps - sweeps);
         for (int sweep = 0; sweep < chunk && ok; ++sweep) {
             for (int colour = 0; colour < 2 && ok; ++colour) {
-                Walker w = make_walker(M, g.aj);
-                for (int L = threadIdx.x; L < slots; L += blockDim.x, w.step(M, g.aj)) {
-                    const int gi = g.i0 + w.li, gj = g.j0 + w.lj;
+                for (int col = warp; col < ncolumns; col += nwarps) {
+                    const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+                    const int gi = g.i0 + li, gj = g.j0 + lj;
                     const int kp = (colour + gi + gj) & 1;
-                    const int k = 2 * w.m + kp;
-                    if (k >= nz) continue;
-                    const float du = a.coeff[((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M + w.m];
-                    if (!(du >= 0.0f)) continue;
-                    const int c2 = (w.li + 1) * g.stride_i + (w.lj + 1);
-                    float* own = s + kp * g.ncm + c2 * M + w.m;
-                    const float o = *own;
-                    const float c = du / (K + o);
-                    float prod = 0.0f;
-                    if (HAS_PROD) prod = prod_term(a, gi * sx + static_cast<int64_t>(gj) * nz + k);
-                    const float gs = (neighbour_sum(s, g.ncm, M, nz, g.stride_i, c2, k) + h * prod) / (6.0f + h * c);
-                    *own = fmaxf(one_minus_omega * o + omega * gs, 0.0f);
+                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
+                    const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
+                    float du[kMaxLanesPerColumn];
+#pragma unroll
+                    for (int r = 0; r < kMaxLanesPerColumn; ++r) {
+                        const int m = lane + 32 * r;
+                        du[r] = (r < lanes_m && m < M) ? crow[m] : -1.0f;
+                    }
+#pragma unroll
+                    for (int r = 0; r < kMaxLanesPerColumn; ++r) {
+                        if (r >= lanes_m) break;
+                        const int m = lane + 32 * r;
+                        const int k = 2 * m + kp;
+                        if (!(du[r] >= 0.0f) || k >= nz) continue;
+                        float* own = s + kp * g.ncm + c2 * M + m;
+                        const float o = *own;
+                        const float c = du[r] / (K + o);
+                        float prod = 0.0f;
+                        if (HAS_PROD) prod = prod_term(a, gi * sx + static_cast<int64_t>(gj) * nz + k);
+                        const float gs =
+                            (neighbour_sum(s, g.ncm, M, nz, g.stride_i, c2, k) + h * prod) / (6.0f + h * c);
+                        *own = fmaxf(one_minus_omega * o + omega * gs, 0.0f);
+                    }
                 }
                 __syncthreads();
-                exchange(s, a, g, colour, false);
+                // publish the updated colour of the columns other tiles read
+                for (int r = warp; r < n_publish; r += nwarps) {
+                    int li, lj;
+                    if (!publish_column(g, rows, nrow, cols, r, li, lj)) continue;
+                    const int gi = g.i0 + li, gj = g.j0 + lj;
+                    const int kpar = (colour + gi + gj) & 1;
+                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
+                    float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
+                    const float* sm = s + kpar * g.ncm + c2 * M;
+                    for (int m = lane; m < M; m += 32)
+                        if (2 * m + kpar < nz) __stcg(x + m, sm[m]);
+                }
                 ok = grid_barrier(a.ctl, gridDim.x, gen, &s_abort);
                 if (!ok) break;
-                exchange(s, a, g, colour, true);
+                // pull the halo ring's updated colour (mirroring moves i, j by 2: parity kept)
+                for (int r = warp; r < n_ring; r += nwarps) {
+                    int li, lj;
+                    ring_column(g, r, li, lj);
+                    const int gi_u = g.i0 + li, gj_u = g.j0 + lj;
+                    const int kpar = (colour + gi_u + gj_u) & 1;
+                    const int gi = mirror(gi_u, nx), gj = mirror(gj_u, ny);
+                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
+                    const float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
+                    float* sm = s + kpar * g.ncm + c2 * M;
+                    for (int m = lane; m < M; m += 32)
+                        if (2 * m + kpar < nz) sm[m] = __ldcg(x + m);
+                }
                 __syncthreads();
             }
         }
@@ -297,18 +297,18 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         sweeps += chunk;
         // Max-norm residual of the current field over every updated node.
         unsigned int bits = 0u;
-        {
-            Walker w = make_walker(M, g.aj);
-            for (int L = threadIdx.x; L < slots; L += blockDim.x, w.step(M, g.aj)) {
-                const int gi = g.i0 + w.li, gj = g.j0 + w.lj;
-                const int c2 = (w.li + 1) * g.stride_i + (w.lj + 1);
-#pragma unroll
-                for (int kp = 0; kp < 2; ++kp) {
-                    const int k = 2 * w.m + kp;
+        for (int col = warp; col < ncolumns; col += nwarps) {
+            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+            const int gi = g.i0 + li, gj = g.j0 + lj;
+            const int c2 = (li + 1) * g.stride_i + (lj + 1);
+            for (int kp = 0; kp < 2; ++kp) {
+                const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
+                for (int m = lane; m < M; m += 32) {
+                    const int k = 2 * m + kp;
                     if (k >= nz) continue;
-                    const float du = a.coeff[((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M + w.m];
+                    const float du = crow[m];
                     if (!(du >= 0.0f)) continue;
-                    const float o = s[kp * g.ncm + c2 * M + w.m];
+                    const float o = s[kp * g.ncm + c2 * M + m];
                     const float c = du / (K + o);
                     float prod = 0.0f;
                     if (HAS_PROD) prod = prod_term(a, gi * sx + static_cast<int64_t>(gj) * nz + k);
@@ -320,14 +320,14 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = bits;
+        if (lane == 0) s_red[warp] = bits;
         __syncthreads();
         const int slot = chunk_index & 1;
-        if (threadIdx.x < 32) {
-            bits = threadIdx.x < (blockDim.x >> 5) ? s_red[threadIdx.x] : 0u;
+        if (warp == 0) {
+            bits = lane < nwarps ? s_red[lane] : 0u;
 #pragma unroll
             for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
-            if (threadIdx.x == 0) atomicMax(&a.ctl->res_bits[slot], bits);
+            if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
         }
         ok = grid_barrier(a.ctl, gridDim.x, gen, &s_abort);
         if (!ok) break;
@@ -345,15 +345,11 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         return;
     }
     // Owned columns back to the field.
-    {
-        const int cols = g.ai * g.aj;
-        for (int e = threadIdx.x; e < cols * nz; e += blockDim.x) {
-            const int col = e / nz;
-            const int k = e - col * nz;
-            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-            const int c2 = (li + 1) * g.stride_i + (lj + 1);
-            a.field[(g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz + k] = s[(k & 1) * g.ncm + c2 * M + (k >> 1)];
-        }
+    for (int col = warp; col < ncolumns; col += nwarps) {
+        const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+        const int c2 = (li + 1) * g.stride_i + (lj + 1);
+        float* out = a.field + (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz;
+        for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * g.ncm + c2 * M + (k >> 1)];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ctl->sweeps = sweeps;
@@ -393,6 +389,7 @@ static DeviceInfo device_info() {
 // halo perimeter); the tile plus halo must fit in shared memory.
 static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, SorTiling* out) {
     const int M = (p.nz + 1) / 2;
+    if (M > 32 * kMaxLanesPerColumn) return false;
     bool found = false;
     SorTiling best{};
     long best_score = 0;
@@ -408,9 +405,8 @@ static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, S
             if (!found || score < best_score) {
                 found = true;
                 best_score = score;
-                const long cells = static_cast<long>(ti) * tj * M;
-                const int threads = cells >= 1024 ? 1024 : static_cast<int>(((cells + 31) / 32) * 32);
-                best = SorTiling{ex, ey, ti, tj, M, threads, smem};
+                const int warps = std::min(32, ti * tj);
+                best = SorTiling{ex, ey, ti, tj, M, 32 * warps, smem};
             }
         }
     }
