@@ -5,10 +5,11 @@
 // per SM) owns one tile with the full z extent. Shared memory holds the tile plus a one-column
 // halo ring, split by k parity (E[col][m] = f(k = 2m), O[col][m] = f(k = 2m + 1)): within a
 // column all nodes of one colour share a k parity, so a warp that owns a column updates its
-// colour with 32 consecutive words per access and no bank conflicts. At the start each CTA
-// writes the uptake coefficients density * uptake_max of its columns, split the same way, to an
-// L2-resident scratch copy (a negative value marks the nodes that are never updated: Dirichlet
-// faces and pinned nodes); a colour reads only its own coefficients, contiguously.
+// colour with 32 consecutive words per access and no bank conflicts, and the k-neighbours of
+// node m are entries m - 1 + kp and m + kp of the other parity (clamped at the ends, which is
+// exactly the reference's mirror rule). At the start each CTA writes the uptake coefficients
+// density * uptake_max of its columns, split the same way, to an L2-resident scratch copy (a
+// negative value marks the nodes that are never updated: Dirichlet faces and pinned nodes).
 //
 // One colour half-sweep = every warp updates its columns' nodes of that colour from shared
 // memory; the tile-edge columns' updated colour is published to a parity-split exchange buffer
@@ -19,8 +20,10 @@
 // Each node's update is the reference kernel's float expression in the same order, so the field
 // after n sweeps is bit-identical to the oracle's and to the streaming kernels'.
 //
-// The grid barrier polls a bounded number of times (about a second); on timeout the CTA raises
-// an abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
+// Grid barrier: every CTA stores the barrier's epoch to its own flag (release), then its threads
+// poll all CTAs' flags in parallel (acquire); no two CTAs update the same word. The polls are
+// bounded (about a second); on timeout the CTA raises an abort flag, every CTA leaves, and the
+// host gets WBC_ERR_TIMEOUT.
 #include <algorithm>
 #include <mutex>
 
@@ -28,18 +31,17 @@
 
 namespace wbc {
 
-struct SorControl {
-    unsigned int bar_count;
-    unsigned int bar_gen;
+struct __align__(128) SorControl {
     unsigned int abort;
     unsigned int res_bits[2];
     int sweeps;
     float residual;
     int converged;
     int status;
-    int pad[7];
+    int pad[25];
 };
-static_assert(sizeof(SorControl) == 64, "SorControl is one 64-byte block");
+static_assert(sizeof(SorControl) == 128, "SorControl is one 128-byte line");
+constexpr int kMaxCtas = 1024;  // barrier flags that follow the control block
 
 struct SorTiling {
     int tx, ty;  // CTAs along i and j
@@ -60,43 +62,55 @@ struct SorArgs {
     float* xchg;   // [2][nx][ny][M] halo exchange
     float* coeff;  // [2][nx][ny][M] density * uptake_max, -1 where not updated
     SorControl* ctl;
+    unsigned int* flags;  // [gridDim.x] barrier epochs
     int check_every;
     int max_sweeps;
     double tolerance;  // compared in double, as the reference compares float(residual) < tolerance
 };
 
-constexpr unsigned kBarrierPolls = 1u << 24;  // x ~64 ns sleep: about a second
+constexpr unsigned kBarrierPolls = 1u << 21;  // L2 round trips: about a second
 constexpr int kMaxLanesPerColumn = 8;         // M <= 256 (nz <= 511)
+
+__device__ __forceinline__ unsigned int load_acquire(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void store_release(unsigned int* p, unsigned int v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n - 1 ? n - 2 : i); }
 
-// Returns false when the barrier was aborted (timeout here or elsewhere).
-__device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned nblocks, unsigned& gen, int* s_abort) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
-        if (arrived == nblocks - 1) {
-            atomicExch(&ctl->bar_count, 0u);
-            __threadfence();
-            atomicAdd(&ctl->bar_gen, 1u);
-        } else {
-            unsigned polls = 0;
-            while (atomicAdd(&ctl->bar_gen, 0u) == gen) {
-                if (atomicAdd(&ctl->abort, 0u) != 0u) break;
-                if (++polls > kBarrierPolls) {
-                    atomicExch(&ctl->abort, 1u);
+// Signals this CTA's arrival at the next epoch, then waits for the CTAs listed in `wait_for`
+// (n_wait of them) or, with n_wait < 0, for every CTA. Returns false when aborted (timeout here or
+// elsewhere). A halo exchange only needs the four neighbouring tiles; the residual needs all.
+__device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch,
+                                             const int* wait_for = nullptr, int n_wait = -1) {
+    epoch += 1;
+    __syncthreads();  // the CTA's writes happen before thread 0's release (bar.sync is cumulative)
+    if (threadIdx.x == 0) store_release(flags + blockIdx.x, epoch);
+    int aborted = 0;
+    const unsigned n = n_wait < 0 ? gridDim.x : static_cast<unsigned>(n_wait);
+    for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
+        const unsigned who = n_wait < 0 ? t : static_cast<unsigned>(wait_for[t]);
+        unsigned polls = 0;
+        while (static_cast<int>(load_acquire(flags + who) - epoch) < 0) {
+            if ((++polls & 255u) == 0u) {
+                if (load_acquire(&ctl->abort) != 0u) {
+                    aborted = 1;
                     break;
                 }
-                __nanosleep(32);
+                if (polls > kBarrierPolls) {
+                    atomicExch(&ctl->abort, 1u);
+                    aborted = 1;
+                    break;
+                }
             }
         }
-        __threadfence();
-        *s_abort = atomicAdd(&ctl->abort, 0u) != 0u;
     }
-    gen += 1;
-    __syncthreads();
-    return *s_abort == 0;
+    return __syncthreads_or(aborted) == 0;
 }
 
 struct TileGeom {
@@ -104,17 +118,6 @@ struct TileGeom {
     int stride_i;        // columns per smem row (tj + 2)
     int ncm;             // (ti + 2) * (tj + 2) * M: floats per parity plane in shared memory
 };
-
-// Sum of the six neighbours (im, ip, jm, jp, km, kp in the reference's order), mirrored in k.
-__device__ __forceinline__ float neighbour_sum(const float* s, int ncm, int M, int nz, int stride_i, int c2, int k) {
-    const int par = (k & 1) * ncm;
-    const int km = k - 1 < 0 ? 1 : k - 1;
-    const int kp = k + 1 > nz - 1 ? nz - 2 : k + 1;
-    const int mk = k >> 1;
-    return s[par + (c2 - stride_i) * M + mk] + s[par + (c2 + stride_i) * M + mk] + s[par + (c2 - 1) * M + mk] +
-           s[par + (c2 + 1) * M + mk] + s[(km & 1) * ncm + c2 * M + (km >> 1)] +
-           s[(kp & 1) * ncm + c2 * M + (kp >> 1)];
-}
 
 __device__ __forceinline__ float prod_term(const SorArgs& a, int64_t idx) {
     const float prod = a.production ? a.production[idx] : 0.0f;
@@ -140,7 +143,7 @@ __device__ __forceinline__ void ring_column(const TileGeom& g, int r, int& li, i
     }
 }
 
-// Column r of the published set: rows rows[0..nrow) x all lj, then cols[0..ncol) x all li.
+// Column r of the published set: rows[0..nrow) x all lj, then cols[0..ncol) x all li.
 __device__ __forceinline__ bool publish_column(const TileGeom& g, const int* rows, int nrow, const int* cols, int r,
                                                int& li, int& lj) {
     if (r < nrow * g.aj) {
@@ -156,14 +159,14 @@ __device__ __forceinline__ bool publish_column(const TileGeom& g, const int* row
     return li >= 0 && li < g.ai && lj >= 0 && lj < g.aj;
 }
 
-template <bool HAS_PROD>
+template <bool HAS_PROD, int LANES>
 __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     extern __shared__ float s[];
     __shared__ unsigned int s_red[32];
-    __shared__ int s_abort;
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     TileGeom g;
+    int neighbours[4], n_neighbours = 0;  // tiles whose edge columns form this tile's halo
     {
         const int bx = blockIdx.x / a.t.ty;
         const int by = blockIdx.x - bx * a.t.ty;
@@ -173,8 +176,16 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         g.aj = min(a.t.tj, ny - g.j0);
         g.stride_i = a.t.tj + 2;
         g.ncm = (a.t.ti + 2) * (a.t.tj + 2) * M;
+        if (bx > 0) neighbours[n_neighbours++] = blockIdx.x - a.t.ty;
+        if (bx + 1 < a.t.tx) neighbours[n_neighbours++] = blockIdx.x + a.t.ty;
+        if (by > 0) neighbours[n_neighbours++] = blockIdx.x - 1;
+        if (by + 1 < a.t.ty) neighbours[n_neighbours++] = blockIdx.x + 1;
     }
+    // Per (column, colour) table after the two parity planes: shared-memory offsets of the own
+    // and other parity column, the coefficient row, and the entry count / last other entry / parity.
+    int4* tab = reinterpret_cast<int4*>(s + ((2 * g.ncm + 3) & ~3));
     const int64_t sx = static_cast<int64_t>(ny) * nz;
+    const int si = g.stride_i * M;
     // Columns other tiles read: the edge rows / columns, plus the second one on a Neumann face
     // (its mirror image is the halo of this very tile).
     int rows[4], cols[4], nrow = 0, ncol = 0;
@@ -189,10 +200,9 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     const int n_publish = nrow * g.aj + ncol * g.ai;
     const int n_ring = 2 * (g.ai + g.aj);
     const int ncolumns = g.ai * g.aj;
-    const int lanes_m = (M + 31) >> 5;
 
     // Tile + halo ring (mirrored at the domain faces) into shared memory; the owned columns'
-    // coefficients into the parity-split scratch copy.
+    // coefficients into the parity-split scratch copy; the column table.
     {
         const int span = g.aj + 2;
         const int cols_all = (g.ai + 2) * span;
@@ -217,6 +227,18 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                 }
             }
         }
+        for (int e = threadIdx.x; e < 2 * ncolumns; e += blockDim.x) {
+            const int col = e >> 1, colour = e & 1;
+            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+            const int gi = g.i0 + li, gj = g.j0 + lj;
+            const int kp = (colour + gi + gj) & 1;
+            const int c2 = (li + 1) * g.stride_i + (lj + 1);
+            const int cnt = kp ? nz / 2 : (nz + 1) / 2;
+            const int last = (kp ? (nz + 1) / 2 : nz / 2) - 1;
+            tab[e] = make_int4(kp * g.ncm + c2 * M, (kp ^ 1) * g.ncm + c2 * M,
+                               static_cast<int>(((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M),
+                               cnt | (last << 9) | (kp << 18));
+        }
     }
     __syncthreads();
 
@@ -224,7 +246,8 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     const float one_minus_omega = 1.0f - omega;
     const float h = a.p.dx2_over_D;
     const float K = a.p.michaelis_k;
-    unsigned gen = 0;
+    const float* __restrict__ coeff = a.coeff;
+    unsigned int epoch = 0;
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
     bool converged = false;
@@ -235,31 +258,30 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         for (int sweep = 0; sweep < chunk && ok; ++sweep) {
             for (int colour = 0; colour < 2 && ok; ++colour) {
                 for (int col = warp; col < ncolumns; col += nwarps) {
-                    const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-                    const int gi = g.i0 + li, gj = g.j0 + lj;
-                    const int kp = (colour + gi + gj) & 1;
-                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
-                    const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
-                    float du[kMaxLanesPerColumn];
+                    const int4 e = tab[2 * col + colour];
+                    const int cnt = e.w & 511, last = (e.w >> 9) & 511, kp = e.w >> 18;
+                    float du[LANES];
 #pragma unroll
-                    for (int r = 0; r < kMaxLanesPerColumn; ++r) {
+                    for (int r = 0; r < LANES; ++r) {
                         const int m = lane + 32 * r;
-                        du[r] = (r < lanes_m && m < M) ? crow[m] : -1.0f;
+                        du[r] = m < cnt ? coeff[e.z + m] : -1.0f;
                     }
 #pragma unroll
-                    for (int r = 0; r < kMaxLanesPerColumn; ++r) {
-                        if (r >= lanes_m) break;
+                    for (int r = 0; r < LANES; ++r) {
+                        if (!(du[r] >= 0.0f)) continue;
                         const int m = lane + 32 * r;
-                        const int k = 2 * m + kp;
-                        if (!(du[r] >= 0.0f) || k >= nz) continue;
-                        float* own = s + kp * g.ncm + c2 * M + m;
-                        const float o = *own;
+                        const int io = e.x + m;
+                        const float o = s[io];
                         const float c = du[r] / (K + o);
                         float prod = 0.0f;
-                        if (HAS_PROD) prod = prod_term(a, gi * sx + static_cast<int64_t>(gj) * nz + k);
-                        const float gs =
-                            (neighbour_sum(s, g.ncm, M, nz, g.stride_i, c2, k) + h * prod) / (6.0f + h * c);
-                        *own = fmaxf(one_minus_omega * o + omega * gs, 0.0f);
+                        if (HAS_PROD) {
+                            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+                            prod = prod_term(a, (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz + 2 * m + kp);
+                        }
+                        const float nb = s[io - si] + s[io + si] + s[io - M] + s[io + M] + s[e.y + max(m + kp - 1, 0)] +
+                                         s[e.y + min(m + kp, last)];
+                        const float gs = (nb + h * prod) / (6.0f + h * c);
+                        s[io] = fmaxf(one_minus_omega * o + omega * gs, 0.0f);
                     }
                 }
                 __syncthreads();
@@ -269,13 +291,14 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                     if (!publish_column(g, rows, nrow, cols, r, li, lj)) continue;
                     const int gi = g.i0 + li, gj = g.j0 + lj;
                     const int kpar = (colour + gi + gj) & 1;
-                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
+                    const int cnt = kpar ? nz / 2 : (nz + 1) / 2;
                     float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
-                    const float* sm = s + kpar * g.ncm + c2 * M;
-                    for (int m = lane; m < M; m += 32)
-                        if (2 * m + kpar < nz) __stcg(x + m, sm[m]);
+                    const float* sm = s + kpar * g.ncm + ((li + 1) * g.stride_i + (lj + 1)) * M;
+                    for (int m = lane; m < cnt; m += 32) __stcg(x + m, sm[m]);
                 }
-                ok = grid_barrier(a.ctl, gridDim.x, gen, &s_abort);
+                // A neighbour overwrites these entries only after this tile has signalled the next
+                // epoch, i.e. after the pull below: waiting for the four neighbours suffices.
+                ok = grid_barrier(a.ctl, a.flags, epoch, neighbours, n_neighbours);
                 if (!ok) break;
                 // pull the halo ring's updated colour (mirroring moves i, j by 2: parity kept)
                 for (int r = warp; r < n_ring; r += nwarps) {
@@ -283,39 +306,39 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                     ring_column(g, r, li, lj);
                     const int gi_u = g.i0 + li, gj_u = g.j0 + lj;
                     const int kpar = (colour + gi_u + gj_u) & 1;
+                    const int cnt = kpar ? nz / 2 : (nz + 1) / 2;
                     const int gi = mirror(gi_u, nx), gj = mirror(gj_u, ny);
-                    const int c2 = (li + 1) * g.stride_i + (lj + 1);
                     const float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
-                    float* sm = s + kpar * g.ncm + c2 * M;
-                    for (int m = lane; m < M; m += 32)
-                        if (2 * m + kpar < nz) sm[m] = __ldcg(x + m);
+                    float* sm = s + kpar * g.ncm + ((li + 1) * g.stride_i + (lj + 1)) * M;
+                    for (int m = lane; m < cnt; m += 32) sm[m] = __ldcg(x + m);
                 }
                 __syncthreads();
             }
         }
         if (!ok) break;
         sweeps += chunk;
-        // Max-norm residual of the current field over every updated node.
+        // Max-norm residual of the current field over every updated node (both colours).
         unsigned int bits = 0u;
-        for (int col = warp; col < ncolumns; col += nwarps) {
-            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-            const int gi = g.i0 + li, gj = g.j0 + lj;
-            const int c2 = (li + 1) * g.stride_i + (lj + 1);
-            for (int kp = 0; kp < 2; ++kp) {
-                const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
-                for (int m = lane; m < M; m += 32) {
-                    const int k = 2 * m + kp;
-                    if (k >= nz) continue;
-                    const float du = crow[m];
-                    if (!(du >= 0.0f)) continue;
-                    const float o = s[kp * g.ncm + c2 * M + m];
-                    const float c = du / (K + o);
-                    float prod = 0.0f;
-                    if (HAS_PROD) prod = prod_term(a, gi * sx + static_cast<int64_t>(gj) * nz + k);
-                    const float r = neighbour_sum(s, g.ncm, M, nz, g.stride_i, c2, k) + h * prod - (6.0f + h * c) * o;
-                    const float v = fabsf(r) / fmaxf(6.0f * o, a.p.reference);
-                    bits = max(bits, __float_as_uint(v));
+        for (int e2 = warp; e2 < 2 * ncolumns; e2 += nwarps) {
+            const int4 e = tab[e2];
+            const int col = e2 >> 1;
+            const int cnt = e.w & 511, last = (e.w >> 9) & 511, kp = e.w >> 18;
+            for (int m = lane; m < cnt; m += 32) {
+                const float du = coeff[e.z + m];
+                if (!(du >= 0.0f)) continue;
+                const int io = e.x + m;
+                const float o = s[io];
+                const float c = du / (K + o);
+                float prod = 0.0f;
+                if (HAS_PROD) {
+                    const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+                    prod = prod_term(a, (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz + 2 * m + kp);
                 }
+                const float nb = s[io - si] + s[io + si] + s[io - M] + s[io + M] + s[e.y + max(m + kp - 1, 0)] +
+                                 s[e.y + min(m + kp, last)];
+                const float r = nb + h * prod - (6.0f + h * c) * o;
+                const float val = fabsf(r) / fmaxf(6.0f * o, a.p.reference);
+                bits = max(bits, __float_as_uint(val));
             }
         }
 #pragma unroll
@@ -329,9 +352,9 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
             for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
             if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
         }
-        ok = grid_barrier(a.ctl, gridDim.x, gen, &s_abort);
+        ok = grid_barrier(a.ctl, a.flags, epoch);
         if (!ok) break;
-        residual = __uint_as_float(atomicAdd(&a.ctl->res_bits[slot], 0u));
+        residual = __uint_as_float(load_acquire(&a.ctl->res_bits[slot]));
         // The next chunk's slot was last read before this chunk's first barrier: safe to clear.
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&a.ctl->res_bits[slot ^ 1], 0u);
         ++chunk_index;
@@ -346,7 +369,8 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     }
     // Owned columns back to the field.
     for (int col = warp; col < ncolumns; col += nwarps) {
-        const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
+        const int li = col / g.aj;
+        const int lj = col - li * g.aj;
         const int c2 = (li + 1) * g.stride_i + (lj + 1);
         float* out = a.field + (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz;
         for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * g.ncm + c2 * M + (k >> 1)];
@@ -361,6 +385,24 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
 
 // ---- host side -------------------------------------------------------------------------------------------
 using KernelFn = void (*)(SorArgs);
+
+template <bool P>
+static KernelFn kernel_for_lanes(int lanes) {
+    switch (lanes) {
+        case 1: return k_sor_resident<P, 1>;
+        case 2: return k_sor_resident<P, 2>;
+        case 3: return k_sor_resident<P, 3>;
+        case 4: return k_sor_resident<P, 4>;
+        case 5: return k_sor_resident<P, 5>;
+        case 6: return k_sor_resident<P, 6>;
+        case 7: return k_sor_resident<P, 7>;
+        default: return k_sor_resident<P, 8>;
+    }
+}
+
+static KernelFn kernel_for(bool has_prod, int lanes) {
+    return has_prod ? kernel_for_lanes<true>(lanes) : kernel_for_lanes<false>(lanes);
+}
 
 struct DeviceInfo {
     int sms = 0;
@@ -393,13 +435,15 @@ static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, S
     bool found = false;
     SorTiling best{};
     long best_score = 0;
-    for (int tx = 1; tx <= std::min(p.nx, sms); ++tx) {
-        const int ty_max = std::min(p.ny, sms / tx);
+    const int max_ctas = std::min(sms, kMaxCtas);
+    for (int tx = 1; tx <= std::min(p.nx, max_ctas); ++tx) {
+        const int ty_max = std::min(p.ny, max_ctas / tx);
         for (int ty = 1; ty <= ty_max; ++ty) {
             const int ti = (p.nx + tx - 1) / tx, tj = (p.ny + ty - 1) / ty;
             if (ti < 2 || tj < 2) continue;
             const int ex = (p.nx + ti - 1) / ti, ey = (p.ny + tj - 1) / tj;
-            const size_t smem = 2ull * (ti + 2) * (tj + 2) * M * sizeof(float);
+            const size_t planes = (2ull * (ti + 2) * (tj + 2) * M + 3) & ~3ull;
+            const size_t smem = planes * sizeof(float) + 2ull * ti * tj * sizeof(int4);
             if (smem > smem_limit) continue;
             const long score = static_cast<long>(ti) * tj * 1000 + (ti + tj);
             if (!found || score < best_score) {
@@ -418,7 +462,9 @@ static size_t plane_bytes(const wbc_sor_params& p) {
     return 2ull * p.nx * p.ny * ((p.nz + 1) / 2) * sizeof(float);
 }
 
-size_t sor_workspace_bytes(const wbc_sor_params& p) { return sizeof(SorControl) + 2 * plane_bytes(p) + 256; }
+static size_t header_bytes() { return sizeof(SorControl) + kMaxCtas * sizeof(unsigned int); }
+
+size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 2 * plane_bytes(p) + 256; }
 
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
@@ -429,7 +475,7 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     *feasible = dev.sms > 0 && choose_tiling(p, dev.sms, static_cast<size_t>(dev.smem_optin) - reserve, &t);
     if (!*feasible) return WBC_OK;
     const bool has_prod = production != nullptr || p.has_source;
-    KernelFn fn = has_prod ? k_sor_resident<true> : k_sor_resident<false>;
+    KernelFn fn = kernel_for(has_prod, (t.M + 31) / 32);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem));
     if (err != cudaSuccess) {
@@ -445,14 +491,16 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     }
     char* base = reinterpret_cast<char*>(workspace);
     auto* ctl = reinterpret_cast<SorControl*>(base);
-    float* xchg = reinterpret_cast<float*>(base + sizeof(SorControl));
-    float* coeff = reinterpret_cast<float*>(base + sizeof(SorControl) + plane_bytes(p));
-    err = cudaMemsetAsync(ctl, 0, sizeof(SorControl), stream);
+    auto* flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
+    float* xchg = reinterpret_cast<float*>(base + header_bytes());
+    float* coeff = reinterpret_cast<float*>(base + header_bytes() + plane_bytes(p));
+    err = cudaMemsetAsync(base, 0, header_bytes(), stream);
     if (err != cudaSuccess) {
         set_error("wbc_sor_solve: cudaMemsetAsync", err);
         return WBC_ERR_CUDA;
     }
-    SorArgs args{p, t, fixed, density, production, source, field, xchg, coeff, ctl, check_every, max_sweeps, tolerance};
+    SorArgs args{p,     t,    fixed,       density,    production, source,   field,
+                 xchg,  coeff, ctl,        flags,      check_every, max_sweeps, tolerance};
     void* params[] = {&args};
     err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(t.tx * t.ty), dim3(t.threads), params,
                                       t.smem, stream);
@@ -512,7 +560,7 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
         }
     }
     // Streaming path: colour launches with a host check of the residual every check_every sweeps.
-    float* residual_dev = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) + sizeof(SorControl));
+    float* residual_dev = reinterpret_cast<float*>(reinterpret_cast<char*>(workspace) + header_bytes());
     int sweeps = 0;
     float residual = __builtin_inff();
     while (sweeps < max_sweeps) {
