@@ -188,6 +188,20 @@ int wbc_lifecycle_decide(const wbc_lifecycle_params* p, int32_t n, int32_t* cell
  * receives the last value. Replaces warp.utils.array_scan at cells/lifecycle.py:146. */
 int wbc_division_scan(int32_t n, const int32_t* divide_flag, int32_t* division_offset, int32_t* total_out,
                       void* workspace, size_t workspace_bytes, void* stream);
+/* Allocation-free variant of wbc_division_scan, for callers that cannot allocate device memory
+ * (a host framework that owns the whole device memory budget, or a loop that must not incur the
+ * device-wide synchronisation cudaMalloc can cause). It takes no workspace: the tile partials live
+ * in a 32,772-byte array inside the library, which every GPU that loads the library holds until
+ * the process exits. It accepts at most WBC_NOALLOC_SCAN_MAX_CELLS cells and returns
+ * WBC_ERR_INVALID (with wbc_last_error explaining) beyond that. The first call on a device looks
+ * up that array's device address (once per device, with the device current); make that first
+ * call before any stream capture. Every call shares the array, which keeps the previous call's
+ * partials (each call overwrites the entries it reads, so nothing needs clearing): calls that
+ * overlap on the GPU, on any stream, race and must be serialised by the caller. Allocates nothing
+ * and frees nothing. This entry point has no counterpart in the reference. */
+#define WBC_NOALLOC_SCAN_MAX_CELLS 33554432
+int wbc_division_scan_noalloc(int32_t n, const int32_t* divide_flag, int32_t* division_offset, int32_t* total_out,
+                              void* stream);
 /* Daughter of the k-th dividing cell into slot count + k (kernels/cell_kernels.py:157-200). */
 int wbc_place_daughters(int32_t count, float placement_factor, const int32_t* divide_flag,
                         const int32_t* division_offset, float* position, float* radius, int32_t* cell_state,

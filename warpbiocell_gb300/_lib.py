@@ -143,6 +143,7 @@ SIGNATURES: dict[str, list] = {
                       c_size_t, _I, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
+    "wbc_division_scan_noalloc": [_I, _P, _P, _P, _P],
     "wbc_place_daughters": [_I, _F, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_count_states": [_I, _P, _P, _P],
     "wbc_network_initialize": [POINTER(NetworkProgramC), _I, _P, _P, _P, _P],

@@ -6,6 +6,8 @@
 // (cell_kernels.py:115-154). Every draw comes from the cell's own stream (wbc_common.cuh), so the
 // decisions depend on the seed and the cell's history only; probabilities use the project's
 // exp (wbc_expf), so the oracle reproduces every decision bit for bit.
+#include <mutex>
+
 #include "wbc_common.cuh"
 
 namespace wbc {
@@ -149,6 +151,67 @@ int wbc_division_scan(int32_t n, const int32_t* divide_flag, int32_t* division_o
     if (workspace_bytes < wbc_scan_workspace_bytes(n)) return WBC_ERR_WORKSPACE;
     return scan_i32(divide_flag, division_offset, n, true, static_cast<int32_t*>(workspace), total_out,
                     as_stream(stream));
+}
+
+}  // extern "C"
+
+// ---- allocation-free division scan ----------------------------------------------------------------
+// For callers that cannot allocate device memory themselves, the scan's tile partials live in
+// this file-scope array instead of a caller-provided workspace. Every GPU that loads the library
+// holds it (32,772 bytes) until the process exits. Host code must not pass the symbol itself to a
+// kernel (on the host it names a stand-in, not device memory): its device address is looked up
+// once per device, with that device current, and cached.
+namespace wbc {
+namespace {
+constexpr int64_t kNoAllocPartials = WBC_NOALLOC_SCAN_MAX_CELLS / kScanTileItems + 1;
+__device__ __align__(256) int32_t g_noalloc_partials[kNoAllocPartials];
+static_assert(WBC_NOALLOC_SCAN_MAX_CELLS % kScanTileItems == 0, "whole tiles");
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+int32_t* g_noalloc_ptr[kMaxDevices] = {};
+
+int noalloc_partials(int32_t** out) {
+    int dev = 0;
+    cudaError_t err = cudaGetDevice(&dev);
+    if (err != cudaSuccess) {
+        set_error("wbc_division_scan_noalloc: cudaGetDevice", err);
+        return WBC_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        set_error_msg("wbc_division_scan_noalloc: device index beyond the supported range");
+        return WBC_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        err = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (err != cudaSuccess || !p) {
+            set_error("wbc_division_scan_noalloc: cudaGetSymbolAddress", err);
+            return WBC_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<int32_t*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return WBC_OK;
+}
+}  // namespace
+}  // namespace wbc
+
+extern "C" {
+
+int wbc_division_scan_noalloc(int32_t n, const int32_t* divide_flag, int32_t* division_offset, int32_t* total_out,
+                              void* stream) {
+    if (n < 0 || (n > 0 && (!divide_flag || !division_offset))) return WBC_ERR_INVALID;
+    if (n > WBC_NOALLOC_SCAN_MAX_CELLS) {
+        set_error_msg("wbc_division_scan_noalloc: n exceeds WBC_NOALLOC_SCAN_MAX_CELLS (33,554,432 cells); "
+                      "use wbc_division_scan with a caller-provided workspace");
+        return WBC_ERR_INVALID;
+    }
+    int32_t* partials = nullptr;
+    int rc = noalloc_partials(&partials);
+    if (rc != WBC_OK) return rc;
+    return scan_i32(divide_flag, division_offset, n, true, partials, total_out, as_stream(stream));
 }
 
 int wbc_place_daughters(int32_t count, float placement_factor, const int32_t* divide_flag,

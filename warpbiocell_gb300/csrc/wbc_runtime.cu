@@ -37,6 +37,7 @@ int check_launch(const char* where, int64_t launches) {
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanTile = kScanThreads * kScanItems;
+static_assert(kScanTile == kScanTileItems, "scan tile size shared with the scratch-free entry point");
 
 int64_t scan_partials_count(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
 
