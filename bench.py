@@ -51,6 +51,11 @@ WORKLOADS = {
     "spheroid_100k_81": dict(cells=100_000, ball_um=600.0, box_um=1600.0, dx_um=20.0, boundary=38.0),
 }
 
+# DRAM bytes per colour half-sweep of the resident SOR solver at 161^3: one `ncu --set full`
+# capture of k_sor_resident (profiles/k_sor_resident_spheroid_1M_161.md) read 37.6 MB over a
+# solve of 980 sweeps = 1960 half-sweeps (tile load, coefficients and write-back included).
+SOR_DRAM_BYTES_PER_HALF_SWEEP = 19200.0
+
 DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
 VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
 KM = 1.0
@@ -263,7 +268,11 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     barrier()
     e2e_ms = e_start.elapsed_time(e_end)
 
+    from warpbiocell_gb300.fields import diffusion as _diffusion
+
     result = {
+        "sor_path": _diffusion.last_solve.get("path"),
+        "sor_tiles": _diffusion.last_solve.get("tiles"),
         "rank": rank,
         "elapsed_ms": elapsed_ms,
         "cell_steps": cell_steps,
@@ -340,24 +349,44 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
     cells_per_step = r0["cell_steps"] / steps
     nodes = r0["nodes"]
     dominant = max(stages, key=lambda k: stages[k]["ms"]) if stages else None
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_source = "measured" if "hbm_gbs" in peaks else "fallback"
     roofline = None
-    if dominant:
+    if dominant == "sor":
+        # Unit: one colour half-sweep of the resident solver. Bytes: what a streaming half-sweep
+        # must move (field read, own-colour n_eff read, own-colour write: 8 B per node); duration:
+        # the solve time per step over its 2 x sweeps half-sweeps (residual checks included).
+        s = stages["sor"]
+        half_sweeps = 2.0 * sum(r0["sweeps"]) / max(1, len(r0["sweeps"]))
+        unit_ms = s["ms"] / steps / half_sweeps
+        nbytes = 8.0 * nodes
+        achieved = nbytes / (unit_ms / 1e3) / 1e9
+        traffic = SOR_DRAM_BYTES_PER_HALF_SWEEP if r0.get("sor_path") == 2 else None
+        roofline = {"bound": "hbm", "kernel": "k_sor_resident (per colour half-sweep)", "achieved": round(achieved, 1),
+                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                    "peak_source": peak_source, "bytes_per_unit": nbytes, "unit_us": round(unit_ms * 1e3, 3),
+                    "node_updates_per_s": round(nodes * half_sweeps / 2.0 / (s["ms"] / steps / 1e3), 1)}
+    elif dominant:
         s = stages[dominant]
-        if dominant == "sor":  # per colour launch (the residual launches are counted as launches too)
-            per_launch_ms = s["ms"] / max(1, s["launches"])
-            nbytes = stage_bytes("sor", cells_per_step, nodes, 1)
-        else:  # per call of the stage
-            per_launch_ms = s["ms"] / max(1, s["calls"])
-            nbytes = stage_bytes(dominant, cells_per_step, nodes, 1)
-        achieved = nbytes / (per_launch_ms / 1e3) / 1e9
-        peak = peaks.get("hbm_gbs", 6800.0)
+        unit_ms = s["ms"] / max(1, s["calls"])
+        nbytes = stage_bytes(dominant, cells_per_step, nodes, 1)
+        achieved = nbytes / (unit_ms / 1e3) / 1e9
         roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                    "frac": round(achieved / peak, 4), "traffic": None,
-                    "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                    "bytes_per_launch": nbytes, "launch_ms": per_launch_ms}
+                    "frac": round(achieved / peak, 4), "traffic": None, "peak_source": peak_source,
+                    "bytes_per_unit": nbytes, "unit_us": round(unit_ms * 1e3, 3)}
+    deposit_roofline = None
+    if "deposit" in stages and "convert" in stages:
+        # The deposit stage as a whole (atomics + conversion + n_eff), against the compulsory
+        # bytes 16 N + 4 M (positions and states in, n_eff out) and the bytes this design moves.
+        ms = (stages["deposit"]["ms"] + stages["convert"]["ms"]) / steps
+        compulsory = 16.0 * cells_per_step + 4.0 * nodes
+        moved = stage_bytes("deposit", cells_per_step, nodes, 1) + stage_bytes("convert", cells_per_step, nodes, 1)
+        deposit_roofline = {"bound": "hbm", "achieved": round(compulsory / (ms / 1e3) / 1e9, 1), "peak": peak,
+                            "unit": "GB/s", "frac": round(compulsory / (ms / 1e3) / 1e9 / peak, 4),
+                            "moved_GBps": round(moved / (ms / 1e3) / 1e9, 1), "us_per_step": round(ms * 1e3, 2)}
     breakdown = {k: {"ms_per_step": round(v["ms"] / steps, 4), "launches_per_step": v["launches"] / steps,
                      "GB/s": round(stage_bytes(k, cells_per_step, nodes, int(v["launches"] / steps)) /
-                                   (v["ms"] / steps / 1e3) / 1e9, 1) if v["ms"] > 0 else None}
+                                   (v["ms"] / steps / 1e3) / 1e9, 1) if v["ms"] > 0 and k != "sor" else None}
                  for k, v in sorted(stages.items(), key=lambda kv: -kv[1]["ms"])}
     out = {
         "metric": METRIC,
@@ -381,8 +410,11 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(r0["h2d"]),
                 "d2h_bytes_per_step": int(r0["d2h"])},
         "roofline": roofline,
+        "roofline_deposit": deposit_roofline,
         "stages": breakdown,
         "sor_sweeps_per_step": r0["sweeps"],
+        "sor_solver": {"path": "shared-memory resident" if r0.get("sor_path") == 2 else "streaming",
+                       "ctas": r0.get("sor_tiles")},
         "initial_solve_sweeps": r0["initial_sweeps"],
         "clocks": r0["clocks"],
         "cells_final": r0["count"],
