@@ -49,6 +49,12 @@ WORKLOADS = {
     "spheroid_1M_161": dict(cells=1_000_000, ball_um=1200.0, box_um=2400.0, dx_um=15.0, boundary=100.0),
     "spheroid_10k_41": dict(cells=10_000, ball_um=250.0, box_um=800.0, dx_um=20.0, boundary=38.0),
     "spheroid_100k_81": dict(cells=100_000, ball_um=600.0, box_um=1600.0, dx_um=20.0, boundary=38.0),
+    # oxygen + glucose (uptake 1:6 to O2, 5 mM boundary, 600 um^2/s) + lactate (zero boundary,
+    # 800 um^2/s, production 2x the glucose uptake scaled by G/(K_G + G)) on three 81^3 grids, and a
+    # 106-node random truth-table network per cell clamped by O2 > 5 mmHg and glucose > 2 mM,
+    # updated synchronously once per step; lifecycle in network mode.
+    "metabolic_network_100k_81": dict(cells=100_000, ball_um=600.0, box_um=1600.0, dx_um=20.0, boundary=38.0,
+                                      metabolic=True, network_nodes=106),
 }
 
 # DRAM bytes per colour half-sweep of the resident SOR solver at 161^3: one `ncu --set full`
@@ -70,7 +76,7 @@ def make_params(w: dict):
     from warpbiocell_gb300.fields.scalar_field import GridGeometry
     from warpbiocell_gb300.simulation.simulator import TimeStepping
 
-    return dict(
+    P = dict(
         geom=GridGeometry.centered_cube(w["box_um"], w["dx_um"]),
         oxygen=OxygenParams(diffusion_coefficient=DIFFUSION, uptake_max=VMAX, michaelis_k=KM,
                             boundary_value=w["boundary"]),
@@ -79,7 +85,29 @@ def make_params(w: dict):
                                   inhibition_threshold=8, hypoxia_threshold=5.0, death_threshold=1.0),
         contact=ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, margin=0.0, wall_rate=4.0),
         stepping=TimeStepping(dt_cells=DT, dt_mechanics=DT),
+        species=[],
+        network=None,
     )
+    if w.get("metabolic"):
+        from warpbiocell_gb300.fields.species import SpeciesParams, by_state
+        from warpbiocell_gb300.network.random_network import random_truth_table_network
+        from warpbiocell_gb300.network.runtime import InputClamp, NetworkParams
+
+        glucose_uptake = 20e-18 / 6.0 * 3600.0 / 1e-18  # mol/cell/s -> mM um^3/h (1 mM = 1e-18 mol/um^3)
+        P["species"] = [
+            SpeciesParams("glucose", "mM", diffusion=600.0 * 3600.0, michaelis_k=0.04, boundary_value=5.0,
+                          uptake_max=by_state(glucose_uptake)),
+            SpeciesParams("lactate", "mM", diffusion=800.0 * 3600.0, michaelis_k=1.0, boundary_value=0.0,
+                          production=by_state(2.0 * glucose_uptake), production_source="glucose"),
+        ]
+        net = random_truth_table_network(w["network_nodes"], seed=0)
+        P["network"] = NetworkParams(net, update="synchronous", updates_per_step=1,
+                                     inputs=(InputClamp("Oxygen_supply", "oxygen", 5.0),
+                                             InputClamp("Glucose_supply", "glucose", 2.0)))
+        P["lifecycle"] = LifecycleParams(division_rate=math.log(2.0) / 24.0, anoxic_death_rate=0.5,
+                                         inhibition_threshold=8, hypoxia_threshold=5.0, death_threshold=1.0,
+                                         phenotype_model="network", apoptosis_rate=0.02, necrosis_rate=0.1)
+    return P
 
 
 def make_cells(w: dict, seed: int):
@@ -193,14 +221,24 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     pos, radii = make_cells(w, seed=args.seed + rank)
     capacity = int(w["cells"] * 1.5)
     pop = CellPopulation.from_numpy(pos, radii, capacity=capacity, device=dev, seed=args.seed + rank)
-    ox = OxygenField(P["geom"], P["oxygen"], P["settings"], device=dev)
+    network = None
+    if P["species"]:
+        from warpbiocell_gb300.fields.metabolism import MetabolicFields
+        from warpbiocell_gb300.network.runtime import NetworkRuntime
+
+        ox = MetabolicFields(P["geom"], P["oxygen"], P["species"], P["settings"], device=dev)
+        if P["network"] is not None:
+            network = NetworkRuntime(P["network"], capacity, device=dev, species_names=tuple(ox.names))
+            network.initialize(pop)
+    else:
+        ox = OxygenField(P["geom"], P["oxygen"], P["settings"], device=dev)
     grid = make_neighbor_grid(P["contact"], dev)
     # As the reference's Experiment.run: initial neighbour counts and an initial field solve.
     contact_substep(pop, grid, P["contact"], dt=0.0)
     first = ox.update(pop)
 
     def step():
-        return cell_step(pop, grid, P["lifecycle"], P["contact"], P["stepping"], oxygen=ox)
+        return cell_step(pop, grid, P["lifecycle"], P["contact"], P["stepping"], oxygen=ox, network=network)
 
     for _ in range(args.warmup):
         step()
@@ -290,7 +328,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
         "nodes": P["geom"].node_count,
     }
     if rank == 0 and not args.skip_cpu:
-        result["cpu_baseline"], result["parity_full_size"] = cpu_sample_and_parity(pop, ox, grid, P, step)
+        result["cpu_baseline"], result["parity_full_size"] = cpu_sample_and_parity(pop, ox, grid, P, step, network)
     return result
 
 
@@ -305,33 +343,69 @@ def _population_to_oracle(pop):
     return sim
 
 
-def cpu_sample_and_parity(pop, ox, grid, P, step):
+def _oracle_species(fields, settings):
+    """Oracle mirrors of the GPU fields (one SpeciesField or the species of a MetabolicFields),
+    with the GPU's current values; returns (species list, production-source map)."""
+    from oracle import oracle as orc
+
+    items = list(fields.species_fields.items()) if hasattr(fields, "species_fields") else [(fields.name, fields)]
+    out, src = [], {}
+    for name, f in items:
+        g = f.geometry
+        sp = orc.OracleSpecies(orc.Geometry(g.origin, g.dx, g.shape), tuple(int(b) for b in f.field.boundary_flags),
+                               f.field.boundary_value, f.species.diffusion, f.species.uptake_max, f.species.michaelis_k,
+                               settings, production=f.species.production, name=name)
+        sp.values = f.numpy()
+        out.append(sp)
+        if f.species.production_source:
+            src[name] = f.species.production_source
+    return out, src
+
+
+def _oracle_network(rt, capacity):
+    from oracle import oracle as orc
+
+    sources = {"oxygen": 0, "glucose": 1, "constant": 4}
+    extra = list(rt.extra_names)
+    clamps = tuple((rt.network.index[c.node], sources.get(c.source, 2 + (extra.index(c.source) if c.source in extra else 0)),
+                    float(np.float32(c.threshold)), 1 if c.above else 0) for c in rt.params.inputs)
+    onet = orc.OracleNetwork({k: v.cpu().numpy() for k, v in rt._arrays.items()}, rt.network.n_nodes, capacity,
+                             update=rt.params.update, updates_per_step=rt.params.updates_per_step,
+                             time_units_per_h=rt.params.time_units_per_h, max_events=rt.params.max_events_per_step,
+                             clamps=clamps, fate_nodes=rt.fate_nodes, extra_names=tuple(extra))
+    onet.words[:] = rt.states.cpu().numpy().view(np.uint64)
+    return onet
+
+
+def cpu_sample_and_parity(pop, fields, grid, P, step, network=None):
     """Time one full-size cell step of the oracle on the host cores from the GPU's current state,
     then run the same step on the GPU and compare the two bit for bit."""
     from oracle import oracle as orc
 
     sim = _population_to_oracle(pop)
-    g = P["geom"]
-    sp = orc.OracleSpecies(orc.Geometry(g.origin, g.dx, g.shape), tuple(int(b) for b in ox.field.boundary_flags),
-                           ox.field.boundary_value, ox.species.diffusion, ox.species.uptake_max,
-                           ox.species.michaelis_k, P["settings"])
-    sp.values = ox.numpy()
+    for name, t in pop.extra_local.items():
+        sim.extra_local[name] = t.cpu().numpy().copy()
+    species, src = _oracle_species(fields, P["settings"])
+    onet = _oracle_network(network, pop.capacity) if network is not None else None
     threads = orc.num_threads()
     cells = sim.count
     t0 = time.perf_counter()
-    daughters, report = orc.cell_step(sim, P["lifecycle"], P["contact"], P["stepping"].dt_cells,
-                                      P["stepping"].dt_mechanics, sp, dim=grid.dim)
+    daughters, reports = orc.full_cell_step(sim, P["lifecycle"], P["contact"], P["stepping"].dt_cells,
+                                            P["stepping"].dt_mechanics, species, src, network=onet, dim=grid.dim)
     cpu_s = time.perf_counter() - t0
     rep = step()
     n = pop.count
-    same = (rep.daughters == daughters and n == sim.count and rep.field_sweeps == report[0]
-            and np.array_equal(ox.numpy(), sp.values)
+    gpu_fields = [f.numpy() for f in (fields.species_fields.values() if hasattr(fields, "species_fields") else [fields])]
+    same = (rep.daughters == daughters and n == sim.count and rep.field_sweeps == sum(r[0] for r in reports)
+            and all(np.array_equal(a, s.values) for a, s in zip(gpu_fields, species))
             and np.array_equal(pop.position[:n].cpu().numpy(), sim.position[:n])
             and np.array_equal(pop.cell_state[:n].cpu().numpy(), sim.cell_state[:n])
             and np.array_equal(pop.neighbor_count[:n].cpu().numpy(), sim.neighbor_count[:n])
-            and np.array_equal(pop.rng_state[:n].cpu().numpy().view(np.uint32), sim.rng_state[:n]))
+            and np.array_equal(pop.rng_state[:n].cpu().numpy().view(np.uint32), sim.rng_state[:n])
+            and (onet is None or np.array_equal(network.states[:n].cpu().numpy().view(np.uint64), onet.words[:n])))
+    sweeps = sum(r[0] for r in reports)
     baseline = {"value": cells / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
-                "sample": f"one full cell step of the same workload ({cells} cells, {report[0]} SOR sweeps) by the "
+                "sample": f"one full cell step of the same workload ({cells} cells, {sweeps} SOR sweeps) by the "
                           f"C++ restatement with {threads} OpenMP threads, from the GPU run's state; {cpu_s:.2f} s"}
     return baseline, bool(same)
 
@@ -432,29 +506,45 @@ def run_reference(args) -> dict:
     w = WORKLOADS[args.workload]
     P = make_params(w)
     pos, radii = make_cells(w, seed=args.seed)
-    sim = orc.OracleSim.from_numpy(pos, radii, capacity=int(w["cells"] * 1.5), seed=args.seed)
+    from warpbiocell_gb300.fields.oxygen import species_params
+
+    capacity = int(w["cells"] * 1.5)
+    sim = orc.OracleSim.from_numpy(pos, radii, capacity=capacity, seed=args.seed)
     g = P["geom"]
-    sp = orc.OracleSpecies(orc.Geometry(g.origin, g.dx, g.shape), (0, 0, 0), w["boundary"], DIFFUSION,
-                           (VMAX, VMAX, VMAX, 0.0), KM, P["settings"])
+    og = orc.Geometry(g.origin, g.dx, g.shape)
+    species = [orc.OracleSpecies(og, (0, 0, 0), s.boundary_value, s.diffusion, s.uptake_max, s.michaelis_k,
+                                 P["settings"], production=s.production, name=s.name)
+               for s in [species_params(P["oxygen"])] + list(P["species"])]
+    src = {s.name: s.production_source for s in P["species"] if s.production_source}
+    onet = None
+    if P["network"] is not None:
+        params = P["network"]
+        net = params.network
+        sources = {"oxygen": 0, "glucose": 1, "constant": 4}
+        clamps = tuple((net.index[c.node], sources[c.source], float(np.float32(c.threshold)), 1 if c.above else 0)
+                       for c in params.inputs)
+        onet = orc.OracleNetwork(net.programs(), net.n_nodes, capacity, update=params.update,
+                                 updates_per_step=params.updates_per_step, clamps=clamps,
+                                 fate_nodes=params.fate_node_indices())
+        onet.initialize(sim)
     threads = orc.num_threads()
     contact, stepping = P["contact"], P["stepping"]
     sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
-    # initial field solve as in the reference's Experiment.run
-    n = sim.count
-    acc = orc.deposit(sp.geom, sim.position[:n], sim.cell_state[:n])
-    dens, _ = orc.density_convert(sp.geom, acc)
-    sp.combine(dens)
-    sp.solve()
-    sp.sample_into(sim, sim.oxygen_local)
+    orc.metabolic_update(sim, species, src)  # initial field solve, as the reference's Experiment.run
+
+    def step():
+        orc.full_cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, species, src,
+                           network=onet)
+
     for _ in range(args.warmup):
-        orc.cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, sp)
+        step()
     cells = 0
     t0 = time.perf_counter()
     done = 0
     budget_s = args.reference_budget_s
     for _ in range(args.steps):
         cells += sim.count
-        orc.cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, sp)
+        step()
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break

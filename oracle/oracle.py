@@ -415,3 +415,105 @@ def cell_step(sim: OracleSim, lifecycle, contact, dt_cells: float, dt_mechanics:
     for _ in range(substeps):
         sim.contact_substep(contact.query_radius, dim, contact.query_radius, contact.rate, dt_mechanics)
     return daughters, report
+
+
+@dataclass
+class OracleNetwork:
+    """Mirror of a NetworkRuntime (network/runtime.py:89-228): program arrays, clamps, words."""
+
+    arrays: dict  # the programs() arrays (ops, args, start, length, updatable, rates, p_on)
+    n_nodes: int
+    capacity: int
+    update: str = "synchronous"
+    updates_per_step: int = 1
+    time_units_per_h: float = 10.0
+    max_events: int = 20000
+    clamps: tuple = ()  # (node index, source code 0-4, threshold, above)
+    fate_nodes: tuple = (-1, -1, -1, -1)
+    extra_names: tuple = ()
+
+    def __post_init__(self):
+        self.n_words = (self.n_nodes + 63) // 64
+        self.words = np.zeros((self.capacity, self.n_words), dtype=np.uint64)
+        self.prog, self._keep = program(self.arrays, self.n_nodes)
+        c = self.clamps or ((0, 4, 0.0, 1),)
+        self.c_node = np.array([x[0] for x in c], np.int32)
+        self.c_source = np.array([x[1] for x in c], np.int32)
+        self.c_thr = np.array([x[2] for x in c], np.float32)
+        self.c_above = np.array([x[3] for x in c], np.int32)
+        self.p_on = np.ascontiguousarray(self.arrays["p_on"], dtype=np.float32)
+        self.rates = {k: np.ascontiguousarray(self.arrays[k], dtype=np.float32)
+                      for k in ("rate_up_true", "rate_up_false", "rate_down_true", "rate_down_false")}
+
+    def initialize(self, sim: OracleSim) -> None:
+        lib().orc_network_initialize(ctypes.byref(self.prog), c_int32(sim.count), P(self.p_on), P(sim.rng_state),
+                                     P(self.words))
+        self.read_fates(sim)
+
+    def read_fates(self, sim: OracleSim) -> None:
+        lib().orc_network_read_fates(c_int32(sim.count), c_int32(self.n_words), *[c_int32(x) for x in self.fate_nodes],
+                                     P(self.words), P(sim.fate_flags))
+
+    def step(self, sim: OracleSim, dt_h: float) -> None:
+        n = sim.count
+        if len(self.clamps):
+            extra = [sim.local_field(x) for x in self.extra_names[:2]]
+            ea = extra[0] if len(extra) > 0 else sim.oxygen_local
+            eb = extra[1] if len(extra) > 1 else sim.oxygen_local
+            lib().orc_network_clamp_inputs(c_int32(n), c_int32(self.n_words), c_int32(len(self.clamps)),
+                                           P(self.c_node), P(self.c_source), P(self.c_thr), P(self.c_above),
+                                           P(sim.oxygen_local), P(sim.glucose_local), P(ea), P(eb), P(self.words))
+        if self.update == "synchronous":
+            lib().orc_network_update_sync(ctypes.byref(self.prog), c_int32(n), c_int32(self.updates_per_step),
+                                          P(self.words))
+        elif self.update == "asynchronous":
+            lib().orc_network_update_async(ctypes.byref(self.prog), c_int32(n), c_int32(self.updates_per_step),
+                                           P(sim.rng_state), P(self.words))
+        else:
+            r = self.rates
+            lib().orc_network_update_maboss(ctypes.byref(self.prog), c_int32(n), f32(dt_h * self.time_units_per_h),
+                                            c_int32(self.max_events), P(r["rate_up_true"]), P(r["rate_up_false"]),
+                                            P(r["rate_down_true"]), P(r["rate_down_false"]), P(sim.rng_state),
+                                            P(self.words))
+        self.read_fates(sim)
+
+    def inherit(self, sim: OracleSim, count_before: int) -> None:
+        if count_before == 0 or sim.count == count_before:
+            return
+        lib().orc_network_inherit(c_int32(count_before), c_int32(self.n_words), P(sim.divide_flag),
+                                  P(sim.division_offset), P(self.words))
+
+
+def metabolic_update(sim: OracleSim, species: list, production_source: dict) -> list:
+    """Mirror of MetabolicFields.update (fields/metabolism.py:99-111): one deposit, then per
+    species in order combine -> solve (with its production source) -> sample. Returns the
+    (sweeps, residual, converged) of every species."""
+    n = sim.count
+    geom = species[0].geom
+    acc = deposit(geom, sim.position[:n], sim.cell_state[:n])
+    dens, _ = density_convert(geom, acc)
+    by_name = {s.name: s for s in species}
+    reports = []
+    for s in species:
+        s.combine(dens)
+        src = by_name.get(production_source.get(s.name))
+        reports.append(s.solve(src.values if src is not None else None, src.michaelis_k if src is not None else 1.0))
+        s.sample_into(sim, sim.local_field(s.name))
+    return reports
+
+
+def full_cell_step(sim: OracleSim, lifecycle, contact, dt_cells: float, dt_mechanics: float, species: list,
+                   production_source: dict, network: OracleNetwork | None = None, dim: int = 128):
+    """Mirror of simulation/simulator.py:58-81 with a MetabolicFields and an optional network."""
+    reports = metabolic_update(sim, species, production_source) if species else []
+    if network is not None:
+        network.step(sim, dt_cells)
+    count_before = sim.count
+    sim.decide_lifecycle(lifecycle, dt_cells)
+    daughters = sim.commit_divisions(lifecycle)
+    if network is not None and daughters:
+        network.inherit(sim, count_before)
+    substeps = max(1, int(round(dt_cells / dt_mechanics)))
+    for _ in range(substeps):
+        sim.contact_substep(contact.query_radius, dim, contact.query_radius, contact.rate, dt_mechanics)
+    return daughters, reports
