@@ -311,6 +311,9 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     result = {
         "sor_path": _diffusion.last_solve.get("path"),
         "sor_tiles": _diffusion.last_solve.get("tiles"),
+        "sor_halo_depth": _diffusion.last_solve.get("halo_depth"),
+        "sor_tile_grid": [_diffusion.last_solve.get("tiles_i"), _diffusion.last_solve.get("tiles_j")],
+        "sor_autotune": [list(v) for v in _diffusion.autotune_cache.values()],
         "rank": rank,
         "elapsed_ms": elapsed_ms,
         "cell_steps": cell_steps,
@@ -488,7 +491,9 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
         "stages": breakdown,
         "sor_sweeps_per_step": r0["sweeps"],
         "sor_solver": {"path": "shared-memory resident" if r0.get("sor_path") == 2 else "streaming",
-                       "ctas": r0.get("sor_tiles")},
+                       "ctas": r0.get("sor_tiles"), "halo_depth": r0.get("sor_halo_depth"),
+                       "tile_grid": r0.get("sor_tile_grid"),
+                       "autotuned": r0.get("sor_autotune")},
         "initial_solve_sweeps": r0["initial_sweeps"],
         "clocks": r0["clocks"],
         "cells_final": r0["count"],

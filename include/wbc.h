@@ -64,6 +64,15 @@ int wbc_rng_uniform(int32_t n, int32_t draws, uint32_t* rng_state, float* out, v
 int wbc_rng_sphere(int32_t n, uint32_t* rng_state, float* out_xyz, void* stream);
 /* Test hook: the project's exp(x) on n floats (used for every death / division probability). */
 int wbc_expf_batch(int32_t n, const float* x, float* out, void* stream);
+/* Test hook: the solver's correctly rounded division a[i] / b[i] (bit-identical to IEEE). */
+int wbc_div_batch(int32_t n, const float* a, const float* b, float* out, void* stream);
+/* Self-check of that division on the device. mode 0: the refined reciprocal of every float with
+ * exponent in [e_lo, e_hi] (both signs) against IEEE 1/b; mode 1: `pairs` seeded operand pairs
+ * (raw bit patterns, wide exponents, exact products, near-midpoint quotients) against IEEE a/b.
+ * Adds the number of differing results to *mismatches (device) and stores the first differing
+ * operands (a, b bits) in first_bad[0..1] (device). */
+int wbc_div_check(int32_t mode, int32_t e_lo, int32_t e_hi, uint32_t seed, int64_t pairs,
+                  unsigned long long* mismatches, uint32_t* first_bad, void* stream);
 
 /* ---- hash-grid binning + contact mechanics -------------------------------------------------- */
 typedef struct wbc_neighbor_grid {
@@ -142,7 +151,18 @@ typedef struct wbc_sor_report {
     int32_t converged;           /* residual < tolerance                                             */
     int32_t path;                /* 2 = shared-memory resident solver, 1 = streaming colour launches */
     int32_t tiles;               /* CTAs of the resident solver (0 for the streaming path)           */
+    int32_t halo_depth;          /* half-sweeps between halo exchanges (resident path)               */
+    int32_t tiles_i, tiles_j;    /* tile grid of the resident solver                                 */
 } wbc_sor_report;
+
+/* Optional choices for the resident solver (NULL or zeros = automatic). halo_depth H in {1, 2, 4}:
+ * each tile keeps a halo of H columns and performs H colour half-sweeps between exchanges with
+ * its neighbours (the halo columns are updated redundantly, with identical results). tiles_i x
+ * tiles_j fixes the tile grid (at most one tile per SM). Every choice gives the same field bits. */
+typedef struct wbc_sor_tuning {
+    int32_t halo_depth;
+    int32_t tiles_i, tiles_j;
+} wbc_sor_tuning;
 
 /* Scratch bytes wbc_sor_solve needs for this grid (control block + halo exchange buffer). */
 size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p);
@@ -152,11 +172,22 @@ size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p);
  * one persistent cooperative launch with the field tile resident in shared memory when the grid
  * fits on chip, otherwise streaming colour launches with a host check per chunk; 1 = streaming;
  * 2 = resident only. Synchronises `stream` and fills the host-side `report`. The field after the
- * solve is bit-identical on both paths. Returns WBC_ERR_TIMEOUT if a grid barrier timed out. */
+ * solve is bit-identical on both paths and for every `tuning` (may be NULL). Returns
+ * WBC_ERR_TIMEOUT if a grid barrier timed out. */
 int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
                   const int32_t* fixed, const float* density, const float* production, const float* source,
                   float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
-                  void* stream);
+                  const wbc_sor_tuning* tuning, void* stream);
+/* Times the resident solver on a copy of `field` (into `scratch_field`, nx*ny*nz floats) for
+ * 2 * check_every sweeps under each candidate tuning (halo depths 1, 2, 4; per depth the tile grid
+ * with the fewest columns per tile, its transpose and the squarest grid) and returns the fastest in
+ * *best (zeros if the grid does not fit on chip) and its time per sweep in *best_us_per_sweep (may
+ * be NULL). `field` is not modified; synchronises `stream`. The choice changes speed only: every
+ * tuning gives the same field bits. */
+int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t* fixed, const float* density,
+                     const float* production, const float* source, const float* field, float* scratch_field,
+                     void* workspace, size_t workspace_bytes, wbc_sor_tuning* best, float* best_us_per_sweep,
+                     void* stream);
 /* Explicit FTCS step field_out = field_in + dt (D lap - uptake + production) (validation only;
  * kernels/field_kernels.py:246-273). `p->dx2_over_D` carries D/dx^2 here. */
 int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,

@@ -428,7 +428,8 @@ def test_coupled_run_is_reproducible_and_independent_of_capacity():
 
 
 # ---- the shared-memory resident solver against the streaming colour launches and the oracle ------------
-def _solve_with_path(path, geom, boundary, start, density, pins=None, production=None, source=None, settings=None):
+def _solve_with_path(path, geom, boundary, start, density, pins=None, production=None, source=None, settings=None,
+                     tuning=None):
     from warpbiocell_gb300.fields import diffusion
     from warpbiocell_gb300.fields.diffusion import solve_steady_state
     from warpbiocell_gb300.fields.scalar_field import ScalarField
@@ -440,15 +441,15 @@ def _solve_with_path(path, geom, boundary, start, density, pins=None, production
     f.assign(start)
     kin = UptakeKinetics(2.0e3, 5.0e4, 3.0)
     res = torch.zeros(1, dtype=torch.float32, device=DEV)
-    old = diffusion.solver_path
-    diffusion.solver_path = path
+    old, old_tuning = diffusion.solver_path, diffusion.solver_tuning
+    diffusion.solver_path, diffusion.solver_tuning = path, tuning
     try:
         rep = solve_steady_state(f, _t(density), kin, settings, res,
                                  production=None if production is None else _t(production),
                                  source=None if source is None else _t(source), source_k=0.04)
         info = dict(diffusion.last_solve)
     finally:
-        diffusion.solver_path = old
+        diffusion.solver_path, diffusion.solver_tuning = old, old_tuning
     return f.numpy(), rep, info
 
 
@@ -486,6 +487,56 @@ def test_resident_solver_bitwise_equals_streaming_and_oracle(shape, boundary, ex
     sweeps, residual, ok = orc.solve_steady_state(p, settings, fixed, density, values, production, source)
     assert (sweeps, ok) == (rb.sweeps, rb.converged) and np.float32(residual) == rb.residual
     np.testing.assert_array_equal(b, values)
+
+
+@pytest.mark.parametrize("shape, boundary", [
+    ((37, 29, 23), MIXED),
+    ((33, 27, 31), (Boundary.NEUMANN, Boundary.DIRICHLET, Boundary.NEUMANN)),
+    ((41, 41, 41), (Boundary.NEUMANN,) * 3),
+])
+def test_resident_halo_depths_and_tilings_bitwise(shape, boundary):
+    """Every halo depth (half-sweeps per exchange) and tile grid gives the streaming path's bits,
+    including tile grids whose last tile is narrower than the halo and a chunk of 2 * 7 half-sweeps
+    that is not a multiple of the depth."""
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
+    rng = np.random.default_rng(7 + sum(shape))
+    start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
+    density = rng.uniform(0.0, 2.0e-3, shape).astype(np.float32)
+    pins = rng.random(shape) < 0.02
+    production = rng.uniform(0.0, 40.0, shape).astype(np.float32)
+    source = rng.uniform(0.0, 5.0, shape).astype(np.float32)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=63, check_every=7)
+    a, ra, _ = _solve_with_path(1, geom, boundary, start, density, pins, production, source, settings)
+    for tuning in [(1, 0, 0), (2, 0, 0), (4, 0, 0), (2, 5, 3), (4, 4, 6), (1, 9, 2), (2, 2, 2)]:
+        b, rb, ib = _solve_with_path(2, geom, boundary, start, density, pins, production, source, settings,
+                                     tuning=tuning)
+        assert ib["path"] == 2 and ib["halo_depth"] == tuning[0], (tuning, ib)
+        if tuning[1]:  # the tile grid actually needed for tiles of ceil(n / requested) columns
+            assert ib["tiles_i"] <= tuning[1] and ib["tiles_j"] <= tuning[2], (tuning, ib)
+        assert (ra.sweeps, ra.converged, ra.residual) == (rb.sweeps, rb.converged, rb.residual), tuning
+        np.testing.assert_array_equal(a, b, err_msg=str(tuning))
+
+
+def test_autotuned_solve_bitwise_equals_streaming():
+    """The autotuner times candidate tunings on a scratch copy (the field is untouched) and the
+    solve with its pick gives the streaming path's bits."""
+    from warpbiocell_gb300.fields import diffusion
+
+    shape = (45, 38, 41)
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
+    rng = np.random.default_rng(11)
+    start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
+    density = rng.uniform(0.0, 2.0e-3, shape).astype(np.float32)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=120, check_every=20)
+    a, ra, _ = _solve_with_path(1, geom, MIXED, start, density, settings=settings)
+    diffusion.autotune_cache.clear()
+    b, rb, ib = _solve_with_path(0, geom, MIXED, start, density, settings=settings, tuning=None)
+    assert len(diffusion.autotune_cache) == 1
+    (depth, ti, tj, us), = diffusion.autotune_cache.values()
+    assert depth in (1, 2, 4) and us > 0.0
+    assert (ib["path"], ib["halo_depth"], ib["tiles_i"], ib["tiles_j"]) == (2, depth, ti, tj)
+    assert (ra.sweeps, ra.converged, ra.residual) == (rb.sweeps, rb.converged, rb.residual)
+    np.testing.assert_array_equal(a, b)
 
 
 def test_resident_solver_runs_the_benchmark_grid():

@@ -81,6 +81,17 @@ class SorReportC(ctypes.Structure):
         ("converged", c_int32),
         ("path", c_int32),
         ("tiles", c_int32),
+        ("halo_depth", c_int32),
+        ("tiles_i", c_int32),
+        ("tiles_j", c_int32),
+    ]
+
+
+class SorTuningC(ctypes.Structure):
+    _fields_ = [
+        ("halo_depth", c_int32),
+        ("tiles_i", c_int32),
+        ("tiles_j", c_int32),
     ]
 
 
@@ -130,6 +141,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_rng_uniform": [_I, _I, _P, _P, _P],
     "wbc_rng_sphere": [_I, _P, _P, _P],
     "wbc_expf_batch": [_I, _P, _P, _P],
+    "wbc_div_batch": [_I, _P, _P, _P, _P],
+    "wbc_div_check": [_I, _I, _I, ctypes.c_uint32, ctypes.c_int64, _P, _P, _P],
     "wbc_grid_build": [POINTER(NeighborGridC), _I, _P, _P, _P],
     "wbc_contact_substep": [POINTER(NeighborGridC), _I, _F, _F, _F, _P, _P, _P, _P],
     "wbc_deposit": [POINTER(GridGeometryC), _I, _P, _P, _P, _P],
@@ -140,7 +153,9 @@ SIGNATURES: dict[str, list] = {
     "wbc_ftcs_step": [POINTER(SorParamsC), _F, _P, _P, _P, _P, _P, _P, _P],
     "wbc_sor_solve_workspace_bytes": [POINTER(SorParamsC)],
     "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, POINTER(SorReportC), _P,
-                      c_size_t, _I, _P],
+                      c_size_t, _I, POINTER(SorTuningC), _P],
+    "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
+                         POINTER(c_float), _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
     "wbc_division_scan_noalloc": [_I, _P, _P, _P, _P],

@@ -138,7 +138,7 @@ __device__ __forceinline__ float production_at(const wbc_sor_params& p, const fl
     const float prod = production ? production[idx] : 0.0f;
     if (!p.has_source) return prod * 1.0f;
     const float v = source[idx];
-    return prod * (v / (p.source_k + v));
+    return prod * div_rn(v, p.source_k + v);
 }
 
 // One colour: thread (i, j, m) updates k = 2m + ((colour + i + j) & 1).
@@ -158,9 +158,9 @@ __global__ void k_sor_colour(wbc_sor_params p, int colour, const int32_t* __rest
     const int64_t idx = (static_cast<int64_t>(i) * p.ny + j) * p.nz + k;
     if ((fixed && fixed[idx] != 0) || on_dirichlet_face(p, i, j, k)) return;
     const float o = field[idx];
-    const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
+    const float c = div_rn(density[idx] * p.uptake_max, p.michaelis_k + o);
     const float prod = production_at(p, production, source, idx);
-    const float gs = (neighbor_sum(field, p, i, j, k) + p.dx2_over_D * prod) / (6.0f + p.dx2_over_D * c);
+    const float gs = div_rn(neighbor_sum(field, p, i, j, k) + p.dx2_over_D * prod, 6.0f + p.dx2_over_D * c);
     field[idx] = fmaxf((1.0f - p.omega) * o + p.omega * gs, 0.0f);
 }
 
@@ -177,10 +177,10 @@ __global__ void k_residual(wbc_sor_params p, const int32_t* __restrict__ fixed, 
         const int i = static_cast<int>(ij / p.ny);
         if ((!fixed || fixed[idx] == 0) && !on_dirichlet_face(p, i, j, k)) {
             const float o = field[idx];
-            const float c = density[idx] * p.uptake_max / (p.michaelis_k + o);
+            const float c = div_rn(density[idx] * p.uptake_max, p.michaelis_k + o);
             const float prod = production_at(p, production, source, idx);
             const float r = neighbor_sum(field, p, i, j, k) + p.dx2_over_D * prod - (6.0f + p.dx2_over_D * c) * o;
-            val = fabsf(r) / fmaxf(6.0f * o, p.reference);
+            val = div_rn(fabsf(r), fmaxf(6.0f * o, p.reference));
         }
     }
     // Max of non-negative floats = max of their bit patterns; NaN (0x7fc00000) dominates.

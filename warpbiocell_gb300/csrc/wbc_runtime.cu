@@ -173,6 +173,69 @@ __global__ void k_expf(int32_t n, const float* __restrict__ x, float* __restrict
     if (i < n) out[i] = wbc_expf(x[i]);
 }
 
+__global__ void k_div(int32_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = div_rn(a[i], b[i]);
+}
+
+__device__ __forceinline__ bool same_result(float x, float y) {
+    return __float_as_uint(x) == __float_as_uint(y) || (x != x && y != y);
+}
+
+__device__ __forceinline__ void note_mismatch(unsigned long long* count, uint32_t* first, float a, float b) {
+    if (atomicAdd(count, 1ull) == 0ull) {
+        first[0] = __float_as_uint(a);
+        first[1] = __float_as_uint(b);
+    }
+}
+
+// Every b = +-1.m * 2^e, e in [e_lo, e_hi]: the refined reciprocal against IEEE 1 / b.
+__global__ void k_recip_exhaustive(int32_t e_lo, int32_t e_hi, unsigned long long* count, uint32_t* first) {
+    const int64_t total = static_cast<int64_t>(e_hi - e_lo + 1) << 23;
+    for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < total;
+         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        const uint32_t e = static_cast<uint32_t>(e_lo + static_cast<int32_t>(t >> 23) + 127);
+        const uint32_t bits = (e << 23) | static_cast<uint32_t>(t & 0x7fffff);
+        for (uint32_t sign = 0; sign < 2; ++sign) {
+            const float b = __uint_as_float(bits | (sign << 31));
+            if (!same_result(recip_rn_estimate(b), __fdiv_rn(1.0f, b))) note_mismatch(count, first, 1.0f, b);
+        }
+    }
+}
+
+// Seeded operand pairs of four kinds against IEEE a / b: raw bit patterns (every class, including
+// zeros, subnormals, infinities and NaN), operands with exponents in [-40, 40], exact products
+// a = q b, and quotients within a few ulp of a rounding midpoint (a = RN(b m), m a midpoint).
+__global__ void k_div_random(uint32_t seed, int64_t pairs, unsigned long long* count, uint32_t* first) {
+    for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < pairs;
+         t += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        uint32_t st = rng_start(seed, static_cast<uint32_t>(t) ^ static_cast<uint32_t>(t >> 32) * 0x85EBCA6Bu);
+        const uint32_t inc = rng_increment(static_cast<uint32_t>(t));
+        const uint32_t kind = static_cast<uint32_t>(t & 3);
+        const uint32_t r1 = rng_next(st, inc), r2 = rng_next(st, inc), r3 = rng_next(st, inc);
+        float a, b;
+        if (kind == 0) {
+            a = __uint_as_float(r1);
+            b = __uint_as_float(r2);
+        } else {
+            const uint32_t ea = 127 - 40 + (r3 % 81), eb = 127 - 40 + ((r3 >> 8) % 81);
+            a = __uint_as_float((r1 & 0x807fffffu) | (ea << 23));
+            b = __uint_as_float((r2 & 0x807fffffu) | (eb << 23));
+            if (kind == 2) {
+                a = __fmul_rn(a, b);
+            } else if (kind == 3) {
+                // m = 1.m' + half an ulp of a 24-bit significand: a midpoint in [1, 2)
+                const float m_lo = __uint_as_float((127u << 23) | (r1 & 0x7fffffu));
+                const double mid = static_cast<double>(m_lo) + 0x1p-24;
+                a = __double2float_rn(mid * static_cast<double>(b));
+                const int nudge = static_cast<int>((r3 >> 24) & 7) - 3;
+                a = __uint_as_float(__float_as_uint(a) + nudge);
+            }
+        }
+        if (!same_result(div_rn(a, b), __fdiv_rn(a, b))) note_mismatch(count, first, a, b);
+    }
+}
+
 }  // namespace wbc
 
 using namespace wbc;
@@ -217,6 +280,28 @@ int wbc_rng_sphere(int32_t n, uint32_t* rng_state, float* out_xyz, void* stream)
     if (n == 0) return WBC_OK;
     k_rng_sphere<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, rng_state, out_xyz);
     return check_launch("wbc_rng_sphere");
+}
+
+int wbc_div_batch(int32_t n, const float* a, const float* b, float* out, void* stream) {
+    if (n < 0 || (n > 0 && (!a || !b || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_div<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, a, b, out);
+    return check_launch("wbc_div_batch");
+}
+
+int wbc_div_check(int32_t mode, int32_t e_lo, int32_t e_hi, uint32_t seed, int64_t pairs,
+                  unsigned long long* mismatches, uint32_t* first_bad, void* stream) {
+    if (!mismatches || !first_bad || mode < 0 || mode > 1) return WBC_ERR_INVALID;
+    cudaStream_t s = as_stream(stream);
+    if (mode == 0) {
+        if (e_lo < -126 || e_hi > 127 || e_lo > e_hi) return WBC_ERR_INVALID;
+        k_recip_exhaustive<<<4096, 256, 0, s>>>(e_lo, e_hi, mismatches, first_bad);
+    } else {
+        if (pairs < 0) return WBC_ERR_INVALID;
+        if (pairs == 0) return WBC_OK;
+        k_div_random<<<4096, 256, 0, s>>>(seed, pairs, mismatches, first_bad);
+    }
+    return check_launch("wbc_div_check");
 }
 
 int wbc_expf_batch(int32_t n, const float* x, float* out, void* stream) {

@@ -2,30 +2,34 @@
 // in shared memory (kernels/field_kernels.py:185-243 iterated as fields/diffusion.py:79-123).
 //
 // Decomposition: the (i, j) plane is cut into tx x ty tiles of ti x tj columns; each CTA (one
-// per SM) owns one tile with the full z extent. Shared memory holds the tile plus a one-column
-// halo ring, split by k parity (E[col][m] = f(k = 2m), O[col][m] = f(k = 2m + 1)): within a
-// column all nodes of one colour share a k parity, so a warp that owns a column updates its
-// colour with 32 consecutive words per access and no bank conflicts, and the k-neighbours of
-// node m are entries m - 1 + kp and m + kp of the other parity (clamped at the ends, which is
-// exactly the reference's mirror rule). At the start each CTA writes the uptake coefficients
-// density * uptake_max of its columns, split the same way, to an L2-resident scratch copy (a
-// negative value marks the nodes that are never updated: Dirichlet faces and pinned nodes).
+// per SM) owns one tile with the full z extent. Shared memory holds the tile plus a halo of all
+// columns within L1 distance H of it, split by k parity (E[col][m] = f(k = 2m),
+// O[col][m] = f(k = 2m + 1)): within a column all nodes of one colour share a k parity, so a warp
+// that owns a column updates its colour with 32 consecutive words per access and no bank
+// conflicts, and the k-neighbours of entry m are entries m - 1 + kp and m + kp of the other
+// parity (clamped at the ends, which is exactly the reference's mirror rule). At the start each
+// CTA writes the uptake coefficients density * uptake_max of its columns, split the same way, to
+// an L2-resident scratch copy (a negative value marks the nodes that are never updated:
+// Dirichlet faces and pinned nodes).
 //
-// One colour half-sweep = every warp updates its columns' nodes of that colour from shared
-// memory; the tile-edge columns' updated colour is published to a parity-split exchange buffer
-// in global memory (L2, bypassing L1); a grid barrier; then the halo ring's updated colour is
-// pulled back into shared memory. Every `check_every` sweeps the max-norm residual is reduced
-// (warp shuffles, one atomicMax per CTA) and all CTAs stop together once it is below the
-// tolerance: the reference's sweep count, residual and stopping rule, with no host round trip.
-// Each node's update is the reference kernel's float expression in the same order, so the field
-// after n sweeps is bit-identical to the oracle's and to the streaming kernels'.
+// Temporal blocking: between two halo exchanges a tile performs H colour half-sweeps; the p-th
+// updates the columns within distance H - 1 - p of the tile (the ring columns redundantly, with
+// the same inputs and the same float expression as their owner, hence the same bits), so each
+// half-sweep still reads only values that are current. Columns outside the domain (on a Neumann
+// face) are refreshed by copying their mirror column after every half-sweep. After the H
+// half-sweeps the columns within H of the tile edge are published to a double-buffered,
+// parity-split exchange buffer in L2, the tile waits for its neighbouring tiles' epoch flags
+// (release / acquire; 4 neighbours for H = 1, 8 for H > 1), and pulls its halo. Every
+// `check_every` sweeps the max-norm residual is reduced (warp shuffles, one atomicMax per CTA,
+// the only global barrier) and all CTAs stop together once it is below the tolerance: the
+// reference's sweep count, residual and stopping rule, with no host round trip. The field after
+// n sweeps is bit-identical to the oracle's and to the streaming kernels'.
 //
-// Grid barrier: every CTA stores the barrier's epoch to its own flag (release), then its threads
-// poll all CTAs' flags in parallel (acquire); no two CTAs update the same word. The polls are
-// bounded (about a second); on timeout the CTA raises an abort flag, every CTA leaves, and the
-// host gets WBC_ERR_TIMEOUT.
+// Every wait polls a bounded number of times (about a second); on timeout the CTA raises an
+// abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
 #include <algorithm>
 #include <mutex>
+#include <vector>
 
 #include "wbc_common.cuh"
 
@@ -48,6 +52,9 @@ struct SorTiling {
     int ti, tj;  // tile extent (columns) along i and j
     int M;       // (nz + 1) / 2 entries per parity per column
     int threads;
+    int H;       // halo depth = half-sweeps between exchanges
+    int nbox;    // columns of the bounding box (ti + 2H) * (tj + 2H)
+    size_t planes_bytes;
     size_t smem;
 };
 
@@ -59,7 +66,7 @@ struct SorArgs {
     const float* production;
     const float* source;
     float* field;
-    float* xchg;   // [2][nx][ny][M] halo exchange
+    float* xchg;   // [2 buffers][2 parities][nx][ny][M] halo exchange
     float* coeff;  // [2][nx][ny][M] density * uptake_max, -1 where not updated
     SorControl* ctl;
     unsigned int* flags;  // [gridDim.x] barrier epochs
@@ -85,7 +92,7 @@ __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n 
 
 // Signals this CTA's arrival at the next epoch, then waits for the CTAs listed in `wait_for`
 // (n_wait of them) or, with n_wait < 0, for every CTA. Returns false when aborted (timeout here or
-// elsewhere). A halo exchange only needs the four neighbouring tiles; the residual needs all.
+// elsewhere). A halo exchange only needs the neighbouring tiles; the residual needs all.
 __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch,
                                              const int* wait_for = nullptr, int n_wait = -1) {
     epoch += 1;
@@ -113,232 +120,384 @@ __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flag
     return __syncthreads_or(aborted) == 0;
 }
 
-struct TileGeom {
-    int i0, j0, ai, aj;  // tile origin and actual extent
-    int stride_i;        // columns per smem row (tj + 2)
-    int ncm;             // (ti + 2) * (tj + 2) * M: floats per parity plane in shared memory
-};
-
 __device__ __forceinline__ float prod_term(const SorArgs& a, int64_t idx) {
     const float prod = a.production ? a.production[idx] : 0.0f;
     if (!a.p.has_source) return prod * 1.0f;
     const float v = a.source[idx];
-    return prod * (v / (a.p.source_k + v));
+    return prod * div_rn(v, a.p.source_k + v);
 }
 
-// Column r of the halo ring (pull) as tile coordinates.
-__device__ __forceinline__ void ring_column(const TileGeom& g, int r, int& li, int& lj) {
-    if (r < g.aj) {
-        li = -1;
-        lj = r;
-    } else if (r < 2 * g.aj) {
-        li = g.ai;
-        lj = r - g.aj;
-    } else if (r < 2 * g.aj + g.ai) {
-        li = r - 2 * g.aj;
-        lj = -1;
-    } else {
-        li = r - 2 * g.aj - g.ai;
-        lj = g.aj;
+// Column lists in shared memory, after the two parity planes. A column is an int2:
+// x = index in the bounding box, y = (gi << 16) | gj with gi, gj its (mirrored) global position.
+struct Lists {
+    int2* upd;       // in-domain columns within distance H - 1, by distance (owned first)
+    int* upd_end;    // upd_end[d]: columns within distance d (d = 0 .. H - 1)
+    int2* pull;      // in-domain columns at distance 1 .. H
+    int2* publish;   // owned columns within H of the tile edge
+    int2* inner;     // owned columns farther than H from the tile edge
+    int2* mir;       // outside the domain: x = box index, y = box index of the mirror column
+    int n_pull, n_publish, n_inner, n_mir;
+};
+
+// Loop invariants of a colour half-sweep.
+struct Sweep {
+    float* s;
+    const float* coeff;
+    int ncm, M, si, nx, ny, nz, cnt_even, cnt_odd;
+    int64_t sx;
+    float K, h, omega, one_minus_omega;
+};
+
+template <int LANES>
+__device__ __forceinline__ void load_coeff(const Sweep& w, int2 c, int colour, int lane, float (&du)[LANES]) {
+    const int gi = c.y >> 16, gj = c.y & 0xffff;
+    const int kp = (colour + gi + gj) & 1;
+    const int cnt = kp ? w.cnt_odd : w.cnt_even;
+    const float* crow = w.coeff + ((static_cast<int64_t>(kp) * w.nx + gi) * w.ny + gj) * w.M;
+#pragma unroll
+    for (int r = 0; r < LANES; ++r) {
+        const int m = lane + 32 * r;
+        du[r] = m < cnt ? crow[m] : -1.0f;
     }
 }
 
-// Column r of the published set: rows[0..nrow) x all lj, then cols[0..ncol) x all li.
-__device__ __forceinline__ bool publish_column(const TileGeom& g, const int* rows, int nrow, const int* cols, int r,
-                                               int& li, int& lj) {
-    if (r < nrow * g.aj) {
-        const int q = r / g.aj;
-        li = rows[q];
-        lj = r - q * g.aj;
-    } else {
-        const int rr = r - nrow * g.aj;
-        const int q = rr / g.ai;
-        lj = cols[q];
-        li = rr - q * g.ai;
-    }
-    return li >= 0 && li < g.ai && lj >= 0 && lj < g.aj;
-}
-
+// One colour of one column: the reference's update (field_kernels.py:185-212) with the
+// Michaelis-Menten uptake linearised at the old value, over-relaxed and clamped at zero.
 template <bool HAS_PROD, int LANES>
-__global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
-    extern __shared__ float s[];
-    __shared__ unsigned int s_red[32];
-    const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    TileGeom g;
-    int neighbours[4], n_neighbours = 0;  // tiles whose edge columns form this tile's halo
-    {
-        const int bx = blockIdx.x / a.t.ty;
-        const int by = blockIdx.x - bx * a.t.ty;
-        g.i0 = bx * a.t.ti;
-        g.j0 = by * a.t.tj;
-        g.ai = min(a.t.ti, nx - g.i0);
-        g.aj = min(a.t.tj, ny - g.j0);
-        g.stride_i = a.t.tj + 2;
-        g.ncm = (a.t.ti + 2) * (a.t.tj + 2) * M;
-        if (bx > 0) neighbours[n_neighbours++] = blockIdx.x - a.t.ty;
-        if (bx + 1 < a.t.tx) neighbours[n_neighbours++] = blockIdx.x + a.t.ty;
-        if (by > 0) neighbours[n_neighbours++] = blockIdx.x - 1;
-        if (by + 1 < a.t.ty) neighbours[n_neighbours++] = blockIdx.x + 1;
+__device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, int2 c, int colour, int lane,
+                                             const float (&du)[LANES]) {
+    const int gi = c.y >> 16, gj = c.y & 0xffff;
+    const int kp = (colour + gi + gj) & 1;
+    const int own = kp * w.ncm + c.x * w.M;
+    const int oth = (kp ^ 1) * w.ncm + c.x * w.M;
+    const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
+    float* s = w.s;
+#pragma unroll
+    for (int r = 0; r < LANES; ++r) {
+        if (!(du[r] >= 0.0f)) continue;
+        const int m = lane + 32 * r;
+        const int io = own + m;
+        const float o = s[io];
+        const float cc = div_rn(du[r], w.K + o);
+        float prod = 0.0f;
+        if (HAS_PROD) prod = prod_term(a, gi * w.sx + static_cast<int64_t>(gj) * w.nz + 2 * m + kp);
+        const float nb = s[io - w.si] + s[io + w.si] + s[io - w.M] + s[io + w.M] + s[oth + max(m + kp - 1, 0)] +
+                         s[oth + min(m + kp, last)];
+        const float gs = div_rn(nb + w.h * prod, 6.0f + w.h * cc);
+        s[io] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
     }
-    // Per (column, colour) table after the two parity planes: shared-memory offsets of the own
-    // and other parity column, the coefficient row, and the entry count / last other entry / parity.
-    int4* tab = reinterpret_cast<int4*>(s + ((2 * g.ncm + 3) & ~3));
-    const int64_t sx = static_cast<int64_t>(ny) * nz;
-    const int si = g.stride_i * M;
-    // Columns other tiles read: the edge rows / columns, plus the second one on a Neumann face
-    // (its mirror image is the halo of this very tile).
-    int rows[4], cols[4], nrow = 0, ncol = 0;
-    rows[nrow++] = 0;
-    if (g.ai > 1) rows[nrow++] = g.ai - 1;
-    if (a.p.bc_x == 1 && g.i0 == 0 && g.ai > 1) rows[nrow++] = 1;
-    if (a.p.bc_x == 1 && g.i0 + g.ai == nx && g.ai > 2) rows[nrow++] = g.ai - 2;
-    cols[ncol++] = 0;
-    if (g.aj > 1) cols[ncol++] = g.aj - 1;
-    if (a.p.bc_y == 1 && g.j0 == 0 && g.aj > 1) cols[ncol++] = 1;
-    if (a.p.bc_y == 1 && g.j0 + g.aj == ny && g.aj > 2) cols[ncol++] = g.aj - 2;
-    const int n_publish = nrow * g.aj + ncol * g.ai;
-    const int n_ring = 2 * (g.ai + g.aj);
-    const int ncolumns = g.ai * g.aj;
+}
 
-    // Tile + halo ring (mirrored at the domain faces) into shared memory; the owned columns'
-    // coefficients into the parity-split scratch copy; the column table.
-    {
-        const int span = g.aj + 2;
-        const int cols_all = (g.ai + 2) * span;
-        for (int col = warp; col < cols_all; col += nwarps) {
-            const int lrow = col / span;
-            const int li = lrow - 1, lj = col - lrow * span - 1;
-            const int gi = mirror(g.i0 + li, nx), gj = mirror(g.j0 + lj, ny);
-            const int c2 = (li + 1) * g.stride_i + (lj + 1);
-            const bool owned = li >= 0 && li < g.ai && lj >= 0 && lj < g.aj;
-            const int64_t base = gi * sx + static_cast<int64_t>(gj) * nz;
-            for (int k = lane; k < nz; k += 32) {
-                const int64_t idx = base + k;
-                s[(k & 1) * g.ncm + c2 * M + (k >> 1)] = a.field[idx];
-                if (owned) {
-                    const wbc_sor_params& p = a.p;
-                    const bool face = (p.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
-                                      (p.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
-                                      (p.bc_z == 0 && (k == 0 || k == nz - 1));
-                    float v = -1.0f;
-                    if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
-                    a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+// The columns list[0 .. end) for one colour, a warp per column; the next column's coefficients
+// are loaded before the current column is relaxed.
+template <bool HAS_PROD, int LANES>
+__device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, const int2* list, int end, int colour,
+                                              int warp, int nwarps, int lane) {
+    int q = warp;
+    if (q >= end) return;
+    int2 c = list[q];
+    float du[LANES];
+    load_coeff<LANES>(w, c, colour, lane, du);
+    while (true) {
+        const int qn = q + nwarps;
+        const bool more = qn < end;
+        int2 cn = c;
+        float dn[LANES];
+        if (more) {
+            cn = list[qn];
+            load_coeff<LANES>(w, cn, colour, lane, dn);
+        }
+        relax_column<HAS_PROD, LANES>(a, w, c, colour, lane, du);
+        if (!more) break;
+        c = cn;
+#pragma unroll
+        for (int r = 0; r < LANES; ++r) du[r] = dn[r];
+        q = qn;
+    }
+}
+
+// Waits until every listed CTA has signalled `epoch`; false when aborted (timeout here or elsewhere).
+__device__ __forceinline__ bool wait_for(SorControl* ctl, const unsigned int* flags, unsigned int epoch,
+                                         const int* who, int n) {
+    int aborted = 0;
+    if (static_cast<int>(threadIdx.x) < n) {
+        const unsigned int* f = flags + who[threadIdx.x];
+        unsigned polls = 0;
+        while (static_cast<int>(load_acquire(f) - epoch) < 0) {
+            if ((++polls & 255u) == 0u) {
+                if (load_acquire(&ctl->abort) != 0u) {
+                    aborted = 1;
+                    break;
+                }
+                if (polls > kBarrierPolls) {
+                    atomicExch(&ctl->abort, 1u);
+                    aborted = 1;
+                    break;
                 }
             }
         }
-        for (int e = threadIdx.x; e < 2 * ncolumns; e += blockDim.x) {
-            const int col = e >> 1, colour = e & 1;
-            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-            const int gi = g.i0 + li, gj = g.j0 + lj;
-            const int kp = (colour + gi + gj) & 1;
-            const int c2 = (li + 1) * g.stride_i + (lj + 1);
-            const int cnt = kp ? nz / 2 : (nz + 1) / 2;
-            const int last = (kp ? (nz + 1) / 2 : nz / 2) - 1;
-            tab[e] = make_int4(kp * g.ncm + c2 * M, (kp ^ 1) * g.ncm + c2 * M,
-                               static_cast<int>(((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M),
-                               cnt | (last << 9) | (kp << 18));
+    }
+    return __syncthreads_or(aborted) == 0;
+}
+
+// Copies parity `par` (or both, par < 0) of columns between the exchange buffer and shared memory.
+__device__ __forceinline__ void copy_columns(const Sweep& w, const int2* list, int n, float* xb, int colour,
+                                             bool both, bool to_xchg, int warp, int nwarps, int lane) {
+    for (int q = warp; q < n; q += nwarps) {
+        const int2 c = list[q];
+        const int gi = c.y >> 16, gj = c.y & 0xffff;
+        for (int par = 0; par < 2; ++par) {
+            if (!both && par != ((colour + gi + gj) & 1)) continue;
+            const int cnt = par ? w.cnt_odd : w.cnt_even;
+            float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M;
+            float* sm = w.s + par * w.ncm + c.x * w.M;
+            if (to_xchg) {
+                for (int m = lane; m < cnt; m += 32) __stcg(x + m, sm[m]);
+            } else {
+                for (int m = lane; m < cnt; m += 32) sm[m] = __ldcg(x + m);
+            }
+        }
+    }
+}
+
+// Refreshes the outside-the-domain columns from their mirror images: the parity that colour
+// `colour` updates in the mirror column, or both.
+__device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list, int n, int bw, int gi0, int gj0,
+                                               int colour, bool both, int warp, int nwarps, int lane) {
+    for (int q = warp; q < n; q += nwarps) {
+        const int2 c = list[q];
+        const int mi = c.y / bw, mj = c.y - (c.y / bw) * bw;
+        const int kp_colour = (colour + gi0 + mi + gj0 + mj) & 1;
+        for (int par = 0; par < 2; ++par) {
+            if (!both && par != kp_colour) continue;
+            const int cnt = par ? w.cnt_odd : w.cnt_even;
+            float* dst = w.s + par * w.ncm + c.x * w.M;
+            const float* src = w.s + par * w.ncm + c.y * w.M;
+            for (int m = lane; m < cnt; m += 32) dst[m] = src[m];
+        }
+    }
+}
+
+template <bool HAS_PROD, int LANES, int H>
+__global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
+    extern __shared__ float s[];
+    __shared__ unsigned int s_red[32];
+    __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
+    const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int bx = blockIdx.x / a.t.ty;
+    const int by = blockIdx.x - bx * a.t.ty;
+    const int i0 = bx * a.t.ti, j0 = by * a.t.tj;
+    const int ai = min(a.t.ti, nx - i0), aj = min(a.t.tj, ny - j0);
+    const int bw = a.t.tj + 2 * H;  // bounding-box row length
+    const int nbox = a.t.nbox;
+    Sweep w;
+    w.s = s;
+    w.coeff = a.coeff;
+    w.M = M;
+    w.ncm = nbox * M;  // floats per parity plane
+    w.si = bw * M;
+    w.nx = nx;
+    w.ny = ny;
+    w.nz = nz;
+    w.cnt_even = (nz + 1) / 2;
+    w.cnt_odd = nz / 2;
+    w.sx = static_cast<int64_t>(ny) * nz;
+    w.K = a.p.michaelis_k;
+    w.h = a.p.dx2_over_D;
+    w.omega = a.p.omega;
+    w.one_minus_omega = 1.0f - a.p.omega;
+    __shared__ int s_neighbours[8];
+    __shared__ int s_n_neighbours;
+    if (threadIdx.x == 0) {
+        int n = 0;
+        for (int di = -1; di <= 1; ++di)
+            for (int dj = -1; dj <= 1; ++dj) {
+                if ((di == 0 && dj == 0) || (H == 1 && di != 0 && dj != 0)) continue;
+                const int nbx = bx + di, nby = by + dj;
+                if (nbx >= 0 && nbx < a.t.tx && nby >= 0 && nby < a.t.ty) s_neighbours[n++] = nbx * a.t.ty + nby;
+            }
+        s_n_neighbours = n;
+    }
+
+    // ---- column lists ---------------------------------------------------------------------------------
+    Lists L;
+    {
+        int2* base = reinterpret_cast<int2*>(reinterpret_cast<char*>(s) + a.t.planes_bytes);
+        L.upd = base;
+        L.pull = base + nbox;
+        L.publish = base + 2 * nbox;
+        L.inner = base + 3 * nbox;
+        L.mir = base + 4 * nbox;
+        L.upd_end = reinterpret_cast<int*>(base + 5 * nbox);
+    }
+    if (threadIdx.x < 12) s_counts[threadIdx.x] = 0;
+    __syncthreads();
+    const int box_rows = ai + 2 * H, box_cols = aj + 2 * H;
+    auto dist_of = [&](int li, int lj) {
+        const int di = li < 0 ? -li : (li >= ai ? li - ai + 1 : 0);
+        const int dj = lj < 0 ? -lj : (lj >= aj ? lj - aj + 1 : 0);
+        return di + dj;
+    };
+    // pass 1: count in-domain columns per distance class
+    for (int e = threadIdx.x; e < box_rows * box_cols; e += blockDim.x) {
+        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
+        const int d = dist_of(li, lj);
+        const int gi = i0 + li, gj = j0 + lj;
+        if (d < H && gi >= 0 && gi < nx && gj >= 0 && gj < ny) atomicAdd(&s_counts[d], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int run = 0;
+        for (int d = 0; d < H; ++d) {
+            const int c = s_counts[d];
+            s_counts[d] = run;  // start of class d
+            run += c;
+            L.upd_end[d] = run;
         }
     }
     __syncthreads();
+    // pass 2: fill the lists
+    for (int e = threadIdx.x; e < box_rows * box_cols; e += blockDim.x) {
+        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
+        const int d = dist_of(li, lj);
+        if (d > H) continue;
+        const int gi = i0 + li, gj = j0 + lj;
+        const int box = (li + H) * bw + (lj + H);
+        const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
+        if (inside) {
+            const int2 c = make_int2(box, (gi << 16) | gj);
+            if (d < H) L.upd[atomicAdd(&s_counts[d], 1)] = c;
+            if (d >= 1) L.pull[atomicAdd(&s_counts[8], 1)] = c;
+            if (d == 0) {
+                if (li < H || li >= ai - H || lj < H || lj >= aj - H)
+                    L.publish[atomicAdd(&s_counts[9], 1)] = c;
+                else
+                    L.inner[atomicAdd(&s_counts[10], 1)] = c;
+            }
+        } else {
+            const int mi = mirror(gi, nx) - i0 + H, mj = mirror(gj, ny) - j0 + H;
+            L.mir[atomicAdd(&s_counts[11], 1)] = make_int2(box, mi * bw + mj);
+        }
+    }
+    __syncthreads();
+    L.n_pull = s_counts[8];
+    L.n_publish = s_counts[9];
+    L.n_inner = s_counts[10];
+    L.n_mir = s_counts[11];
+    const int n_neighbours = s_n_neighbours;
+    const int gi0 = i0 - H, gj0 = j0 - H;  // global position of box row / column 0
 
-    const float omega = a.p.omega;
-    const float one_minus_omega = 1.0f - omega;
-    const float h = a.p.dx2_over_D;
-    const float K = a.p.michaelis_k;
-    const float* __restrict__ coeff = a.coeff;
+    // ---- tile + halo into shared memory; owned coefficients into the scratch copy -------------------
+    for (int e = warp; e < box_rows * box_cols; e += nwarps) {
+        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
+        if (dist_of(li, lj) > H) continue;
+        const int gi = mirror(i0 + li, nx), gj = mirror(j0 + lj, ny);
+        const int box = (li + H) * bw + (lj + H);
+        const bool owned = li >= 0 && li < ai && lj >= 0 && lj < aj;
+        const int64_t base = gi * w.sx + static_cast<int64_t>(gj) * nz;
+        for (int k = lane; k < nz; k += 32) {
+            const int64_t idx = base + k;
+            s[(k & 1) * w.ncm + box * M + (k >> 1)] = a.field[idx];
+            if (owned) {
+                const wbc_sor_params& p = a.p;
+                const bool face = (p.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
+                                  (p.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
+                                  (p.bc_z == 0 && (k == 0 || k == nz - 1));
+                float v = -1.0f;
+                if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
+                a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+            }
+        }
+    }
     unsigned int epoch = 0;
+    // The ring columns' coefficients are written by their owners: one global barrier first.
+    bool ok = grid_barrier(a.ctl, a.flags, epoch);
+
+    const float K = w.K, h = w.h;
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
     bool converged = false;
-    bool ok = true;
     int chunk_index = 0;
-    while (sweeps < a.max_sweeps) {
+    unsigned int interval = 0;
+    const int signal_thread = blockDim.x - 32;  // lane 0 of the last warp, which has the fewest inner columns
+    while (ok && sweeps < a.max_sweeps) {
         const int chunk = min(a.check_every, a.max_sweeps - sweeps);
-        for (int sweep = 0; sweep < chunk && ok; ++sweep) {
-            for (int colour = 0; colour < 2 && ok; ++colour) {
-                for (int col = warp; col < ncolumns; col += nwarps) {
-                    const int4 e = tab[2 * col + colour];
-                    const int cnt = e.w & 511, last = (e.w >> 9) & 511, kp = e.w >> 18;
-                    float du[LANES];
-#pragma unroll
-                    for (int r = 0; r < LANES; ++r) {
-                        const int m = lane + 32 * r;
-                        du[r] = m < cnt ? coeff[e.z + m] : -1.0f;
-                    }
-#pragma unroll
-                    for (int r = 0; r < LANES; ++r) {
-                        if (!(du[r] >= 0.0f)) continue;
-                        const int m = lane + 32 * r;
-                        const int io = e.x + m;
-                        const float o = s[io];
-                        const float c = du[r] / (K + o);
-                        float prod = 0.0f;
-                        if (HAS_PROD) {
-                            const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-                            prod = prod_term(a, (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz + 2 * m + kp);
-                        }
-                        const float nb = s[io - si] + s[io + si] + s[io - M] + s[io + M] + s[e.y + max(m + kp - 1, 0)] +
-                                         s[e.y + min(m + kp, last)];
-                        const float gs = (nb + h * prod) / (6.0f + h * c);
-                        s[io] = fmaxf(one_minus_omega * o + omega * gs, 0.0f);
-                    }
-                }
+        int half_left = 2 * chunk;
+        int colour = 0;
+        while (ok && half_left > 0) {
+            if constexpr (H == 1) {
+                // Edge columns first, published while the inner columns are relaxed; the parity
+                // split of the exchange buffer keeps a colour's entries until the neighbour has
+                // signalled the next colour, which follows its pull.
+                relax_columns<HAS_PROD, LANES>(a, w, L.publish, L.n_publish, colour, warp, nwarps, lane);
                 __syncthreads();
-                // publish the updated colour of the columns other tiles read
-                for (int r = warp; r < n_publish; r += nwarps) {
-                    int li, lj;
-                    if (!publish_column(g, rows, nrow, cols, r, li, lj)) continue;
-                    const int gi = g.i0 + li, gj = g.j0 + lj;
-                    const int kpar = (colour + gi + gj) & 1;
-                    const int cnt = kpar ? nz / 2 : (nz + 1) / 2;
-                    float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
-                    const float* sm = s + kpar * g.ncm + ((li + 1) * g.stride_i + (lj + 1)) * M;
-                    for (int m = lane; m < cnt; m += 32) __stcg(x + m, sm[m]);
-                }
-                // A neighbour overwrites these entries only after this tile has signalled the next
-                // epoch, i.e. after the pull below: waiting for the four neighbours suffices.
-                ok = grid_barrier(a.ctl, a.flags, epoch, neighbours, n_neighbours);
+                copy_columns(w, L.publish, L.n_publish, a.xchg, colour, false, true, warp, nwarps, lane);
+                __syncthreads();
+                epoch += 1;
+                if (static_cast<int>(threadIdx.x) == signal_thread) store_release(a.flags + blockIdx.x, epoch);
+                relax_columns<HAS_PROD, LANES>(a, w, L.inner, L.n_inner, colour, warp, nwarps, lane);
+                ok = wait_for(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
                 if (!ok) break;
-                // pull the halo ring's updated colour (mirroring moves i, j by 2: parity kept)
-                for (int r = warp; r < n_ring; r += nwarps) {
-                    int li, lj;
-                    ring_column(g, r, li, lj);
-                    const int gi_u = g.i0 + li, gj_u = g.j0 + lj;
-                    const int kpar = (colour + gi_u + gj_u) & 1;
-                    const int cnt = kpar ? nz / 2 : (nz + 1) / 2;
-                    const int gi = mirror(gi_u, nx), gj = mirror(gj_u, ny);
-                    const float* x = a.xchg + ((static_cast<int64_t>(kpar) * nx + gi) * ny + gj) * M;
-                    float* sm = s + kpar * g.ncm + ((li + 1) * g.stride_i + (lj + 1)) * M;
-                    for (int m = lane; m < cnt; m += 32) sm[m] = __ldcg(x + m);
-                }
+                copy_columns(w, L.pull, L.n_pull, a.xchg, colour, false, false, warp, nwarps, lane);
                 __syncthreads();
+                mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
+                __syncthreads();
+                colour ^= 1;
+                half_left -= 1;
+            } else {
+                // H half-sweeps over shrinking regions (the halo columns relaxed redundantly), then
+                // one exchange of both parities through a double buffer.
+                const int nph = min(H, half_left);
+                for (int ph = 0; ph < nph; ++ph) {
+                    relax_columns<HAS_PROD, LANES>(a, w, L.upd, L.upd_end[nph - 1 - ph], colour, warp, nwarps, lane);
+                    __syncthreads();
+                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
+                    __syncthreads();
+                    colour ^= 1;
+                }
+                half_left -= nph;
+                float* xb = a.xchg + static_cast<int64_t>(interval & 1u) * 2 * nx * ny * M;
+                copy_columns(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
+                // A neighbour overwrites this buffer two exchanges later, i.e. only after this tile
+                // has signalled the next epoch, which comes after the pull below.
+                ok = grid_barrier(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
+                if (!ok) break;
+                copy_columns(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
+                __syncthreads();
+                mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, 0, true, warp, nwarps, lane);
+                __syncthreads();
+                ++interval;
             }
         }
         if (!ok) break;
         sweeps += chunk;
         // Max-norm residual of the current field over every updated node (both colours).
         unsigned int bits = 0u;
-        for (int e2 = warp; e2 < 2 * ncolumns; e2 += nwarps) {
-            const int4 e = tab[e2];
-            const int col = e2 >> 1;
-            const int cnt = e.w & 511, last = (e.w >> 9) & 511, kp = e.w >> 18;
-            for (int m = lane; m < cnt; m += 32) {
-                const float du = coeff[e.z + m];
-                if (!(du >= 0.0f)) continue;
-                const int io = e.x + m;
-                const float o = s[io];
-                const float c = du / (K + o);
-                float prod = 0.0f;
-                if (HAS_PROD) {
-                    const int li = col / g.aj, lj = col - (col / g.aj) * g.aj;
-                    prod = prod_term(a, (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz + 2 * m + kp);
+        const int n_owned = L.upd_end[0];
+        for (int q = warp; q < n_owned; q += nwarps) {
+            const int2 c = L.upd[q];
+            const int gi = c.y >> 16, gj = c.y & 0xffff;
+            for (int kp = 0; kp < 2; ++kp) {
+                const int own = kp * w.ncm + c.x * M;
+                const int oth = (kp ^ 1) * w.ncm + c.x * M;
+                const int cnt = kp ? w.cnt_odd : w.cnt_even;
+                const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
+                const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
+                for (int m = lane; m < cnt; m += 32) {
+                    const float du = crow[m];
+                    if (!(du >= 0.0f)) continue;
+                    const int io = own + m;
+                    const float o = s[io];
+                    const float cc = div_rn(du, K + o);
+                    float prod = 0.0f;
+                    if (HAS_PROD) prod = prod_term(a, gi * w.sx + static_cast<int64_t>(gj) * nz + 2 * m + kp);
+                    const float nb = s[io - w.si] + s[io + w.si] + s[io - M] + s[io + M] +
+                                     s[oth + max(m + kp - 1, 0)] + s[oth + min(m + kp, last)];
+                    const float r = nb + h * prod - (6.0f + h * cc) * o;
+                    const float val = div_rn(fabsf(r), fmaxf(6.0f * o, a.p.reference));
+                    bits = max(bits, __float_as_uint(val));
                 }
-                const float nb = s[io - si] + s[io + si] + s[io - M] + s[io + M] + s[e.y + max(m + kp - 1, 0)] +
-                                 s[e.y + min(m + kp, last)];
-                const float r = nb + h * prod - (6.0f + h * c) * o;
-                const float val = fabsf(r) / fmaxf(6.0f * o, a.p.reference);
-                bits = max(bits, __float_as_uint(val));
             }
         }
 #pragma unroll
@@ -368,12 +527,12 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
         return;
     }
     // Owned columns back to the field.
-    for (int col = warp; col < ncolumns; col += nwarps) {
-        const int li = col / g.aj;
-        const int lj = col - li * g.aj;
-        const int c2 = (li + 1) * g.stride_i + (lj + 1);
-        float* out = a.field + (g.i0 + li) * sx + static_cast<int64_t>(g.j0 + lj) * nz;
-        for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * g.ncm + c2 * M + (k >> 1)];
+    const int n_owned = L.upd_end[0];
+    for (int q = warp; q < n_owned; q += nwarps) {
+        const int2 c = L.upd[q];
+        const int gi = c.y >> 16, gj = c.y & 0xffff;
+        float* out = a.field + gi * w.sx + static_cast<int64_t>(gj) * nz;
+        for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * w.ncm + c.x * M + (k >> 1)];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ctl->sweeps = sweeps;
@@ -386,22 +545,29 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
 // ---- host side -------------------------------------------------------------------------------------------
 using KernelFn = void (*)(SorArgs);
 
-template <bool P>
+template <bool P, int Hd>
 static KernelFn kernel_for_lanes(int lanes) {
     switch (lanes) {
-        case 1: return k_sor_resident<P, 1>;
-        case 2: return k_sor_resident<P, 2>;
-        case 3: return k_sor_resident<P, 3>;
-        case 4: return k_sor_resident<P, 4>;
-        case 5: return k_sor_resident<P, 5>;
-        case 6: return k_sor_resident<P, 6>;
-        case 7: return k_sor_resident<P, 7>;
-        default: return k_sor_resident<P, 8>;
+        case 1: return k_sor_resident<P, 1, Hd>;
+        case 2: return k_sor_resident<P, 2, Hd>;
+        case 3: return k_sor_resident<P, 3, Hd>;
+        case 4: return k_sor_resident<P, 4, Hd>;
+        case 5: return k_sor_resident<P, 5, Hd>;
+        case 6: return k_sor_resident<P, 6, Hd>;
+        case 7: return k_sor_resident<P, 7, Hd>;
+        default: return k_sor_resident<P, 8, Hd>;
     }
 }
 
-static KernelFn kernel_for(bool has_prod, int lanes) {
-    return has_prod ? kernel_for_lanes<true>(lanes) : kernel_for_lanes<false>(lanes);
+static KernelFn kernel_for(bool has_prod, int lanes, int H) {
+    if (has_prod) {
+        if (H == 1) return kernel_for_lanes<true, 1>(lanes);
+        if (H == 2) return kernel_for_lanes<true, 2>(lanes);
+        return kernel_for_lanes<true, 4>(lanes);
+    }
+    if (H == 1) return kernel_for_lanes<false, 1>(lanes);
+    if (H == 2) return kernel_for_lanes<false, 2>(lanes);
+    return kernel_for_lanes<false, 4>(lanes);
 }
 
 struct DeviceInfo {
@@ -427,34 +593,44 @@ static DeviceInfo device_info() {
     return d;
 }
 
-// tx x ty tiles, at most one CTA per SM, minimising the columns of the largest tile (then the
-// halo perimeter); the tile plus halo must fit in shared memory.
-static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, SorTiling* out) {
+static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t smem_limit, SorTiling* out) {
     const int M = (p.nz + 1) / 2;
-    if (M > 32 * kMaxLanesPerColumn) return false;
-    bool found = false;
-    SorTiling best{};
-    long best_score = 0;
+    const int ti = (p.nx + tx - 1) / tx, tj = (p.ny + ty - 1) / ty;
+    if (ti < H || tj < H || ti < 2 || tj < 2) return false;
+    const int ex = (p.nx + ti - 1) / ti, ey = (p.ny + tj - 1) / tj;
+    const int nbox = (ti + 2 * H) * (tj + 2 * H);
+    const size_t planes = ((2ull * nbox * M * sizeof(float)) + 15) & ~15ull;
+    const size_t lists = 5ull * nbox * sizeof(int2) + 16 * sizeof(int);
+    const size_t smem = planes + lists;
+    if (smem > smem_limit) return false;
+    const int warps = std::min(32, std::max(1, ti * tj));
+    *out = SorTiling{ex, ey, ti, tj, M, 32 * warps, H, nbox, planes, smem};
+    return true;
+}
+
+// tx x ty tiles, at most one CTA per SM (and within the barrier flags), minimising the columns of
+// the largest tile, then the halo perimeter.
+static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, int H, int want_tx, int want_ty,
+                          SorTiling* out) {
+    const int M = (p.nz + 1) / 2;
+    if (M > 32 * kMaxLanesPerColumn || p.nx > 32767 || p.ny > 32767) return false;
     const int max_ctas = std::min(sms, kMaxCtas);
+    if (want_tx > 0 && want_ty > 0) return want_tx * want_ty <= max_ctas && tiling_for(p, want_tx, want_ty, H, smem_limit, out);
+    bool found = false;
+    long best_score = 0;
     for (int tx = 1; tx <= std::min(p.nx, max_ctas); ++tx) {
         const int ty_max = std::min(p.ny, max_ctas / tx);
         for (int ty = 1; ty <= ty_max; ++ty) {
-            const int ti = (p.nx + tx - 1) / tx, tj = (p.ny + ty - 1) / ty;
-            if (ti < 2 || tj < 2) continue;
-            const int ex = (p.nx + ti - 1) / ti, ey = (p.ny + tj - 1) / tj;
-            const size_t planes = (2ull * (ti + 2) * (tj + 2) * M + 3) & ~3ull;
-            const size_t smem = planes * sizeof(float) + 2ull * ti * tj * sizeof(int4);
-            if (smem > smem_limit) continue;
-            const long score = static_cast<long>(ti) * tj * 1000 + (ti + tj);
+            SorTiling t{};
+            if (!tiling_for(p, tx, ty, H, smem_limit, &t)) continue;
+            const long score = static_cast<long>(t.ti) * t.tj * 1000 + (t.ti + t.tj);
             if (!found || score < best_score) {
                 found = true;
                 best_score = score;
-                const int warps = std::min(32, ti * tj);
-                best = SorTiling{ex, ey, ti, tj, M, 32 * warps, smem};
+                *out = t;
             }
         }
     }
-    if (found) *out = best;
     return found;
 }
 
@@ -464,18 +640,52 @@ static size_t plane_bytes(const wbc_sor_params& p) {
 
 static size_t header_bytes() { return sizeof(SorControl) + kMaxCtas * sizeof(unsigned int); }
 
-size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 2 * plane_bytes(p) + 256; }
+size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 3 * plane_bytes(p) + 256; }
 
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
-                       float* field, wbc_sor_report* report, void* workspace, cudaStream_t stream, bool* feasible) {
+                       float* field, wbc_sor_report* report, void* workspace, const wbc_sor_tuning* tuning,
+                       cudaStream_t stream, bool* feasible) {
     const DeviceInfo dev = device_info();
-    SorTiling t{};
     const size_t reserve = 1024;  // static shared memory of the kernel
-    *feasible = dev.sms > 0 && choose_tiling(p, dev.sms, static_cast<size_t>(dev.smem_optin) - reserve, &t);
+    const size_t limit = static_cast<size_t>(dev.smem_optin) - reserve;
+    SorTiling t{};
+    int H = tuning && tuning->halo_depth > 0 ? tuning->halo_depth : 0;
+    const int want_tx = tuning ? tuning->tiles_i : 0, want_ty = tuning ? tuning->tiles_j : 0;
+    if (H != 0 && H != 1 && H != 2 && H != 4) {
+        set_error_msg("wbc_sor_solve: halo_depth must be 1, 2 or 4");
+        return WBC_ERR_INVALID;
+    }
+    *feasible = false;
+    if (dev.sms > 0) {
+        if (H != 0) {
+            *feasible = choose_tiling(p, dev.sms, limit, H, want_tx, want_ty, &t);
+        } else {
+            // Default: a one-column halo, exchanged while the inner columns are relaxed, when
+            // the tiles have inner columns to hide it behind; otherwise the deepest halo that fits
+            // (fewer exchanges for small grids, where the exchange latency dominates).
+            SorTiling t1{};
+            const bool f1 = choose_tiling(p, dev.sms, limit, 1, want_tx, want_ty, &t1);
+            if (f1 && std::min(t1.ti, t1.tj) >= 4) {
+                t = t1;
+                *feasible = true;
+            } else {
+                for (int depth : {4, 2}) {
+                    if (choose_tiling(p, dev.sms, limit, depth, want_tx, want_ty, &t)) {
+                        *feasible = true;
+                        break;
+                    }
+                }
+                if (!*feasible && f1) {
+                    t = t1;
+                    *feasible = true;
+                }
+            }
+        }
+    }
     if (!*feasible) return WBC_OK;
     const bool has_prod = production != nullptr || p.has_source;
-    KernelFn fn = kernel_for(has_prod, (t.M + 31) / 32);
+    KernelFn fn = kernel_for(has_prod, (t.M + 31) / 32, t.H);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem));
     if (err != cudaSuccess) {
@@ -493,14 +703,14 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     auto* ctl = reinterpret_cast<SorControl*>(base);
     auto* flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
     float* xchg = reinterpret_cast<float*>(base + header_bytes());
-    float* coeff = reinterpret_cast<float*>(base + header_bytes() + plane_bytes(p));
+    float* coeff = reinterpret_cast<float*>(base + header_bytes() + 2 * plane_bytes(p));
     err = cudaMemsetAsync(base, 0, header_bytes(), stream);
     if (err != cudaSuccess) {
         set_error("wbc_sor_solve: cudaMemsetAsync", err);
         return WBC_ERR_CUDA;
     }
-    SorArgs args{p,     t,    fixed,       density,    production, source,   field,
-                 xchg,  coeff, ctl,        flags,      check_every, max_sweeps, tolerance};
+    SorArgs args{p,    t,     fixed, density, production, source,      field,
+                 xchg, coeff, ctl,   flags,   check_every, max_sweeps, tolerance};
     void* params[] = {&args};
     err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(t.tx * t.ty), dim3(t.threads), params,
                                       t.smem, stream);
@@ -526,7 +736,33 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     report->converged = host.converged;
     report->path = 2;
     report->tiles = t.tx * t.ty;
+    report->halo_depth = t.H;
+    report->tiles_i = t.tx;
+    report->tiles_j = t.ty;
     return WBC_OK;
+}
+
+// Candidate tunings for the autotuner: per halo depth, the tile grid with the fewest columns per
+// tile, its transpose, and the squarest grid within the SM count.
+static std::vector<wbc_sor_tuning> tuning_candidates(const wbc_sor_params& p, int sms, size_t limit) {
+    std::vector<wbc_sor_tuning> out;
+    auto add = [&](int H, int want_tx, int want_ty) {
+        SorTiling t{};
+        if (!choose_tiling(p, sms, limit, H, want_tx, want_ty, &t)) return;
+        for (const wbc_sor_tuning& c : out)
+            if (c.halo_depth == H && c.tiles_i == t.tx && c.tiles_j == t.ty) return;
+        out.push_back(wbc_sor_tuning{H, t.tx, t.ty});
+    };
+    int q = 1;
+    while ((q + 1) * (q + 1) <= std::min(sms, kMaxCtas)) ++q;
+    for (int H : {1, 2, 4}) {
+        SorTiling t{};
+        if (!choose_tiling(p, sms, limit, H, 0, 0, &t)) continue;
+        add(H, t.tx, t.ty);
+        add(H, t.ty, t.tx);
+        add(H, q, q);
+    }
+    return out;
 }
 
 }  // namespace wbc
@@ -540,10 +776,78 @@ size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p) {
     return sor_workspace_bytes(*p);
 }
 
+int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t* fixed, const float* density,
+                     const float* production, const float* source, const float* field, float* scratch_field,
+                     void* workspace, size_t workspace_bytes, wbc_sor_tuning* best, float* best_us_per_sweep,
+                     void* stream) {
+    if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || check_every < 1 || !density || !field || !scratch_field ||
+        !workspace || !best || (p->has_source && !source))
+        return WBC_ERR_INVALID;
+    if (workspace_bytes < sor_workspace_bytes(*p)) return WBC_ERR_WORKSPACE;
+    *best = wbc_sor_tuning{0, 0, 0};
+    if (best_us_per_sweep) *best_us_per_sweep = 0.0f;
+    const DeviceInfo dev = device_info();
+    if (dev.sms <= 0) return WBC_OK;
+    const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;
+    const std::vector<wbc_sor_tuning> cands = tuning_candidates(*p, dev.sms, limit);
+    if (cands.empty()) return WBC_OK;
+    cudaStream_t s = as_stream(stream);
+    const size_t field_bytes = static_cast<size_t>(p->nx) * p->ny * p->nz * sizeof(float);
+    const int sweeps = 2 * check_every;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t err = cudaEventCreate(&e0);
+    if (err == cudaSuccess) err = cudaEventCreate(&e1);
+    if (err != cudaSuccess) {
+        set_error("wbc_sor_autotune: cudaEventCreate", err);
+        if (e0) cudaEventDestroy(e0);
+        return WBC_ERR_CUDA;
+    }
+    std::vector<float> best_ms(cands.size(), -1.0f);
+    int rc = WBC_OK;
+    for (int rep = 0; rep < 2 && rc == WBC_OK; ++rep) {
+        for (size_t c = 0; c < cands.size() && rc == WBC_OK; ++c) {
+            err = cudaMemcpyAsync(scratch_field, field, field_bytes, cudaMemcpyDeviceToDevice, s);
+            if (err == cudaSuccess) err = cudaEventRecord(e0, s);
+            if (err != cudaSuccess) {
+                set_error("wbc_sor_autotune: copying the field", err);
+                rc = WBC_ERR_CUDA;
+                break;
+            }
+            wbc_sor_report r{};
+            bool feasible = false;
+            // A negative tolerance never converges: every candidate runs the same sweeps.
+            rc = sor_solve_resident(*p, check_every, sweeps, -1.0, fixed, density, production, source, scratch_field,
+                                    &r, workspace, &cands[c], s, &feasible);
+            if (rc != WBC_OK) break;
+            err = cudaEventRecord(e1, s);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err != cudaSuccess) {
+                set_error("wbc_sor_autotune: timing", err);
+                rc = WBC_ERR_CUDA;
+                break;
+            }
+            if (feasible && (best_ms[c] < 0.0f || ms < best_ms[c])) best_ms[c] = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != WBC_OK) return rc;
+    int pick = -1;
+    for (size_t c = 0; c < cands.size(); ++c)
+        if (best_ms[c] >= 0.0f && (pick < 0 || best_ms[c] < best_ms[pick])) pick = static_cast<int>(c);
+    if (pick >= 0) {
+        *best = cands[pick];
+        if (best_us_per_sweep) *best_us_per_sweep = best_ms[pick] * 1000.0f / sweeps;
+    }
+    return WBC_OK;
+}
+
 int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
                   const int32_t* fixed, const float* density, const float* production, const float* source,
                   float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
-                  void* stream) {
+                  const wbc_sor_tuning* tuning, void* stream) {
     if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || check_every < 1 || max_sweeps < 1 || !density || !field ||
         !report || !workspace || (p->has_source && !source) || path < 0 || path > 2)
         return WBC_ERR_INVALID;
@@ -552,7 +856,7 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
     bool feasible = false;
     if (path != 1) {
         int rc = sor_solve_resident(*p, check_every, max_sweeps, tolerance, fixed, density, production, source, field,
-                                    report, workspace, s, &feasible);
+                                    report, workspace, tuning, s, &feasible);
         if (rc != WBC_OK || feasible) return rc;
         if (path == 2) {
             set_error_msg("wbc_sor_solve: the grid does not fit the shared-memory resident solver");
@@ -581,6 +885,9 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
     report->converged = static_cast<double>(residual) < tolerance ? 1 : 0;
     report->path = 1;
     report->tiles = 0;
+    report->halo_depth = 0;
+    report->tiles_i = 0;
+    report->tiles_j = 0;
     return WBC_OK;
 }
 

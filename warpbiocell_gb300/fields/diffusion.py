@@ -108,21 +108,55 @@ def solve_steady_state(
     params = sor_params(field, kinetics, settings.omega, has_source, source_k)
     workspace = _workspace(field, params)
     report = _lib.SorReportC()
+    if solver_tuning is not None:
+        tuning = _lib.SorTuningC(*solver_tuning)
+    elif solver_path != 1:
+        tuning = _autotuned(field, params, settings, density, prod, src, workspace)
+    else:
+        tuning = None
     with profiling.stage("sor"):
         _lib.call("wbc_sor_solve", ctypes.byref(params), int(settings.check_every), int(settings.max_sweeps),
                   float(settings.tolerance), _lib.ptr(field.fixed_or_none()), _lib.ptr(density), _lib.ptr(prod),
                   _lib.ptr(src), _lib.ptr(field.values), ctypes.byref(report), _lib.ptr(workspace),
-                  workspace.numel(), int(solver_path), _lib.stream(field.device))
+                  workspace.numel(), int(solver_path), ctypes.byref(tuning) if tuning is not None else None,
+                  _lib.stream(field.device))
     residual_buffer.fill_(float(report.residual))
-    last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles)
+    last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles, halo_depth=report.halo_depth,
+                      tiles_i=report.tiles_i, tiles_j=report.tiles_j)
     return SolveReport(sweeps=int(report.sweeps), residual=float(report.residual), converged=bool(report.converged))
 
 
 # 0: the shared-memory resident solver when the grid fits on chip, else streaming colour launches;
 # 1: streaming colour launches only; 2: resident only (an error if the grid does not fit).
 solver_path = 0
+# (halo_depth, tiles_i, tiles_j) for the resident solver: None = measured by the autotuner on the
+# first solve of each grid configuration; zeros = the library's built-in choice.
+solver_tuning: tuple[int, int, int] | None = None
 # sweeps / path / CTA count of the most recent solve (for benchmarks and tests)
 last_solve: dict = {}
+# autotuner results: key -> (halo_depth, tiles_i, tiles_j, us_per_sweep)
+autotune_cache: dict = {}
+
+
+def _autotuned(field: ScalarField, params: _lib.SorParamsC, settings: SolverSettings, density: torch.Tensor,
+               prod, src, workspace: torch.Tensor) -> _lib.SorTuningC:
+    """The resident solver's tuning for this grid configuration, timed once by ``wbc_sor_autotune``
+    on a copy of the field and cached (every tuning gives the same field bits)."""
+    fixed = field.fixed_or_none()
+    key = (str(field.device), field.geometry.shape, (params.bc_x, params.bc_y, params.bc_z), prod is not None,
+           bool(params.has_source), fixed is not None, int(settings.check_every))
+    hit = autotune_cache.get(key)
+    if hit is None:
+        best = _lib.SorTuningC()
+        us = ctypes.c_float(0.0)
+        scratch = torch.empty_like(field.values)
+        _lib.call("wbc_sor_autotune", ctypes.byref(params), int(settings.check_every), _lib.ptr(fixed),
+                  _lib.ptr(density), _lib.ptr(prod), _lib.ptr(src), _lib.ptr(field.values), _lib.ptr(scratch),
+                  _lib.ptr(workspace), workspace.numel(), ctypes.byref(best), ctypes.byref(us),
+                  _lib.stream(field.device))
+        hit = (int(best.halo_depth), int(best.tiles_i), int(best.tiles_j), float(us.value))
+        autotune_cache[key] = hit
+    return _lib.SorTuningC(*hit[:3])
 
 
 def _workspace(field: ScalarField, params: _lib.SorParamsC) -> torch.Tensor:
