@@ -216,6 +216,10 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.sor_tuning:
+        from warpbiocell_gb300.fields import diffusion as _diff
+
+        _diff.solver_tuning = tuple(int(v) for v in args.sor_tuning.split(","))
     w = WORKLOADS[args.workload]
     P = make_params(w)
     pos, radii = make_cells(w, seed=args.seed + rank)
@@ -579,6 +583,8 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline sample and parity check")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--sor-tuning", default="",
+                    help="halo_depth,tiles_i,tiles_j for the resident solver instead of the autotuner's pick")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)

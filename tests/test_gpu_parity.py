@@ -517,6 +517,27 @@ def test_resident_halo_depths_and_tilings_bitwise(shape, boundary):
         np.testing.assert_array_equal(a, b, err_msg=str(tuning))
 
 
+@pytest.mark.parametrize("shape, boundary", [
+    ((21, 17, 301), MIXED),
+    ((19, 22, 263), (Boundary.DIRICHLET,) * 3),
+])
+def test_resident_long_columns_bitwise(shape, boundary):
+    """Columns of more than 128 entries per parity (16-warp CTAs) at every halo depth."""
+    geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
+    rng = np.random.default_rng(3 + sum(shape))
+    start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
+    density = rng.uniform(0.0, 2.0e-3, shape).astype(np.float32)
+    production = rng.uniform(0.0, 40.0, shape).astype(np.float32)
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=40, check_every=10)
+    a, ra, _ = _solve_with_path(1, geom, boundary, start, density, production=production, settings=settings)
+    for tuning in [(1, 0, 0), (2, 0, 0), (4, 0, 0)]:
+        b, rb, ib = _solve_with_path(2, geom, boundary, start, density, production=production, settings=settings,
+                                     tuning=tuning)
+        assert ib["path"] == 2 and ib["halo_depth"] == tuning[0]
+        assert (ra.sweeps, ra.residual) == (rb.sweeps, rb.residual), tuning
+        np.testing.assert_array_equal(a, b, err_msg=str(tuning))
+
+
 def test_autotuned_solve_bitwise_equals_streaming():
     """The autotuner times candidate tunings on a scratch copy (the field is untouched) and the
     solve with its pick gives the streaming path's bits."""

@@ -146,6 +146,7 @@ struct Sweep {
     int ncm, M, si, nx, ny, nz, cnt_even, cnt_odd;
     int64_t sx;
     float K, h, omega, one_minus_omega;
+    bool zclamp;  // Neumann z faces: the k-neighbours of the end nodes are mirrored
 };
 
 template <int LANES>
@@ -153,11 +154,43 @@ __device__ __forceinline__ void load_coeff(const Sweep& w, int2 c, int colour, i
     const int gi = c.y >> 16, gj = c.y & 0xffff;
     const int kp = (colour + gi + gj) & 1;
     const int cnt = kp ? w.cnt_odd : w.cnt_even;
-    const float* crow = w.coeff + ((static_cast<int64_t>(kp) * w.nx + gi) * w.ny + gj) * w.M;
+    const float* crow = w.coeff + ((static_cast<int64_t>(kp) * w.nx + gi) * w.ny + gj) * w.M + lane;
+#pragma unroll
+    for (int r = 0; r < LANES; ++r) du[r] = lane + 32 * r < cnt ? crow[32 * r] : -1.0f;
+}
+
+// Entries m = lane + 32 r of one parity column: `po` points at entry `lane` of the column, the four
+// lateral neighbours are po -+ si (i) and po -+ M (j). The k-neighbours of entry m are entries
+// m + kp - 1 and m + kp of the other parity: with Dirichlet z faces every updated node has both
+// inside the column (pv points at entry lane + kp - 1), with Neumann z faces they are clamped to
+// the column ends (the mirror rule k = -1 -> 1, k = nz -> nz - 2).
+template <bool HAS_PROD, bool ZCLAMP, int LANES>
+__device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
+                                            int kp, int last, int64_t gbase, const float (&du)[LANES]) {
+    const float* pim = po - w.si;
+    const float* pip = po + w.si;
+    const float* pjm = po - w.M;
+    const float* pjp = po + w.M;
 #pragma unroll
     for (int r = 0; r < LANES; ++r) {
-        const int m = lane + 32 * r;
-        du[r] = m < cnt ? crow[m] : -1.0f;
+        if (!(du[r] >= 0.0f)) continue;
+        const int off = 32 * r;
+        const float o = po[off];
+        const float cc = div_rn(du[r], w.K + o);
+        float prod = 0.0f;
+        if (HAS_PROD) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+        float vlo, vhi;
+        if (ZCLAMP) {
+            const int m = lane + off;
+            vlo = pv[max(m + kp - 1, 0)];
+            vhi = pv[min(m + kp, last)];
+        } else {
+            vlo = pv[off];
+            vhi = pv[off + 1];
+        }
+        const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
+        const float gs = div_rn(nb + w.h * prod, 6.0f + w.h * cc);
+        po[off] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
     }
 }
 
@@ -168,24 +201,14 @@ __device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, i
                                              const float (&du)[LANES]) {
     const int gi = c.y >> 16, gj = c.y & 0xffff;
     const int kp = (colour + gi + gj) & 1;
-    const int own = kp * w.ncm + c.x * w.M;
-    const int oth = (kp ^ 1) * w.ncm + c.x * w.M;
+    float* po = w.s + kp * w.ncm + c.x * w.M + lane;
+    const float* oth = w.s + (kp ^ 1) * w.ncm + c.x * w.M;
     const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
-    float* s = w.s;
-#pragma unroll
-    for (int r = 0; r < LANES; ++r) {
-        if (!(du[r] >= 0.0f)) continue;
-        const int m = lane + 32 * r;
-        const int io = own + m;
-        const float o = s[io];
-        const float cc = div_rn(du[r], w.K + o);
-        float prod = 0.0f;
-        if (HAS_PROD) prod = prod_term(a, gi * w.sx + static_cast<int64_t>(gj) * w.nz + 2 * m + kp);
-        const float nb = s[io - w.si] + s[io + w.si] + s[io - w.M] + s[io + w.M] + s[oth + max(m + kp - 1, 0)] +
-                         s[oth + min(m + kp, last)];
-        const float gs = div_rn(nb + w.h * prod, 6.0f + w.h * cc);
-        s[io] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
-    }
+    const int64_t gbase = HAS_PROD ? gi * w.sx + static_cast<int64_t>(gj) * w.nz : 0;
+    if (w.zclamp)
+        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, du);
+    else
+        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
 }
 
 // The columns list[0 .. end) for one colour, a warp per column; the next column's coefficients
@@ -240,7 +263,10 @@ __device__ __forceinline__ bool wait_for(SorControl* ctl, const unsigned int* fl
     return __syncthreads_or(aborted) == 0;
 }
 
-// Copies parity `par` (or both, par < 0) of columns between the exchange buffer and shared memory.
+// Copies one parity (the one colour `colour` updates in each column) or both parities of the
+// listed columns between the exchange buffer and shared memory. All of a column's entries are
+// loaded before any is stored, so a warp has the whole column in flight at once.
+template <int LANES>
 __device__ __forceinline__ void copy_columns(const Sweep& w, const int2* list, int n, float* xb, int colour,
                                              bool both, bool to_xchg, int warp, int nwarps, int lane) {
     for (int q = warp; q < n; q += nwarps) {
@@ -249,12 +275,23 @@ __device__ __forceinline__ void copy_columns(const Sweep& w, const int2* list, i
         for (int par = 0; par < 2; ++par) {
             if (!both && par != ((colour + gi + gj) & 1)) continue;
             const int cnt = par ? w.cnt_odd : w.cnt_even;
-            float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M;
-            float* sm = w.s + par * w.ncm + c.x * w.M;
+            float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
+            float* sm = w.s + par * w.ncm + c.x * w.M + lane;
+            float v[LANES];
             if (to_xchg) {
-                for (int m = lane; m < cnt; m += 32) __stcg(x + m, sm[m]);
+#pragma unroll
+                for (int r = 0; r < LANES; ++r)
+                    if (lane + 32 * r < cnt) v[r] = sm[32 * r];
+#pragma unroll
+                for (int r = 0; r < LANES; ++r)
+                    if (lane + 32 * r < cnt) __stcg(x + 32 * r, v[r]);
             } else {
-                for (int m = lane; m < cnt; m += 32) sm[m] = __ldcg(x + m);
+#pragma unroll
+                for (int r = 0; r < LANES; ++r)
+                    if (lane + 32 * r < cnt) v[r] = __ldcg(x + 32 * r);
+#pragma unroll
+                for (int r = 0; r < LANES; ++r)
+                    if (lane + 32 * r < cnt) sm[32 * r] = v[r];
             }
         }
     }
@@ -278,8 +315,11 @@ __device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list,
     }
 }
 
+// Columns longer than 4 x 32 entries per parity run 16 warps per CTA (128 registers a thread).
+constexpr int max_threads_for_lanes(int lanes) { return lanes > 4 ? 512 : 1024; }
+
 template <bool HAS_PROD, int LANES, int H>
-__global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
+__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
     extern __shared__ float s[];
     __shared__ unsigned int s_red[32];
     __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
@@ -307,6 +347,7 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
     w.h = a.p.dx2_over_D;
     w.omega = a.p.omega;
     w.one_minus_omega = 1.0f - a.p.omega;
+    w.zclamp = a.p.bc_z != 0;
     __shared__ int s_neighbours[8];
     __shared__ int s_n_neighbours;
     if (threadIdx.x == 0) {
@@ -376,8 +417,15 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                     L.inner[atomicAdd(&s_counts[10], 1)] = c;
             }
         } else {
-            const int mi = mirror(gi, nx) - i0 + H, mj = mirror(gj, ny) - j0 + H;
-            L.mir[atomicAdd(&s_counts[11], 1)] = make_int2(box, mi * bw + mj);
+            // Only the columns just outside a Neumann face are read (by the face column, which is
+            // updated); across a Dirichlet face, at a corner or farther out nothing reads them.
+            const bool out_i = gi < 0 || gi >= nx, out_j = gj < 0 || gj >= ny;
+            const bool read = out_i != out_j && (out_i ? (a.p.bc_x != 0 && (gi == -1 || gi == nx))
+                                                       : (a.p.bc_y != 0 && (gj == -1 || gj == ny)));
+            if (read) {
+                const int mi = mirror(gi, nx) - i0 + H, mj = mirror(gj, ny) - j0 + H;
+                L.mir[atomicAdd(&s_counts[11], 1)] = make_int2(box, mi * bw + mj);
+            }
         }
     }
     __syncthreads();
@@ -432,17 +480,19 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                 // signalled the next colour, which follows its pull.
                 relax_columns<HAS_PROD, LANES>(a, w, L.publish, L.n_publish, colour, warp, nwarps, lane);
                 __syncthreads();
-                copy_columns(w, L.publish, L.n_publish, a.xchg, colour, false, true, warp, nwarps, lane);
+                copy_columns<LANES>(w, L.publish, L.n_publish, a.xchg, colour, false, true, warp, nwarps, lane);
                 __syncthreads();
                 epoch += 1;
                 if (static_cast<int>(threadIdx.x) == signal_thread) store_release(a.flags + blockIdx.x, epoch);
                 relax_columns<HAS_PROD, LANES>(a, w, L.inner, L.n_inner, colour, warp, nwarps, lane);
                 ok = wait_for(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
                 if (!ok) break;
-                copy_columns(w, L.pull, L.n_pull, a.xchg, colour, false, false, warp, nwarps, lane);
+                copy_columns<LANES>(w, L.pull, L.n_pull, a.xchg, colour, false, false, warp, nwarps, lane);
                 __syncthreads();
-                mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
-                __syncthreads();
+                if (L.n_mir > 0) {
+                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
+                    __syncthreads();
+                }
                 colour ^= 1;
                 half_left -= 1;
             } else {
@@ -452,21 +502,25 @@ __global__ void __launch_bounds__(1024, 1) k_sor_resident(SorArgs a) {
                 for (int ph = 0; ph < nph; ++ph) {
                     relax_columns<HAS_PROD, LANES>(a, w, L.upd, L.upd_end[nph - 1 - ph], colour, warp, nwarps, lane);
                     __syncthreads();
-                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
-                    __syncthreads();
+                    if (L.n_mir > 0) {
+                        mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
+                        __syncthreads();
+                    }
                     colour ^= 1;
                 }
                 half_left -= nph;
                 float* xb = a.xchg + static_cast<int64_t>(interval & 1u) * 2 * nx * ny * M;
-                copy_columns(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
+                copy_columns<LANES>(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
                 // A neighbour overwrites this buffer two exchanges later, i.e. only after this tile
                 // has signalled the next epoch, which comes after the pull below.
                 ok = grid_barrier(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
                 if (!ok) break;
-                copy_columns(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
+                copy_columns<LANES>(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
                 __syncthreads();
-                mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, 0, true, warp, nwarps, lane);
-                __syncthreads();
+                if (L.n_mir > 0) {
+                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, 0, true, warp, nwarps, lane);
+                    __syncthreads();
+                }
                 ++interval;
             }
         }
@@ -603,7 +657,7 @@ static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t sm
     const size_t lists = 5ull * nbox * sizeof(int2) + 16 * sizeof(int);
     const size_t smem = planes + lists;
     if (smem > smem_limit) return false;
-    const int warps = std::min(32, std::max(1, ti * tj));
+    const int warps = std::min(max_threads_for_lanes((M + 31) / 32) / 32, std::max(1, ti * tj));
     *out = SorTiling{ex, ey, ti, tj, M, 32 * warps, H, nbox, planes, smem};
     return true;
 }
