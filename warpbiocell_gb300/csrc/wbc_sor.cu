@@ -55,6 +55,7 @@ struct SorTiling {
     int H;       // halo depth = half-sweeps between exchanges
     int nbox;    // columns of the bounding box (ti + 2H) * (tj + 2H)
     size_t planes_bytes;
+    size_t table_offset;  // byte offset of the column table (2 int4 per box column)
     size_t smem;
 };
 
@@ -142,6 +143,7 @@ struct Lists {
 // Loop invariants of a colour half-sweep.
 struct Sweep {
     float* s;
+    const int4* tab;
     const float* coeff;
     int ncm, M, si, nx, ny, nz, cnt_even, cnt_odd;
     int64_t sx;
@@ -149,21 +151,37 @@ struct Sweep {
     bool zclamp;  // Neumann z faces: the k-neighbours of the end nodes are mirrored
 };
 
-template <int LANES>
-__device__ __forceinline__ void load_coeff(const Sweep& w, int2 c, int colour, int lane, float (&du)[LANES]) {
-    const int gi = c.y >> 16, gj = c.y & 0xffff;
+// Per (box column, colour) entry of the column table in shared memory:
+// x = offset of entry 0 of the parity the colour updates, y = the same for the other parity,
+// z = offset of the column's coefficient row (that parity) in the scratch copy,
+// w = kp | cnt << 1 | last << 11 (kp: the parity updated, cnt: its entries, last: the other
+// parity's last entry).
+__device__ __forceinline__ int4 column_entry(const Sweep& w, int box, int gi, int gj, int colour) {
     const int kp = (colour + gi + gj) & 1;
     const int cnt = kp ? w.cnt_odd : w.cnt_even;
-    const float* crow = w.coeff + ((static_cast<int64_t>(kp) * w.nx + gi) * w.ny + gj) * w.M + lane;
+    const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
+    return make_int4(kp * w.ncm + box * w.M, (kp ^ 1) * w.ncm + box * w.M, ((kp * w.nx + gi) * w.ny + gj) * w.M,
+                     kp | (cnt << 1) | (last << 11));
+}
+
+template <int LANES>
+__device__ __forceinline__ void load_column(const Sweep& w, const int2* list, int q, int colour, int lane, int2& c,
+                                            int4& e, float (&du)[LANES]) {
+    c = list[q];
+    e = w.tab[2 * c.x + colour];
+    const int cnt = (e.w >> 1) & 1023;
+    const float* crow = w.coeff + e.z + lane;
 #pragma unroll
     for (int r = 0; r < LANES; ++r) du[r] = lane + 32 * r < cnt ? crow[32 * r] : -1.0f;
 }
 
-// Entries m = lane + 32 r of one parity column: `po` points at entry `lane` of the column, the four
-// lateral neighbours are po -+ si (i) and po -+ M (j). The k-neighbours of entry m are entries
-// m + kp - 1 and m + kp of the other parity: with Dirichlet z faces every updated node has both
-// inside the column (pv points at entry lane + kp - 1), with Neumann z faces they are clamped to
-// the column ends (the mirror rule k = -1 -> 1, k = nz -> nz - 2).
+// Entries m = lane + 32 r of one parity column: `po` points at entry `lane`, the four lateral
+// neighbours are po -+ si (i) and po -+ M (j). The k-neighbours of entry m are entries m + kp - 1
+// and m + kp of the other parity: with Dirichlet z faces every updated node has both inside the
+// column (pv points at entry lane + kp - 1), with Neumann z faces they are clamped to the column
+// ends (the mirror rule k = -1 -> 1, k = nz -> nz - 2). Every lane computes; only nodes with a
+// coefficient (not a Dirichlet face, a pinned node or past the column end) are written, and the
+// IEEE division replaces the fast one only where an operand is outside its range.
 template <bool HAS_PROD, bool ZCLAMP, int LANES>
 __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
                                             int kp, int last, int64_t gbase, const float (&du)[LANES]) {
@@ -173,12 +191,15 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
     const float* pjp = po + w.M;
 #pragma unroll
     for (int r = 0; r < LANES; ++r) {
-        if (!(du[r] >= 0.0f)) continue;
         const int off = 32 * r;
+        const bool active = du[r] >= 0.0f;
         const float o = po[off];
-        const float cc = div_rn(du[r], w.K + o);
+        const float b1 = w.K + o;
+        float cc = div_rn_fast(du[r], b1);
         float prod = 0.0f;
-        if (HAS_PROD) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+        if (HAS_PROD) {
+            if (active) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+        }
         float vlo, vhi;
         if (ZCLAMP) {
             const int m = lane + off;
@@ -189,54 +210,124 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
             vhi = pv[off + 1];
         }
         const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
-        const float gs = div_rn(nb + w.h * prod, 6.0f + w.h * cc);
-        po[off] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
+        const float a2 = nb + w.h * prod;
+        float b2 = 6.0f + w.h * cc;
+        float gs = div_rn_fast(a2, b2);
+        if (active && !(div_fast_range(du[r], b1) && div_fast_range(a2, b2))) {
+            cc = __fdiv_rn(du[r], b1);
+            b2 = 6.0f + w.h * cc;
+            gs = __fdiv_rn(a2, b2);
+        }
+        if (active) po[off] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
     }
 }
 
 // One colour of one column: the reference's update (field_kernels.py:185-212) with the
 // Michaelis-Menten uptake linearised at the old value, over-relaxed and clamped at zero.
 template <bool HAS_PROD, int LANES>
-__device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, int2 c, int colour, int lane,
+__device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, int2 c, int4 e, int lane,
                                              const float (&du)[LANES]) {
-    const int gi = c.y >> 16, gj = c.y & 0xffff;
-    const int kp = (colour + gi + gj) & 1;
-    float* po = w.s + kp * w.ncm + c.x * w.M + lane;
-    const float* oth = w.s + (kp ^ 1) * w.ncm + c.x * w.M;
-    const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
-    const int64_t gbase = HAS_PROD ? gi * w.sx + static_cast<int64_t>(gj) * w.nz : 0;
+    const int kp = e.w & 1;
+    const int last = e.w >> 11;
+    float* po = w.s + e.x + lane;
+    const float* oth = w.s + e.y;
+    int64_t gbase = 0;
+    if (HAS_PROD) gbase = (c.y >> 16) * w.sx + static_cast<int64_t>(c.y & 0xffff) * w.nz;
     if (w.zclamp)
         relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, du);
     else
         relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
 }
 
-// The columns list[0 .. end) for one colour, a warp per column; the next column's coefficients
-// are loaded before the current column is relaxed.
+// The columns list[0 .. end) for one colour, a warp per column; the next column's table entry and
+// coefficients are loaded before the current column is relaxed.
 template <bool HAS_PROD, int LANES>
 __device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, const int2* list, int end, int colour,
                                               int warp, int nwarps, int lane) {
     int q = warp;
     if (q >= end) return;
-    int2 c = list[q];
+    int2 c;
+    int4 e;
     float du[LANES];
-    load_coeff<LANES>(w, c, colour, lane, du);
+    load_column<LANES>(w, list, q, colour, lane, c, e, du);
     while (true) {
         const int qn = q + nwarps;
         const bool more = qn < end;
         int2 cn = c;
+        int4 en = e;
         float dn[LANES];
-        if (more) {
-            cn = list[qn];
-            load_coeff<LANES>(w, cn, colour, lane, dn);
-        }
-        relax_column<HAS_PROD, LANES>(a, w, c, colour, lane, du);
+        if (more) load_column<LANES>(w, list, qn, colour, lane, cn, en, dn);
+        relax_column<HAS_PROD, LANES>(a, w, c, e, lane, du);
         if (!more) break;
         c = cn;
+        e = en;
 #pragma unroll
         for (int r = 0; r < LANES; ++r) du[r] = dn[r];
         q = qn;
     }
+}
+
+// Max-norm residual |r| / max(6 u, reference) of the nodes relax_nodes would update, with
+// r = nb + h prod - (6 + h c) u (field_kernels.py:215-243), as float bits (all values are >= 0).
+template <bool HAS_PROD, bool ZCLAMP, int LANES>
+__device__ __forceinline__ unsigned int residual_nodes(const SorArgs& a, const Sweep& w, const float* po,
+                                                       const float* pv, int lane, int kp, int last, int64_t gbase,
+                                                       const float (&du)[LANES]) {
+    const float* pim = po - w.si;
+    const float* pip = po + w.si;
+    const float* pjm = po - w.M;
+    const float* pjp = po + w.M;
+    unsigned int bits = 0u;
+#pragma unroll
+    for (int r = 0; r < LANES; ++r) {
+        const int off = 32 * r;
+        const bool active = du[r] >= 0.0f;
+        const float o = po[off];
+        const float b1 = w.K + o;
+        float cc = div_rn_fast(du[r], b1);
+        float prod = 0.0f;
+        if (HAS_PROD) {
+            if (active) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+        }
+        float vlo, vhi;
+        if (ZCLAMP) {
+            const int m = lane + off;
+            vlo = pv[max(m + kp - 1, 0)];
+            vhi = pv[min(m + kp, last)];
+        } else {
+            vlo = pv[off];
+            vhi = pv[off + 1];
+        }
+        const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
+        float res = nb + w.h * prod - (6.0f + w.h * cc) * o;
+        const float den = fmaxf(6.0f * o, a.p.reference);
+        float val = div_rn_fast(fabsf(res), den);
+        if (active && !(div_fast_range(du[r], b1) && div_fast_range(fabsf(res), den))) {
+            cc = __fdiv_rn(du[r], b1);
+            res = nb + w.h * prod - (6.0f + w.h * cc) * o;
+            val = __fdiv_rn(fabsf(res), den);
+        }
+        if (active) bits = max(bits, __float_as_uint(val));
+    }
+    return bits;
+}
+
+// Residual bits of one column's `colour` nodes.
+template <bool HAS_PROD, int LANES>
+__device__ __forceinline__ unsigned int residual_column(const SorArgs& a, const Sweep& w, const int2* list, int q,
+                                                        int colour, int lane) {
+    int2 c;
+    int4 e;
+    float du[LANES];
+    load_column<LANES>(w, list, q, colour, lane, c, e, du);
+    const int kp = e.w & 1;
+    const int last = e.w >> 11;
+    const float* po = w.s + e.x + lane;
+    const float* oth = w.s + e.y;
+    int64_t gbase = 0;
+    if (HAS_PROD) gbase = (c.y >> 16) * w.sx + static_cast<int64_t>(c.y & 0xffff) * w.nz;
+    if (w.zclamp) return residual_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, du);
+    return residual_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
 }
 
 // Waits until every listed CTA has signalled `epoch`; false when aborted (timeout here or elsewhere).
@@ -264,36 +355,49 @@ __device__ __forceinline__ bool wait_for(SorControl* ctl, const unsigned int* fl
 }
 
 // Copies one parity (the one colour `colour` updates in each column) or both parities of the
-// listed columns between the exchange buffer and shared memory. All of a column's entries are
-// loaded before any is stored, so a warp has the whole column in flight at once.
+// listed columns between the exchange buffer and shared memory. A warp moves two column parities
+// at a time and loads all of their entries before storing any, so two whole columns are in flight.
 template <int LANES>
 __device__ __forceinline__ void copy_columns(const Sweep& w, const int2* list, int n, float* xb, int colour,
                                              bool both, bool to_xchg, int warp, int nwarps, int lane) {
-    for (int q = warp; q < n; q += nwarps) {
-        const int2 c = list[q];
-        const int gi = c.y >> 16, gj = c.y & 0xffff;
-        for (int par = 0; par < 2; ++par) {
-            if (!both && par != ((colour + gi + gj) & 1)) continue;
-            const int cnt = par ? w.cnt_odd : w.cnt_even;
-            float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
-            float* sm = w.s + par * w.ncm + c.x * w.M + lane;
-            float v[LANES];
-            if (to_xchg) {
+    const int per = both ? 2 : 1;
+    const int items = n * per;
+    for (int t0 = warp; t0 < items; t0 += 2 * nwarps) {
+        float* src[2];
+        float* dst[2];
+        int cnt[2];
 #pragma unroll
-                for (int r = 0; r < LANES; ++r)
-                    if (lane + 32 * r < cnt) v[r] = sm[32 * r];
-#pragma unroll
-                for (int r = 0; r < LANES; ++r)
-                    if (lane + 32 * r < cnt) __stcg(x + 32 * r, v[r]);
-            } else {
-#pragma unroll
-                for (int r = 0; r < LANES; ++r)
-                    if (lane + 32 * r < cnt) v[r] = __ldcg(x + 32 * r);
-#pragma unroll
-                for (int r = 0; r < LANES; ++r)
-                    if (lane + 32 * r < cnt) sm[32 * r] = v[r];
+        for (int u = 0; u < 2; ++u) {
+            const int t = t0 + u * nwarps;
+            cnt[u] = 0;
+            src[u] = dst[u] = nullptr;
+            if (t < items) {
+                const int2 c = list[both ? (t >> 1) : t];
+                const int gi = c.y >> 16, gj = c.y & 0xffff;
+                const int par = both ? (t & 1) : ((colour + gi + gj) & 1);
+                cnt[u] = par ? w.cnt_odd : w.cnt_even;
+                float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
+                float* sm = w.s + par * w.ncm + c.x * w.M + lane;
+                src[u] = to_xchg ? sm : x;
+                dst[u] = to_xchg ? x : sm;
             }
         }
+        float v[2][LANES];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int r = 0; r < LANES; ++r)
+                if (lane + 32 * r < cnt[u]) v[u][r] = to_xchg ? src[u][32 * r] : __ldcg(src[u] + 32 * r);
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int r = 0; r < LANES; ++r)
+                if (lane + 32 * r < cnt[u]) {
+                    if (to_xchg)
+                        __stcg(dst[u] + 32 * r, v[u][r]);
+                    else
+                        dst[u][32 * r] = v[u][r];
+                }
     }
 }
 
@@ -315,8 +419,8 @@ __device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list,
     }
 }
 
-// Columns longer than 4 x 32 entries per parity run 16 warps per CTA (128 registers a thread).
-constexpr int max_threads_for_lanes(int lanes) { return lanes > 4 ? 512 : 1024; }
+// Columns longer than 3 x 32 entries per parity run 16 warps per CTA (128 registers a thread).
+constexpr int max_threads_for_lanes(int lanes) { return lanes > 3 ? 512 : 1024; }
 
 template <bool HAS_PROD, int LANES, int H>
 __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
@@ -348,6 +452,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     w.omega = a.p.omega;
     w.one_minus_omega = 1.0f - a.p.omega;
     w.zclamp = a.p.bc_z != 0;
+    w.tab = reinterpret_cast<const int4*>(reinterpret_cast<char*>(s) + a.t.table_offset);
     __shared__ int s_neighbours[8];
     __shared__ int s_n_neighbours;
     if (threadIdx.x == 0) {
@@ -408,7 +513,12 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
         if (inside) {
             const int2 c = make_int2(box, (gi << 16) | gj);
-            if (d < H) L.upd[atomicAdd(&s_counts[d], 1)] = c;
+            if (d < H) {
+                L.upd[atomicAdd(&s_counts[d], 1)] = c;
+                int4* tab = const_cast<int4*>(w.tab);
+                tab[2 * box] = column_entry(w, box, gi, gj, 0);
+                tab[2 * box + 1] = column_entry(w, box, gi, gj, 1);
+            }
             if (d >= 1) L.pull[atomicAdd(&s_counts[8], 1)] = c;
             if (d == 0) {
                 if (li < H || li >= ai - H || lj < H || lj >= aj - H)
@@ -462,7 +572,6 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     // The ring columns' coefficients are written by their owners: one global barrier first.
     bool ok = grid_barrier(a.ctl, a.flags, epoch);
 
-    const float K = w.K, h = w.h;
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
     bool converged = false;
@@ -530,29 +639,8 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         unsigned int bits = 0u;
         const int n_owned = L.upd_end[0];
         for (int q = warp; q < n_owned; q += nwarps) {
-            const int2 c = L.upd[q];
-            const int gi = c.y >> 16, gj = c.y & 0xffff;
-            for (int kp = 0; kp < 2; ++kp) {
-                const int own = kp * w.ncm + c.x * M;
-                const int oth = (kp ^ 1) * w.ncm + c.x * M;
-                const int cnt = kp ? w.cnt_odd : w.cnt_even;
-                const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
-                const float* crow = a.coeff + ((static_cast<int64_t>(kp) * nx + gi) * ny + gj) * M;
-                for (int m = lane; m < cnt; m += 32) {
-                    const float du = crow[m];
-                    if (!(du >= 0.0f)) continue;
-                    const int io = own + m;
-                    const float o = s[io];
-                    const float cc = div_rn(du, K + o);
-                    float prod = 0.0f;
-                    if (HAS_PROD) prod = prod_term(a, gi * w.sx + static_cast<int64_t>(gj) * nz + 2 * m + kp);
-                    const float nb = s[io - w.si] + s[io + w.si] + s[io - M] + s[io + M] +
-                                     s[oth + max(m + kp - 1, 0)] + s[oth + min(m + kp, last)];
-                    const float r = nb + h * prod - (6.0f + h * cc) * o;
-                    const float val = div_rn(fabsf(r), fmaxf(6.0f * o, a.p.reference));
-                    bits = max(bits, __float_as_uint(val));
-                }
-            }
+            bits = max(bits, residual_column<HAS_PROD, LANES>(a, w, L.upd, q, 0, lane));
+            bits = max(bits, residual_column<HAS_PROD, LANES>(a, w, L.upd, q, 1, lane));
         }
 #pragma unroll
         for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
@@ -655,10 +743,12 @@ static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t sm
     const int nbox = (ti + 2 * H) * (tj + 2 * H);
     const size_t planes = ((2ull * nbox * M * sizeof(float)) + 15) & ~15ull;
     const size_t lists = 5ull * nbox * sizeof(int2) + 16 * sizeof(int);
-    const size_t smem = planes + lists;
+    const size_t table = (planes + lists + 15) & ~15ull;
+    const size_t smem = table + 2ull * nbox * sizeof(int4);
     if (smem > smem_limit) return false;
+    if (2ll * p.nx * p.ny * M >= (1ll << 31)) return false;  // coefficient offsets are 32-bit
     const int warps = std::min(max_threads_for_lanes((M + 31) / 32) / 32, std::max(1, ti * tj));
-    *out = SorTiling{ex, ey, ti, tj, M, 32 * warps, H, nbox, planes, smem};
+    *out = SorTiling{ex, ey, ti, tj, M, 32 * warps, H, nbox, planes, table, smem};
     return true;
 }
 
