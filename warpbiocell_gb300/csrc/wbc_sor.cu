@@ -50,7 +50,8 @@ constexpr int kMaxCtas = 1024;  // barrier flags that follow the control block
 struct SorTiling {
     int tx, ty;  // CTAs along i and j
     int ti, tj;  // tile extent (columns) along i and j
-    int M;       // (nz + 1) / 2 entries per parity per column
+    int M;       // column stride per parity: (nz + 1) / 2 entries rounded up to 4 (16-byte rows)
+    int lanes;   // 32-entry chunks per parity column
     int threads;
     int H;       // halo depth = half-sweeps between exchanges
     int nbox;    // columns of the bounding box (ti + 2H) * (tj + 2H)
@@ -87,6 +88,22 @@ __device__ __forceinline__ unsigned int load_acquire(const unsigned int* p) {
 
 __device__ __forceinline__ void store_release(unsigned int* p, unsigned int v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// ---- halo exchange with tagged words (H = 1) ------------------------------------------------------------
+// Each exchanged entry is one 64-bit word {value bits, tag} written with a single relaxed store, so a
+// reader that sees the tag of the half-sweep it needs also sees that half-sweep's value: no flag,
+// fence or barrier between neighbouring tiles. The buffer has the layout of the coefficient copy
+// ([parity][nx][ny][M]) in 8-byte words.
+__device__ __forceinline__ void store_tagged(unsigned long long* p, float v, unsigned int tag) {
+    const unsigned long long word = (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(word) : "memory");
+}
+
+__device__ __forceinline__ unsigned long long load_tagged(const unsigned long long* p) {
+    unsigned long long word;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(word) : "l"(p) : "memory");
+    return word;
 }
 
 __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n - 1 ? n - 2 : i); }
@@ -145,6 +162,7 @@ struct Sweep {
     float* s;
     const int4* tab;
     const float* coeff;
+    float* xchg;  // exchange buffer, laid out like the coefficient scratch copy
     int ncm, M, si, nx, ny, nz, cnt_even, cnt_odd;
     int64_t sx;
     float K, h, omega, one_minus_omega;
@@ -184,7 +202,8 @@ __device__ __forceinline__ void load_column(const Sweep& w, const int2* list, in
 // IEEE division replaces the fast one only where an operand is outside its range.
 template <bool HAS_PROD, bool ZCLAMP, int LANES>
 __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
-                                            int kp, int last, int64_t gbase, const float (&du)[LANES]) {
+                                            int kp, int last, int64_t gbase, unsigned long long* xrow, int cnt,
+                                            unsigned int tag, const float (&du)[LANES]) {
     const float* pim = po - w.si;
     const float* pip = po + w.si;
     const float* pjm = po - w.M;
@@ -218,7 +237,10 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
             b2 = 6.0f + w.h * cc;
             gs = __fdiv_rn(a2, b2);
         }
-        if (active) po[off] = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
+        const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
+        if (active) po[off] = v;
+        // An edge column publishes every entry (unchanged ones too) with this half-sweep's tag.
+        if (xrow && lane + off < cnt) store_tagged(xrow + off, active ? v : o, tag);
     }
 }
 
@@ -226,24 +248,28 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
 // Michaelis-Menten uptake linearised at the old value, over-relaxed and clamped at zero.
 template <bool HAS_PROD, int LANES>
 __device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, int2 c, int4 e, int lane,
-                                             const float (&du)[LANES]) {
+                                             unsigned int tag, const float (&du)[LANES]) {
     const int kp = e.w & 1;
     const int last = e.w >> 11;
     float* po = w.s + e.x + lane;
     const float* oth = w.s + e.y;
     int64_t gbase = 0;
     if (HAS_PROD) gbase = (c.y >> 16) * w.sx + static_cast<int64_t>(c.y & 0xffff) * w.nz;
+    unsigned long long* xrow = tag ? reinterpret_cast<unsigned long long*>(w.xchg) + e.z + lane : nullptr;
+    const int cnt = (e.w >> 1) & 1023;
     if (w.zclamp)
-        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, du);
+        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, xrow, cnt, tag, du);
     else
-        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
+        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, xrow, cnt, tag,
+                                            du);
 }
 
 // The columns list[0 .. end) for one colour, a warp per column; the next column's table entry and
-// coefficients are loaded before the current column is relaxed.
+// coefficients are loaded before the current column is relaxed. A nonzero `tag` also publishes
+// the columns to the exchange buffer.
 template <bool HAS_PROD, int LANES>
 __device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, const int2* list, int end, int colour,
-                                              int warp, int nwarps, int lane) {
+                                              int warp, int nwarps, int lane, unsigned int tag = 0u) {
     int q = warp;
     if (q >= end) return;
     int2 c;
@@ -257,7 +283,7 @@ __device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, 
         int4 en = e;
         float dn[LANES];
         if (more) load_column<LANES>(w, list, qn, colour, lane, cn, en, dn);
-        relax_column<HAS_PROD, LANES>(a, w, c, e, lane, du);
+        relax_column<HAS_PROD, LANES>(a, w, c, e, lane, tag, du);
         if (!more) break;
         c = cn;
         e = en;
@@ -330,28 +356,56 @@ __device__ __forceinline__ unsigned int residual_column(const SorArgs& a, const 
     return residual_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
 }
 
-// Waits until every listed CTA has signalled `epoch`; false when aborted (timeout here or elsewhere).
-__device__ __forceinline__ bool wait_for(SorControl* ctl, const unsigned int* flags, unsigned int epoch,
-                                         const int* who, int n) {
-    int aborted = 0;
-    if (static_cast<int>(threadIdx.x) < n) {
-        const unsigned int* f = flags + who[threadIdx.x];
-        unsigned polls = 0;
-        while (static_cast<int>(load_acquire(f) - epoch) < 0) {
-            if ((++polls & 255u) == 0u) {
-                if (load_acquire(&ctl->abort) != 0u) {
-                    aborted = 1;
-                    break;
-                }
-                if (polls > kBarrierPolls) {
-                    atomicExch(&ctl->abort, 1u);
-                    aborted = 1;
-                    break;
-                }
+// Reads the parity `colour` updated in each listed halo column once every entry carries `tag`
+// (two columns per warp at a time, all of their words in flight before any is checked) and stores
+// the values in shared memory. Returns false when a wait timed out or another CTA aborted.
+template <int LANES>
+__device__ __forceinline__ bool pull_tagged(const Sweep& w, const int2* list, int n, int colour, unsigned int tag,
+                                            const SorControl* ctl, int warp, int nwarps, int lane) {
+    const unsigned long long* ll = reinterpret_cast<const unsigned long long*>(w.xchg);
+    bool fine = true;
+    for (int q0 = warp; q0 < n; q0 += 2 * nwarps) {
+        const unsigned long long* src[2];
+        float* dst[2];
+        int cnt[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int q = q0 + u * nwarps;
+            cnt[u] = 0;
+            src[u] = nullptr;
+            dst[u] = nullptr;
+            if (q < n) {
+                const int2 c = list[q];
+                const int gi = c.y >> 16, gj = c.y & 0xffff;
+                const int par = (colour + gi + gj) & 1;
+                cnt[u] = par ? w.cnt_odd : w.cnt_even;
+                src[u] = ll + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
+                dst[u] = w.s + par * w.ncm + c.x * w.M + lane;
             }
         }
+        unsigned long long v[2][LANES];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int r = 0; r < LANES; ++r)
+                if (lane + 32 * r < cnt[u]) v[u][r] = load_tagged(src[u] + 32 * r);
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int r = 0; r < LANES; ++r)
+                if (lane + 32 * r < cnt[u]) {
+                    unsigned polls = 0;
+                    while (static_cast<unsigned int>(v[u][r] >> 32) != tag) {
+                        if ((++polls & 255u) == 0u && (polls > kBarrierPolls || load_acquire(&ctl->abort) != 0u)) {
+                            fine = false;
+                            break;
+                        }
+                        v[u][r] = load_tagged(src[u] + 32 * r);
+                    }
+                    dst[u][32 * r] = __uint_as_float(static_cast<unsigned int>(v[u][r]));
+                }
     }
-    return __syncthreads_or(aborted) == 0;
+    return fine;
 }
 
 // Copies one parity (the one colour `colour` updates in each column) or both parities of the
@@ -424,7 +478,7 @@ constexpr int max_threads_for_lanes(int lanes) { return lanes > 3 ? 512 : 1024; 
 
 template <bool HAS_PROD, int LANES, int H>
 __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
-    extern __shared__ float s[];
+    extern __shared__ __align__(128) float s[];
     __shared__ unsigned int s_red[32];
     __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
@@ -453,6 +507,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     w.one_minus_omega = 1.0f - a.p.omega;
     w.zclamp = a.p.bc_z != 0;
     w.tab = reinterpret_cast<const int4*>(reinterpret_cast<char*>(s) + a.t.table_offset);
+    w.xchg = a.xchg;
     __shared__ int s_neighbours[8];
     __shared__ int s_n_neighbours;
     if (threadIdx.x == 0) {
@@ -569,7 +624,24 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         }
     }
     unsigned int epoch = 0;
-    // The ring columns' coefficients are written by their owners: one global barrier first.
+    if (H == 1) {
+        // The edge rows start with tag 0 (half-sweeps are tagged from 1), so words a previous solve
+        // left in the buffer are never taken for this solve's.
+        __syncthreads();
+        unsigned long long* ll = reinterpret_cast<unsigned long long*>(a.xchg);
+        for (int q = warp; q < L.n_publish; q += nwarps) {
+            const int2 c = L.publish[q];
+            const int gi = c.y >> 16, gj = c.y & 0xffff;
+            for (int par = 0; par < 2; ++par) {
+                const int cnt = par ? w.cnt_odd : w.cnt_even;
+                for (int m = lane; m < cnt; m += 32)
+                    store_tagged(ll + ((static_cast<int64_t>(par) * nx + gi) * ny + gj) * M + m,
+                                 s[par * w.ncm + c.x * M + m], 0u);
+            }
+        }
+    }
+    // The ring columns' coefficients (and edge rows) are written by their owners: one global
+    // barrier first.
     bool ok = grid_barrier(a.ctl, a.flags, epoch);
 
     int sweeps = 0;
@@ -577,27 +649,25 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     bool converged = false;
     int chunk_index = 0;
     unsigned int interval = 0;
-    const int signal_thread = blockDim.x - 32;  // lane 0 of the last warp, which has the fewest inner columns
     while (ok && sweeps < a.max_sweeps) {
         const int chunk = min(a.check_every, a.max_sweeps - sweeps);
         int half_left = 2 * chunk;
         int colour = 0;
         while (ok && half_left > 0) {
             if constexpr (H == 1) {
-                // Edge columns first, published while the inner columns are relaxed; the parity
-                // split of the exchange buffer keeps a colour's entries until the neighbour has
-                // signalled the next colour, which follows its pull.
-                relax_columns<HAS_PROD, LANES>(a, w, L.publish, L.n_publish, colour, warp, nwarps, lane);
-                __syncthreads();
-                copy_columns<LANES>(w, L.publish, L.n_publish, a.xchg, colour, false, true, warp, nwarps, lane);
-                __syncthreads();
-                epoch += 1;
-                if (static_cast<int>(threadIdx.x) == signal_thread) store_release(a.flags + blockIdx.x, epoch);
+                // Edge columns first, each new value also stored to the exchange buffer tagged
+                // with this half-sweep; then the inner columns; then the halo is read from the
+                // neighbours' tagged words. A neighbour rewrites a word two half-sweeps later, which
+                // needs this tile's words of the half-sweep in between, written after this pull.
+                const unsigned int tag = static_cast<unsigned int>(2 * sweeps + (2 * chunk - half_left) + 1);
+                relax_columns<HAS_PROD, LANES>(a, w, L.publish, L.n_publish, colour, warp, nwarps, lane, tag);
                 relax_columns<HAS_PROD, LANES>(a, w, L.inner, L.n_inner, colour, warp, nwarps, lane);
-                ok = wait_for(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
-                if (!ok) break;
-                copy_columns<LANES>(w, L.pull, L.n_pull, a.xchg, colour, false, false, warp, nwarps, lane);
-                __syncthreads();
+                const bool fine = pull_tagged<LANES>(w, L.pull, L.n_pull, colour, tag, a.ctl, warp, nwarps, lane);
+                if (__syncthreads_or(!fine)) {
+                    if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
+                    ok = false;
+                    break;
+                }
                 if (L.n_mir > 0) {
                     mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
                     __syncthreads();
@@ -635,6 +705,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         }
         if (!ok) break;
         sweeps += chunk;
+        __syncthreads();  // the halo warp may be ahead of the relaxing warps
         // Max-norm residual of the current field over every updated node (both colours).
         unsigned int bits = 0u;
         const int n_owned = L.upd_end[0];
@@ -736,7 +807,9 @@ static DeviceInfo device_info() {
 }
 
 static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t smem_limit, SorTiling* out) {
-    const int M = (p.nz + 1) / 2;
+    const int entries = (p.nz + 1) / 2;
+    const int M = (entries + 3) & ~3;
+    const int lanes = (entries + 31) / 32;
     const int ti = (p.nx + tx - 1) / tx, tj = (p.ny + ty - 1) / ty;
     if (ti < H || tj < H || ti < 2 || tj < 2) return false;
     const int ex = (p.nx + ti - 1) / ti, ey = (p.ny + tj - 1) / tj;
@@ -747,8 +820,8 @@ static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t sm
     const size_t smem = table + 2ull * nbox * sizeof(int4);
     if (smem > smem_limit) return false;
     if (2ll * p.nx * p.ny * M >= (1ll << 31)) return false;  // coefficient offsets are 32-bit
-    const int warps = std::min(max_threads_for_lanes((M + 31) / 32) / 32, std::max(1, ti * tj));
-    *out = SorTiling{ex, ey, ti, tj, M, 32 * warps, H, nbox, planes, table, smem};
+    const int warps = std::min(max_threads_for_lanes(lanes) / 32, std::max(1, ti * tj));
+    *out = SorTiling{ex, ey, ti, tj, M, lanes, 32 * warps, H, nbox, planes, table, smem};
     return true;
 }
 
@@ -756,8 +829,8 @@ static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t sm
 // the largest tile, then the halo perimeter.
 static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, int H, int want_tx, int want_ty,
                           SorTiling* out) {
-    const int M = (p.nz + 1) / 2;
-    if (M > 32 * kMaxLanesPerColumn || p.nx > 32767 || p.ny > 32767) return false;
+    const int entries = (p.nz + 1) / 2;
+    if (entries > 32 * kMaxLanesPerColumn || p.nx > 32767 || p.ny > 32767) return false;
     const int max_ctas = std::min(sms, kMaxCtas);
     if (want_tx > 0 && want_ty > 0) return want_tx * want_ty <= max_ctas && tiling_for(p, want_tx, want_ty, H, smem_limit, out);
     bool found = false;
@@ -779,7 +852,7 @@ static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, i
 }
 
 static size_t plane_bytes(const wbc_sor_params& p) {
-    return 2ull * p.nx * p.ny * ((p.nz + 1) / 2) * sizeof(float);
+    return 2ull * p.nx * p.ny * ((((p.nz + 1) / 2) + 3) & ~3) * sizeof(float);
 }
 
 static size_t header_bytes() { return sizeof(SorControl) + kMaxCtas * sizeof(unsigned int); }
@@ -829,7 +902,7 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     }
     if (!*feasible) return WBC_OK;
     const bool has_prod = production != nullptr || p.has_source;
-    KernelFn fn = kernel_for(has_prod, (t.M + 31) / 32, t.H);
+    KernelFn fn = kernel_for(has_prod, t.lanes, t.H);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem));
     if (err != cudaSuccess) {
@@ -928,6 +1001,10 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
         !workspace || !best || (p->has_source && !source))
         return WBC_ERR_INVALID;
     if (workspace_bytes < sor_workspace_bytes(*p)) return WBC_ERR_WORKSPACE;
+    if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0) {
+        set_error_msg("wbc_sor_autotune: the workspace must be 16-byte aligned");
+        return WBC_ERR_INVALID;
+    }
     *best = wbc_sor_tuning{0, 0, 0};
     if (best_us_per_sweep) *best_us_per_sweep = 0.0f;
     const DeviceInfo dev = device_info();
@@ -996,6 +1073,10 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
         !report || !workspace || (p->has_source && !source) || path < 0 || path > 2)
         return WBC_ERR_INVALID;
     if (workspace_bytes < sor_workspace_bytes(*p)) return WBC_ERR_WORKSPACE;
+    if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0) {
+        set_error_msg("wbc_sor_solve: the workspace must be 16-byte aligned");
+        return WBC_ERR_INVALID;
+    }
     cudaStream_t s = as_stream(stream);
     bool feasible = false;
     if (path != 1) {
