@@ -189,6 +189,38 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
                      const float* production, const float* source, const float* field, float* scratch_field,
                      void* workspace, size_t workspace_bytes, wbc_sor_tuning* best, float* best_us_per_sweep,
                      void* stream);
+/* ---- batched solves: many grids in one persistent launch -------------------------------------------
+ * Each item is one wbc_sor_solve (resident path, halo depth 1) with its own grid, coefficients,
+ * field and workspace. The items' tiles form one work list; a CTA takes the next tile and runs it
+ * until that item's solve ends, so small and large grids share the GPU in one launch, and each
+ * item stops at its own sweep count, residual and stopping rule, with the same field bits as its
+ * own wbc_sor_solve. No counterpart in the reference. */
+typedef struct wbc_sor_batch_item {
+    wbc_sor_params params;
+    const int32_t* fixed;         /* may be NULL                                                    */
+    const float* density;
+    const float* production;      /* may be NULL                                                    */
+    const float* source;          /* required when params.has_source                                */
+    float* field;
+    void* workspace;              /* wbc_sor_solve_workspace_bytes(&params) bytes, 16-byte aligned  */
+} wbc_sor_batch_item;
+
+typedef struct wbc_sor_batch {    /* filled by wbc_sor_batch_prepare                                */
+    int32_t items, total_tiles, ctas, threads, lanes, has_prod;
+    int64_t smem_bytes;
+    void* device_plan;
+} wbc_sor_batch;
+
+size_t wbc_sor_batch_plan_bytes(int32_t n);
+/* Tiles every item (CTAs in proportion to its nodes), copies the work list into `plan` (device
+ * memory) and fills `out`. Synchronises `stream`; not for use during stream capture. */
+int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t check_every, int32_t max_sweeps,
+                          double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out, void* stream);
+/* Solves every item from its field's current values; nothing is read back (capturable). */
+int wbc_sor_batch_solve(const wbc_sor_batch* b, void* stream);
+/* The items' reports (host array of b->items); synchronises. WBC_ERR_TIMEOUT if a solve timed out. */
+int wbc_sor_batch_reports(const wbc_sor_batch* b, wbc_sor_report* reports, void* stream);
+
 /* Explicit FTCS step field_out = field_in + dt (D lap - uptake + production) (validation only;
  * kernels/field_kernels.py:246-273). `p->dx2_over_D` carries D/dx^2 here. */
 int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const float* density,
@@ -285,6 +317,71 @@ int wbc_network_inherit(int32_t count_before, int32_t n_words, const int32_t* di
 /* counts[k] += (living) cells with node nodes[k] ON (kernels/network_kernels.py:287-302). */
 int wbc_network_count_on(int32_t n, int32_t n_words, int32_t n_query, const int32_t* nodes, int32_t living_only,
                          const int32_t* cell_state, const uint64_t* states, int32_t* counts, void* stream);
+
+/* ---- batches: many independent spheroids advanced together ------------------------------------
+ * One instance = one population with its hash grid and oxygen grid, described by device pointers
+ * into arrays the caller owns (the same arrays the single-population calls take). Every batched
+ * call launches one kernel per stage for all instances over a static work list and reads each
+ * instance's cell count from counts[instance] in device memory; no call reads anything back to
+ * the host, so a whole step can be captured in a CUDA graph. Each instance's results are
+ * bit-identical to the single-population calls on it. No counterpart in the reference, whose
+ * parameter sweep runs its experiments one after another (simulation/sweep.py:132-139). */
+typedef struct wbc_batch_instance {
+    int32_t capacity;
+    float* position;              /* float[capacity][3]                                             */
+    float* radius;
+    int32_t* cell_state;
+    int32_t* cell_type;
+    float* age;
+    float* oxygen_local;
+    float* glucose_local;
+    uint32_t* rng_state;
+    float* velocity;              /* float[capacity][3]                                             */
+    int32_t* neighbor_count;
+    int32_t* divide_flag;
+    int32_t* division_offset;
+    int32_t* fate_flags;
+    wbc_neighbor_grid grid;       /* this instance's hash grid (scan_partials unused)               */
+    float query_radius;           /* contact: ContactParams.query_radius                            */
+    float contact_rate;           /* stiffness / damping                                            */
+    float contact_dt;             /* dt_mechanics                                                    */
+    int32_t contact_substeps;
+    wbc_grid_geometry geom;       /* the oxygen grid                                                 */
+    int64_t* accumulator;         /* int64[4][nodes], cleared by wbc_batch_deposit after reading it  */
+    float* density;               /* float[4][nodes] per-state densities, or NULL                    */
+    float* uptake_density;        /* the solver's combined uptake density, float[nodes]              */
+    float uptake_weights[4];
+    float inv_voxel_volume;
+    float* field;                 /* oxygen values sampled into oxygen_local                         */
+    wbc_lifecycle_params lifecycle;
+    float placement_factor;
+} wbc_batch_instance;
+
+typedef struct wbc_batch {        /* filled by wbc_batch_prepare                                     */
+    int32_t instances;
+    void* device_plan;
+    int32_t cell_chunks, node_chunks, bucket_tiles, slot_tiles;
+    int32_t max_substeps;
+} wbc_batch;
+
+/* Device bytes of the plan for these instances (0 if the description is too large). */
+size_t wbc_batch_plan_bytes(int32_t n, const wbc_batch_instance* insts);
+/* Copies the descriptions and the work lists into `plan` (device memory) and fills `out`.
+ * Synchronises `stream`; not for use during stream capture. */
+int wbc_batch_prepare(int32_t n, const wbc_batch_instance* insts, void* plan, size_t plan_bytes, wbc_batch* out,
+                      void* stream);
+/* wbc_grid_build for every instance. */
+int wbc_batch_grid_build(const wbc_batch* b, const int32_t* counts, void* stream);
+/* wbc_contact_substep for every instance (one substep). */
+int wbc_batch_contact(const wbc_batch* b, const int32_t* counts, void* stream);
+/* wbc_deposit then wbc_density_convert (clearing the accumulator) for every instance. */
+int wbc_batch_deposit(const wbc_batch* b, const int32_t* counts, void* stream);
+/* wbc_sample of `field` into oxygen_local for every instance. */
+int wbc_batch_sample(const wbc_batch* b, const int32_t* counts, void* stream);
+/* wbc_lifecycle_decide, wbc_division_scan and wbc_place_daughters for every instance, then
+ * counts[i] += daughters. An instance whose daughters would exceed its capacity places none,
+ * keeps its count and gets status[i] = WBC_ERR_CAPACITY (status may be NULL). */
+int wbc_batch_lifecycle(const wbc_batch* b, int32_t* counts, int32_t* status, void* stream);
 
 #ifdef __cplusplus
 }

@@ -113,6 +113,76 @@ class LifecycleParamsC(ctypes.Structure):
     ]
 
 
+class BatchInstanceC(ctypes.Structure):
+    _fields_ = [
+        ("capacity", c_int32),
+        ("position", c_void_p),
+        ("radius", c_void_p),
+        ("cell_state", c_void_p),
+        ("cell_type", c_void_p),
+        ("age", c_void_p),
+        ("oxygen_local", c_void_p),
+        ("glucose_local", c_void_p),
+        ("rng_state", c_void_p),
+        ("velocity", c_void_p),
+        ("neighbor_count", c_void_p),
+        ("divide_flag", c_void_p),
+        ("division_offset", c_void_p),
+        ("fate_flags", c_void_p),
+        ("grid", NeighborGridC),
+        ("query_radius", c_float),
+        ("contact_rate", c_float),
+        ("contact_dt", c_float),
+        ("contact_substeps", c_int32),
+        ("geom", GridGeometryC),
+        ("accumulator", c_void_p),
+        ("density", c_void_p),
+        ("uptake_density", c_void_p),
+        ("uptake_weights", c_float * 4),
+        ("inv_voxel_volume", c_float),
+        ("field", c_void_p),
+        ("lifecycle", LifecycleParamsC),
+        ("placement_factor", c_float),
+    ]
+
+
+class BatchC(ctypes.Structure):
+    _fields_ = [
+        ("instances", c_int32),
+        ("device_plan", c_void_p),
+        ("cell_chunks", c_int32),
+        ("node_chunks", c_int32),
+        ("bucket_tiles", c_int32),
+        ("slot_tiles", c_int32),
+        ("max_substeps", c_int32),
+    ]
+
+
+class SorBatchItemC(ctypes.Structure):
+    _fields_ = [
+        ("params", SorParamsC),
+        ("fixed", c_void_p),
+        ("density", c_void_p),
+        ("production", c_void_p),
+        ("source", c_void_p),
+        ("field", c_void_p),
+        ("workspace", c_void_p),
+    ]
+
+
+class SorBatchC(ctypes.Structure):
+    _fields_ = [
+        ("items", c_int32),
+        ("total_tiles", c_int32),
+        ("ctas", c_int32),
+        ("threads", c_int32),
+        ("lanes", c_int32),
+        ("has_prod", c_int32),
+        ("smem_bytes", c_int64),
+        ("device_plan", c_void_p),
+    ]
+
+
 class NetworkProgramC(ctypes.Structure):
     _fields_ = [
         ("n_nodes", c_int32),
@@ -156,6 +226,18 @@ SIGNATURES: dict[str, list] = {
                       c_size_t, _I, POINTER(SorTuningC), _P],
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
                          POINTER(c_float), _P],
+    "wbc_sor_batch_plan_bytes": [_I],
+    "wbc_sor_batch_prepare": [_I, POINTER(SorBatchItemC), _I, _I, ctypes.c_double, _P, c_size_t, POINTER(SorBatchC),
+                              _P],
+    "wbc_sor_batch_solve": [POINTER(SorBatchC), _P],
+    "wbc_sor_batch_reports": [POINTER(SorBatchC), POINTER(SorReportC), _P],
+    "wbc_batch_plan_bytes": [_I, POINTER(BatchInstanceC)],
+    "wbc_batch_prepare": [_I, POINTER(BatchInstanceC), _P, c_size_t, POINTER(BatchC), _P],
+    "wbc_batch_grid_build": [POINTER(BatchC), _P, _P],
+    "wbc_batch_contact": [POINTER(BatchC), _P, _P],
+    "wbc_batch_deposit": [POINTER(BatchC), _P, _P],
+    "wbc_batch_sample": [POINTER(BatchC), _P, _P],
+    "wbc_batch_lifecycle": [POINTER(BatchC), _P, _P, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
     "wbc_division_scan_noalloc": [_I, _P, _P, _P, _P],
@@ -171,7 +253,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_network_count_on": [_I, _I, _I, _P, _I, _P, _P, _P, _P],
 }
 _RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64,
-            "wbc_sor_solve_workspace_bytes": c_size_t}
+            "wbc_sor_solve_workspace_bytes": c_size_t, "wbc_sor_batch_plan_bytes": c_size_t,
+            "wbc_batch_plan_bytes": c_size_t}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

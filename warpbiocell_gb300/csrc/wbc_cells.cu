@@ -8,15 +8,9 @@
 // exp (wbc_expf), so the oracle reproduces every decision bit for bit.
 #include <mutex>
 
-#include "wbc_common.cuh"
+#include "wbc_bodies.cuh"
 
 namespace wbc {
-
-__device__ __forceinline__ float oxygen_factor(float o, float hypoxia_threshold, float death_threshold) {
-    if (o >= hypoxia_threshold) return 1.0f;
-    if (o <= death_threshold) return 0.0f;
-    return (o - death_threshold) / (hypoxia_threshold - death_threshold);
-}
 
 __global__ void k_lifecycle_decide(wbc_lifecycle_params p, int32_t n, int32_t* __restrict__ cell_state,
                                    float* __restrict__ age, const int32_t* __restrict__ neighbor_count,
@@ -24,52 +18,9 @@ __global__ void k_lifecycle_decide(wbc_lifecycle_params p, int32_t n, int32_t* _
                                    const int32_t* __restrict__ fate_flags, uint32_t* __restrict__ rng_state,
                                    int32_t* __restrict__ divide_flag) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    divide_flag[i] = 0;
-    if (cell_state[i] == WBC_STATE_DEAD) return;
-
-    age[i] = age[i] + p.dt;
-    uint32_t rng = rng_state[i];
-    const uint32_t inc = rng_increment(static_cast<uint32_t>(i));
-    const float o = oxygen_local[i];
-    const float g = glucose_local[i];
-    const int flags = p.phenotype_model == 1 ? fate_flags[i] : 0;
-
-    bool lethal = o < p.death_threshold;
-    if (p.necrosis_requires_glucose != 0) lethal = lethal && (g < p.glucose_death_threshold);
-    float rate = p.death_rate;
-    if (lethal) rate = fmaxf(p.death_rate, p.anoxic_death_rate);
-    if (flags & WBC_FATE_NECROSIS) rate = fmaxf(rate, p.necrosis_rate);
-    if (flags & WBC_FATE_APOPTOSIS) rate = fmaxf(rate, p.apoptosis_rate);
-    const float p_death = 1.0f - wbc_expf(-rate * p.dt);
-    if (randf(rng, inc) < p_death) {
-        cell_state[i] = WBC_STATE_DEAD;
-        rng_state[i] = rng;
-        return;
-    }
-
-    const bool crowded = neighbor_count[i] >= p.inhibition_threshold;
-    bool may_divide = !crowded;
-    float factor = 1.0f;
-    if (p.phenotype_model == 1) {
-        may_divide = may_divide && (flags & WBC_FATE_PROLIFERATION) != 0 && (flags & WBC_FATE_GROWTH_ARREST) == 0;
-    } else {
-        factor = oxygen_factor(o, p.hypoxia_threshold, p.death_threshold) *
-                 oxygen_factor(g, p.glucose_threshold, p.glucose_death_threshold);
-    }
-
-    if (o < p.hypoxia_threshold)
-        cell_state[i] = WBC_STATE_HYPOXIC;
-    else if (may_divide)
-        cell_state[i] = WBC_STATE_PROLIFERATIVE;
-    else
-        cell_state[i] = WBC_STATE_QUIESCENT;
-
-    if (may_divide) {
-        const float p_divide = 1.0f - wbc_expf(-p.division_rate * factor * p.dt);
-        if (randf(rng, inc) < p_divide) divide_flag[i] = 1;
-    }
-    rng_state[i] = rng;
+    if (i < n)
+        lifecycle_cell(p, i, cell_state, age, neighbor_count, oxygen_local, glucose_local, fate_flags, rng_state,
+                       divide_flag);
 }
 
 __global__ void k_place_daughters(int32_t count, float placement_factor, const int32_t* __restrict__ divide_flag,
@@ -81,36 +32,8 @@ __global__ void k_place_daughters(int32_t count, float placement_factor, const i
                                   int32_t* __restrict__ neighbor_count, int32_t* __restrict__ fate_flags) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count || divide_flag[i] == 0) return;
-    const int j = count + division_offset[i] - 1;
-
-    uint32_t rng = rng_state[i];
-    float dx, dy, dz;
-    unit_sphere(rng, rng_increment(static_cast<uint32_t>(i)), dx, dy, dz);
-    rng_state[i] = rng;
-
-    const float scale = 0.5f * placement_factor * radius[i];
-    const float hx = dx * scale, hy = dy * scale, hz = dz * scale;
-    const int64_t pi = 3 * static_cast<int64_t>(i), pj = 3 * static_cast<int64_t>(j);
-    const float x = position[pi], y = position[pi + 1], z = position[pi + 2];
-    position[pi] = x - hx;
-    position[pi + 1] = y - hy;
-    position[pi + 2] = z - hz;
-    position[pj] = x + hx;
-    position[pj + 1] = y + hy;
-    position[pj + 2] = z + hz;
-
-    radius[j] = radius[i];
-    cell_state[j] = cell_state[i];
-    cell_type[j] = cell_type[i];
-    age[j] = 0.0f;
-    oxygen_local[j] = oxygen_local[i];
-    glucose_local[j] = glucose_local[i];
-    velocity[pj] = 0.0f;
-    velocity[pj + 1] = 0.0f;
-    velocity[pj + 2] = 0.0f;
-    neighbor_count[j] = 0;
-    fate_flags[j] = fate_flags[i];
-    // rng_state[j] was set for every slot when the population was created and stays as it is.
+    place_daughter(i, count, placement_factor, division_offset, position, radius, cell_state, cell_type, age,
+                   oxygen_local, glucose_local, rng_state, velocity, neighbor_count, fate_flags);
 }
 
 __global__ void k_count_states(int32_t n, const int32_t* __restrict__ cell_state, int32_t* __restrict__ counts) {

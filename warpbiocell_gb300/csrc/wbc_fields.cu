@@ -12,63 +12,20 @@
 // Layout: fields are float[nx][ny][nz] with k fastest; the accumulator is int64[4][nodes].
 // Every float expression is evaluated in the reference's order (no contraction, see
 // wbc_common.cuh), so the field after a given number of sweeps is bit-identical to the oracle's.
-#include "wbc_common.cuh"
+#include "wbc_bodies.cuh"
 
 namespace wbc {
-
-constexpr float kFixedOne = 16777216.0f;  // 2^24
 
 __global__ void k_deposit(wbc_grid_geometry g, int32_t n, const float* __restrict__ position,
                           const int32_t* __restrict__ cell_state, unsigned long long* __restrict__ acc) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const int s = cell_state[c];
-    if (s < 0 || s >= 4) return;
-    const float* p = position + 3 * static_cast<int64_t>(c);
-    const float ux = (p[0] - g.origin_x) * g.inv_dx;
-    const float uy = (p[1] - g.origin_y) * g.inv_dx;
-    const float uz = (p[2] - g.origin_z) * g.inv_dx;
-    const int i0 = static_cast<int>(floorf(ux));
-    const int j0 = static_cast<int>(floorf(uy));
-    const int k0 = static_cast<int>(floorf(uz));
-    if (i0 < 0 || j0 < 0 || k0 < 0) return;
-    if (i0 + 1 >= g.nx || j0 + 1 >= g.ny || k0 + 1 >= g.nz) return;
-    const float fx = ux - static_cast<float>(i0);
-    const float fy = uy - static_cast<float>(j0);
-    const float fz = uz - static_cast<float>(k0);
-    const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
-    unsigned long long* layer = acc + s * nodes;
-#pragma unroll
-    for (int di = 0; di < 2; ++di) {
-        const float wx = di == 0 ? 1.0f - fx : fx;
-#pragma unroll
-        for (int dj = 0; dj < 2; ++dj) {
-            const float wy = dj == 0 ? 1.0f - fy : fy;
-#pragma unroll
-            for (int dk = 0; dk < 2; ++dk) {
-                const float wz = dk == 0 ? 1.0f - fz : fz;
-                const float w = wx * wy * wz;
-                const int q = static_cast<int>(w * kFixedOne + 0.5f);
-                const int64_t node = (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + (k0 + dk);
-                atomicAdd(layer + node, static_cast<unsigned long long>(static_cast<long long>(q)));
-            }
-        }
-    }
+    if (c < n) deposit_cell(g, c, position, cell_state, acc);
 }
 
 __global__ void k_convert(int64_t nodes, long long* __restrict__ acc, float inv_vol, float* __restrict__ density,
                           float w0, float w1, float w2, float w3, float* __restrict__ combined, int clear) {
     int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (node >= nodes) return;
-    float d[4];
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-        const long long a = acc[s * nodes + node];
-        d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
-        if (density) density[s * nodes + node] = d[s];
-        if (clear) acc[s * nodes + node] = 0;
-    }
-    if (combined) combined[node] = w0 * d[0] + w1 * d[1] + w2 * d[2] + w3 * d[3];
+    if (node < nodes) convert_node(nodes, node, acc, inv_vol, density, w0, w1, w2, w3, combined, clear);
 }
 
 __global__ void k_combine(int64_t nodes, float w0, float w1, float w2, float w3, const float* __restrict__ density,
@@ -82,30 +39,7 @@ __global__ void k_combine(int64_t nodes, float w0, float w1, float w2, float w3,
 __global__ void k_sample(wbc_grid_geometry g, const float* __restrict__ field, int32_t n,
                          const float* __restrict__ position, float* __restrict__ out) {
     int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const float* p = position + 3 * static_cast<int64_t>(c);
-    const float ux = (p[0] - g.origin_x) * g.inv_dx;
-    const float uy = (p[1] - g.origin_y) * g.inv_dx;
-    const float uz = (p[2] - g.origin_z) * g.inv_dx;
-    const float cx = fminf(fmaxf(ux, 0.0f), static_cast<float>(g.nx - 1));
-    const float cy = fminf(fmaxf(uy, 0.0f), static_cast<float>(g.ny - 1));
-    const float cz = fminf(fmaxf(uz, 0.0f), static_cast<float>(g.nz - 1));
-    const int i0 = min(static_cast<int>(floorf(cx)), g.nx - 2);
-    const int j0 = min(static_cast<int>(floorf(cy)), g.ny - 2);
-    const int k0 = min(static_cast<int>(floorf(cz)), g.nz - 2);
-    const float fx = cx - static_cast<float>(i0);
-    const float fy = cy - static_cast<float>(j0);
-    const float fz = cz - static_cast<float>(k0);
-    const int64_t sy = g.nz, sx = static_cast<int64_t>(g.ny) * g.nz;
-    const int64_t b = i0 * sx + j0 * sy + k0;
-    const float gx = 1.0f - fx;
-    const float c00 = field[b] * gx + field[b + sx] * fx;
-    const float c10 = field[b + sy] * gx + field[b + sx + sy] * fx;
-    const float c01 = field[b + 1] * gx + field[b + sx + 1] * fx;
-    const float c11 = field[b + sy + 1] * gx + field[b + sx + sy + 1] * fx;
-    const float c0 = c00 * (1.0f - fy) + c10 * fy;
-    const float c1 = c01 * (1.0f - fy) + c11 * fy;
-    out[c] = c0 * (1.0f - fz) + c1 * fz;
+    if (c < n) sample_cell(g, field, c, position, out);
 }
 
 // ---- SOR -----------------------------------------------------------------------------------------

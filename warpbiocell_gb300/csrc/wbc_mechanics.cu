@@ -11,27 +11,9 @@
 //
 // Reference: spatial/neighbors.py:33-37 (HashGrid build over the active prefix) and
 // kernels/mechanics_kernels.py:26-67 (contact_velocities, integrate_positions).
-#include "wbc_common.cuh"
+#include "wbc_bodies.cuh"
 
 namespace wbc {
-
-struct BucketMap {
-    float inv_edge;
-    int dim;
-
-    __device__ __forceinline__ int coord(float x) const {
-        float q = x * inv_edge;
-        q = fminf(fmaxf(q, -1.0e9f), 1.0e9f);
-        return static_cast<int>(floorf(q));
-    }
-    __device__ __forceinline__ int wrap(int c) const {
-        int m = c % dim;
-        return m < 0 ? m + dim : m;
-    }
-    __device__ __forceinline__ int bucket(int cx, int cy, int cz) const {
-        return (wrap(cx) * dim + wrap(cy)) * dim + wrap(cz);
-    }
-};
 
 // Host-side: the bucket edge and its inverse, rounded exactly as the oracle rounds them.
 static BucketMap make_map(float cell_size, int dim) {
@@ -46,35 +28,22 @@ __global__ void k_bin_assign(BucketMap map, int32_t n, const float* __restrict__
                              int32_t* __restrict__ bucket_count, int32_t* __restrict__ cell_bucket,
                              int32_t* __restrict__ cell_rank) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float* p = position + 3 * static_cast<int64_t>(i);
-    int b = map.bucket(map.coord(p[0]), map.coord(p[1]), map.coord(p[2]));
-    cell_bucket[i] = b;
-    cell_rank[i] = atomicAdd(bucket_count + b, 1);
+    if (i < n) bin_assign_cell(map, i, position, bucket_count, cell_bucket, cell_rank);
 }
 
 __global__ void k_bin_scatter(int32_t n, const int32_t* __restrict__ cell_bucket, const int32_t* __restrict__ cell_rank,
                               const int32_t* __restrict__ bucket_start, int32_t* __restrict__ scatter) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    scatter[bucket_start[cell_bucket[i]] + cell_rank[i]] = i;
+    if (i < n) bin_scatter_cell(i, cell_bucket, cell_rank, bucket_start, scatter);
 }
 
-// Each slot finds its place among the members of its bucket in ascending slot order.
 __global__ void k_bin_order(int32_t n, const float* __restrict__ position, const float* __restrict__ radius,
                             const int32_t* __restrict__ cell_bucket, const int32_t* __restrict__ bucket_start,
                             const int32_t* __restrict__ bucket_count, const int32_t* __restrict__ scatter,
                             int32_t* __restrict__ sorted_id, float4* __restrict__ sorted_xyzr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int b = cell_bucket[i];
-    const int s = bucket_start[b];
-    const int c = bucket_count[b];
-    int rank = 0;
-    for (int u = s; u < s + c; ++u) rank += scatter[u] < i ? 1 : 0;
-    const float* p = position + 3 * static_cast<int64_t>(i);
-    sorted_id[s + rank] = i;
-    sorted_xyzr[s + rank] = make_float4(p[0], p[1], p[2], radius[i]);
+    if (i < n)
+        bin_order_cell(i, position, radius, cell_bucket, bucket_start, bucket_count, scatter, sorted_id, sorted_xyzr);
 }
 
 // One thread per sorted slot t (so a warp works on neighbouring cells and shares buckets).
@@ -85,47 +54,9 @@ __global__ void __launch_bounds__(256) k_contact(BucketMap map, int32_t n, const
                                                  float dt, float* __restrict__ position, float* __restrict__ velocity,
                                                  int32_t* __restrict__ neighbor_count) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const float4 me = sorted_xyzr[t];
-    const int i = sorted_id[t];
-    const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
-    float vx = 0.0f, vy = 0.0f, vz = 0.0f;
-    int count = 0;
-    for (int ox = -1; ox <= 1; ++ox) {
-        for (int oy = -1; oy <= 1; ++oy) {
-            for (int oz = -1; oz <= 1; ++oz) {
-                const int b = map.bucket(cx + ox, cy + oy, cz + oz);
-                const int s = bucket_start[b];
-                const int e = s + bucket_count[b];
-                for (int u = s; u < e; ++u) {
-                    if (u == t) continue;
-                    const float4 q = sorted_xyzr[u];
-                    const float dx = me.x - q.x;
-                    const float dy = me.y - q.y;
-                    const float dz = me.z - q.z;
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (d < query_radius) {
-                        ++count;
-                        const float overlap = me.w + q.w - d;
-                        if (overlap > 0.0f && d > 1.0e-6f) {
-                            const float f = rate * overlap / d;
-                            vx = vx + f * dx;
-                            vy = vy + f * dy;
-                            vz = vz + f * dz;
-                        }
-                    }
-                }
-            }
-        }
-    }
-    const int64_t o = 3 * static_cast<int64_t>(i);
-    velocity[o + 0] = vx;
-    velocity[o + 1] = vy;
-    velocity[o + 2] = vz;
-    neighbor_count[i] = count;
-    position[o + 0] = me.x + vx * dt;
-    position[o + 1] = me.y + vy * dt;
-    position[o + 2] = me.z + vz * dt;
+    if (t < n)
+        contact_slot(map, t, bucket_start, bucket_count, sorted_id, sorted_xyzr, query_radius, rate, dt, position,
+                     velocity, neighbor_count);
 }
 
 static bool grid_ok(const wbc_neighbor_grid* g) {

@@ -34,42 +34,7 @@ int check_launch(const char* where, int64_t launches) {
 // partial; phase 2 (one block) turns the partials into exclusive tile offsets with a running
 // carry, so any number of tiles works; phase 3 rescans each tile from its offset. Pure integer
 // work, so the result does not depend on the launch shape.
-constexpr int kScanThreads = 512;
-constexpr int kScanItems = 8;
-constexpr int kScanTile = kScanThreads * kScanItems;
-static_assert(kScanTile == kScanTileItems, "scan tile size shared with the scratch-free entry point");
-
 int64_t scan_partials_count(int64_t n) { return (n + kScanTile - 1) / kScanTile + 1; }
-
-__device__ __forceinline__ int32_t warp_inclusive(int32_t v) {
-    const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        int32_t o = __shfl_up_sync(0xffffffffu, v, d);
-        if (lane >= d) v += o;
-    }
-    return v;
-}
-
-// Block-wide exclusive scan of one value per thread; returns the exclusive prefix, *total the sum.
-__device__ __forceinline__ int32_t block_exclusive(int32_t v, int32_t* total) {
-    __shared__ int32_t warp_sums[kScanThreads / 32];
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    int32_t inc = warp_inclusive(v);
-    if (lane == 31) warp_sums[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        int32_t s = (lane < kScanThreads / 32) ? warp_sums[lane] : 0;
-        s = warp_inclusive(s);
-        if (lane < kScanThreads / 32) warp_sums[lane] = s;
-    }
-    __syncthreads();
-    int32_t warp_offset = warp > 0 ? warp_sums[warp - 1] : 0;
-    *total = warp_sums[kScanThreads / 32 - 1];
-    __syncthreads();
-    return warp_offset + inc - v;
-}
 
 __global__ void scan_reduce_tiles(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ partials) {
     const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;

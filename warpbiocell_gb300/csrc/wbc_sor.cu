@@ -28,6 +28,7 @@
 // Every wait polls a bounded number of times (about a second); on timeout the CTA raises an
 // abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -71,7 +72,7 @@ struct SorArgs {
     float* xchg;   // [2 buffers][2 parities][nx][ny][M] halo exchange
     float* coeff;  // [2][nx][ny][M] density * uptake_max, -1 where not updated
     SorControl* ctl;
-    unsigned int* flags;  // [gridDim.x] barrier epochs
+    unsigned int* flags;  // [tiles] barrier epochs
     int check_every;
     int max_sweeps;
     double tolerance;  // compared in double, as the reference compares float(residual) < tolerance
@@ -111,13 +112,14 @@ __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n 
 // Signals this CTA's arrival at the next epoch, then waits for the CTAs listed in `wait_for`
 // (n_wait of them) or, with n_wait < 0, for every CTA. Returns false when aborted (timeout here or
 // elsewhere). A halo exchange only needs the neighbouring tiles; the residual needs all.
-__device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch,
-                                             const int* wait_for = nullptr, int n_wait = -1) {
+// `me` is this CTA's tile among the `ntiles` tiles of its solve.
+__device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch, int me,
+                                             int ntiles, const int* wait_for = nullptr, int n_wait = -1) {
     epoch += 1;
     __syncthreads();  // the CTA's writes happen before thread 0's release (bar.sync is cumulative)
-    if (threadIdx.x == 0) store_release(flags + blockIdx.x, epoch);
+    if (threadIdx.x == 0) store_release(flags + me, epoch);
     int aborted = 0;
-    const unsigned n = n_wait < 0 ? gridDim.x : static_cast<unsigned>(n_wait);
+    const unsigned n = n_wait < 0 ? static_cast<unsigned>(ntiles) : static_cast<unsigned>(n_wait);
     for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
         const unsigned who = n_wait < 0 ? t : static_cast<unsigned>(wait_for[t]);
         unsigned polls = 0;
@@ -476,15 +478,16 @@ __device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list,
 // Columns longer than 3 x 32 entries per parity run 16 warps per CTA (128 registers a thread).
 constexpr int max_threads_for_lanes(int lanes) { return lanes > 3 ? 512 : 1024; }
 
+// One tile (`tile` of `ntiles`) of one solve, for the whole solve.
 template <bool HAS_PROD, int LANES, int H>
-__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
+__device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles) {
     extern __shared__ __align__(128) float s[];
     __shared__ unsigned int s_red[32];
     __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int bx = blockIdx.x / a.t.ty;
-    const int by = blockIdx.x - bx * a.t.ty;
+    const int bx = tile / a.t.ty;
+    const int by = tile - bx * a.t.ty;
     const int i0 = bx * a.t.ti, j0 = by * a.t.tj;
     const int ai = min(a.t.ti, nx - i0), aj = min(a.t.tj, ny - j0);
     const int bw = a.t.tj + 2 * H;  // bounding-box row length
@@ -642,7 +645,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     }
     // The ring columns' coefficients (and edge rows) are written by their owners: one global
     // barrier first.
-    bool ok = grid_barrier(a.ctl, a.flags, epoch);
+    bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles);
 
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
@@ -692,7 +695,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
                 copy_columns<LANES>(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
                 // A neighbour overwrites this buffer two exchanges later, i.e. only after this tile
                 // has signalled the next epoch, which comes after the pull below.
-                ok = grid_barrier(a.ctl, a.flags, epoch, s_neighbours, n_neighbours);
+                ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, s_neighbours, n_neighbours);
                 if (!ok) break;
                 copy_columns<LANES>(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
                 __syncthreads();
@@ -724,11 +727,11 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
             for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
             if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
         }
-        ok = grid_barrier(a.ctl, a.flags, epoch);
+        ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles);
         if (!ok) break;
         residual = __uint_as_float(load_acquire(&a.ctl->res_bits[slot]));
         // The next chunk's slot was last read before this chunk's first barrier: safe to clear.
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&a.ctl->res_bits[slot ^ 1], 0u);
+        if (tile == 0 && threadIdx.x == 0) atomicExch(&a.ctl->res_bits[slot ^ 1], 0u);
         ++chunk_index;
         if (static_cast<double>(residual) < a.tolerance) {
             converged = true;
@@ -736,7 +739,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         }
     }
     if (!ok) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) a.ctl->status = 1;
+        if (tile == 0 && threadIdx.x == 0) a.ctl->status = 1;
         return;
     }
     // Owned columns back to the field.
@@ -747,12 +750,65 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
         float* out = a.field + gi * w.sx + static_cast<int64_t>(gj) * nz;
         for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * w.ncm + c.x * M + (k >> 1)];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (tile == 0 && threadIdx.x == 0) {
         a.ctl->sweeps = sweeps;
         a.ctl->residual = residual;
         a.ctl->converged = converged ? 1 : 0;
         a.ctl->status = 0;
     }
+}
+
+template <bool HAS_PROD, int LANES, int H>
+__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
+    sor_tile<HAS_PROD, LANES, H>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
+}
+
+// ---- batched solves ----------------------------------------------------------------------------------
+// One persistent launch solves many grids. A CTA claims the next tile of the work list (the tiles
+// of item 0, then of item 1, ...) and runs it until that item's solve ends, then claims again.
+// An item's tiles wait for one another in its first barrier, so its tiles are all resident
+// before it starts; since claims are handed out in order and no item has more tiles than there
+// are CTAs, the tiles of every item eventually get CTAs.
+__device__ __forceinline__ int find_batch_item(const int32_t* first, int n, int x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= x)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool HAS_PROD, int LANES>
+__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1)
+    k_sor_batched(const SorArgs* __restrict__ args, const int32_t* __restrict__ tile_first, int n,
+                  unsigned int* __restrict__ next_tile) {
+    __shared__ int s_tile;
+    const int total = tile_first[n];
+    while (true) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_tile = static_cast<int>(atomicAdd(next_tile, 1u));
+        __syncthreads();
+        const int t = s_tile;
+        if (t >= total) return;
+        const int b = find_batch_item(tile_first, n, t);
+        sor_tile<HAS_PROD, LANES, 1>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b]);
+    }
+}
+
+// Zeroes every item's control line and barrier flags, and the claim counter.
+__global__ void k_sor_batch_reset(const SorArgs* __restrict__ args, const int32_t* __restrict__ tile_first, int n,
+                                  unsigned int* __restrict__ next_tile) {
+    for (int b = blockIdx.x; b < n; b += gridDim.x) {
+        const SorArgs& a = args[b];
+        unsigned int* ctl = reinterpret_cast<unsigned int*>(a.ctl);
+        for (int k = threadIdx.x; k < static_cast<int>(sizeof(SorControl) / 4); k += blockDim.x) ctl[k] = 0u;
+        const int tiles = tile_first[b + 1] - tile_first[b];
+        for (int k = threadIdx.x; k < tiles; k += blockDim.x) a.flags[k] = 0u;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) *next_tile = 0u;
 }
 
 // ---- host side -------------------------------------------------------------------------------------------
@@ -985,6 +1041,205 @@ static std::vector<wbc_sor_tuning> tuning_candidates(const wbc_sor_params& p, in
 }  // namespace wbc
 
 using namespace wbc;
+
+// ---- batched solves: host side -------------------------------------------------------------------------
+namespace wbc {
+
+using BatchedFn = void (*)(const SorArgs*, const int32_t*, int, unsigned int*);
+
+template <bool P>
+static BatchedFn batched_for_lanes(int lanes) {
+    switch (lanes) {
+        case 1: return k_sor_batched<P, 1>;
+        case 2: return k_sor_batched<P, 2>;
+        case 3: return k_sor_batched<P, 3>;
+        case 4: return k_sor_batched<P, 4>;
+        case 5: return k_sor_batched<P, 5>;
+        case 6: return k_sor_batched<P, 6>;
+        case 7: return k_sor_batched<P, 7>;
+        default: return k_sor_batched<P, 8>;
+    }
+}
+
+struct SorBatchLayout {
+    size_t next, args, first, bytes;
+};
+
+static SorBatchLayout sor_batch_layout(int n) {
+    SorBatchLayout L{};
+    L.next = 0;
+    L.args = 256;
+    L.first = L.args + ((n * sizeof(SorArgs) + 255) / 256) * 256;
+    L.bytes = L.first + (n + 1) * sizeof(int32_t);
+    return L;
+}
+
+}  // namespace wbc
+
+extern "C" {
+
+size_t wbc_sor_batch_plan_bytes(int32_t n) { return n > 0 ? sor_batch_layout(n).bytes : 0; }
+
+int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t check_every, int32_t max_sweeps,
+                          double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out, void* stream) {
+    if (n <= 0 || !items || !plan || !out || check_every < 1 || max_sweeps < 1) return WBC_ERR_INVALID;
+    const SorBatchLayout L = sor_batch_layout(n);
+    if (plan_bytes < L.bytes) return WBC_ERR_WORKSPACE;
+    const DeviceInfo dev = device_info();
+    if (dev.sms <= 0) {
+        set_error_msg("wbc_sor_batch_prepare: no device");
+        return WBC_ERR_CUDA;
+    }
+    const int G = std::min(dev.sms, kMaxCtas);
+    const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;
+    double total_nodes = 0.0;
+    for (int b = 0; b < n; ++b) {
+        const wbc_sor_params& p = items[b].params;
+        if (p.nx < 3 || p.ny < 3 || p.nz < 3 || !items[b].density || !items[b].field || !items[b].workspace ||
+            (p.has_source && !items[b].source) || reinterpret_cast<uintptr_t>(items[b].workspace) % 16 != 0) {
+            set_error_msg("wbc_sor_batch_prepare: invalid item");
+            return WBC_ERR_INVALID;
+        }
+        total_nodes += static_cast<double>(p.nx) * p.ny * p.nz;
+    }
+    std::vector<SorArgs> args(n);
+    std::vector<int32_t> first(n + 1, 0);
+    int lanes = 1, threads = 32;
+    bool has_prod = false;
+    size_t smem = 0;
+    for (int b = 0; b < n; ++b) {
+        const wbc_sor_batch_item& it = items[b];
+        const wbc_sor_params& p = it.params;
+        // CTAs in proportion to the grid's nodes, raised until the tiles fit in shared memory.
+        const double nodes = static_cast<double>(p.nx) * p.ny * p.nz;
+        int share = std::max(1, static_cast<int>(G * nodes / total_nodes));
+        SorTiling t{};
+        bool fits = false;
+        for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 1, 0, 0, &t);
+        if (!fits) {
+            set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
+            return WBC_ERR_INVALID;
+        }
+        char* base = static_cast<char*>(it.workspace);
+        SorArgs& a = args[b];
+        a.p = p;
+        a.t = t;
+        a.fixed = it.fixed;
+        a.density = it.density;
+        a.production = it.production;
+        a.source = it.source;
+        a.field = it.field;
+        a.xchg = reinterpret_cast<float*>(base + header_bytes());
+        a.coeff = reinterpret_cast<float*>(base + header_bytes() + 2 * plane_bytes(p));
+        a.ctl = reinterpret_cast<SorControl*>(base);
+        a.flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
+        a.check_every = check_every;
+        a.max_sweeps = max_sweeps;
+        a.tolerance = tolerance;
+        first[b + 1] = first[b] + t.tx * t.ty;
+        lanes = std::max(lanes, t.lanes);
+        threads = std::max(threads, t.threads);
+        smem = std::max(smem, t.smem);
+        has_prod = has_prod || it.production != nullptr || p.has_source;
+    }
+    threads = std::min(threads, max_threads_for_lanes(lanes));
+    BatchedFn fn = has_prod ? batched_for_lanes<true>(lanes) : batched_for_lanes<false>(lanes);
+    cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    int per_sm = 0;
+    if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    if (err != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        set_error_msg("wbc_sor_batch_prepare: the batched solver does not fit on an SM");
+        return WBC_ERR_INVALID;
+    }
+    const int ctas = std::min(G, first[n]);
+    std::vector<char> host(L.bytes, 0);
+    std::memcpy(host.data() + L.args, args.data(), n * sizeof(SorArgs));
+    std::memcpy(host.data() + L.first, first.data(), (n + 1) * sizeof(int32_t));
+    cudaStream_t s = as_stream(stream);
+    err = cudaMemcpyAsync(plan, host.data(), L.bytes, cudaMemcpyHostToDevice, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);  // `host` goes out of scope
+    if (err != cudaSuccess) {
+        set_error("wbc_sor_batch_prepare: copying the plan", err);
+        return WBC_ERR_CUDA;
+    }
+    out->items = n;
+    out->total_tiles = first[n];
+    out->ctas = ctas;
+    out->threads = threads;
+    out->lanes = lanes;
+    out->has_prod = has_prod ? 1 : 0;
+    out->smem_bytes = static_cast<int64_t>(smem);
+    out->device_plan = plan;
+    return WBC_OK;
+}
+
+int wbc_sor_batch_solve(const wbc_sor_batch* b, void* stream) {
+    if (!b || b->items <= 0 || !b->device_plan || b->ctas < 1) return WBC_ERR_INVALID;
+    const SorBatchLayout L = sor_batch_layout(b->items);
+    char* base = static_cast<char*>(b->device_plan);
+    const SorArgs* args = reinterpret_cast<const SorArgs*>(base + L.args);
+    const int32_t* first = reinterpret_cast<const int32_t*>(base + L.first);
+    unsigned int* next = reinterpret_cast<unsigned int*>(base + L.next);
+    cudaStream_t s = as_stream(stream);
+    k_sor_batch_reset<<<std::min(b->items, 1024), 128, 0, s>>>(args, first, b->items, next);
+    BatchedFn fn = b->has_prod ? batched_for_lanes<true>(b->lanes) : batched_for_lanes<false>(b->lanes);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(b->ctas);
+    cfg.blockDim = dim3(b->threads);
+    cfg.dynamicSmemBytes = static_cast<size_t>(b->smem_bytes);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int items = b->items;
+    cudaError_t err = cudaLaunchKernelEx(&cfg, fn, args, first, items, next);
+    if (err != cudaSuccess) {
+        set_error("wbc_sor_batch_solve: cudaLaunchKernelEx", err);
+        return WBC_ERR_CUDA;
+    }
+    return check_launch("wbc_sor_batch_solve", 2);
+}
+
+int wbc_sor_batch_reports(const wbc_sor_batch* b, wbc_sor_report* reports, void* stream) {
+    if (!b || b->items <= 0 || !b->device_plan || !reports) return WBC_ERR_INVALID;
+    const SorBatchLayout L = sor_batch_layout(b->items);
+    std::vector<SorArgs> args(b->items);
+    std::vector<int32_t> first(b->items + 1);
+    cudaStream_t s = as_stream(stream);
+    char* base = static_cast<char*>(b->device_plan);
+    cudaError_t err = cudaMemcpyAsync(args.data(), base + L.args, b->items * sizeof(SorArgs), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(first.data(), base + L.first, (b->items + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    std::vector<SorControl> ctl(b->items);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    for (int i = 0; i < b->items && err == cudaSuccess; ++i)
+        err = cudaMemcpyAsync(&ctl[i], args[i].ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+        set_error("wbc_sor_batch_reports: reading the reports", err);
+        return WBC_ERR_CUDA;
+    }
+    int rc = WBC_OK;
+    for (int i = 0; i < b->items; ++i) {
+        reports[i].sweeps = ctl[i].sweeps;
+        reports[i].residual = ctl[i].residual;
+        reports[i].converged = ctl[i].converged;
+        reports[i].path = 2;
+        reports[i].tiles = first[i + 1] - first[i];
+        reports[i].halo_depth = 1;
+        reports[i].tiles_i = args[i].t.tx;
+        reports[i].tiles_j = args[i].t.ty;
+        if (ctl[i].status != 0) rc = WBC_ERR_TIMEOUT;
+    }
+    if (rc != WBC_OK) set_error_msg("wbc_sor_batch_reports: a solve timed out");
+    return rc;
+}
+
+}  // extern "C"
 
 extern "C" {
 
