@@ -55,6 +55,11 @@ WORKLOADS = {
     # updated synchronously once per step; lifecycle in network mode.
     "metabolic_network_100k_81": dict(cells=100_000, ball_um=600.0, box_um=1600.0, dx_um=20.0, boundary=38.0,
                                       metabolic=True, network_nodes=106),
+    # 15 spheroids: boundary O2 {10, 20, 38, 60, 100} mmHg x 3 seeds, cell counts log-uniform in
+    # [2,000, 200,000] at the 1M-cell workload's density, cubic grids of 41-121 nodes (odd, growing
+    # with the count) over a box of 2.5 spheroid radii; advanced as one batch against 15 plain runs.
+    "batched_sweep_15": dict(batched=True, boundaries=(10.0, 20.0, 38.0, 60.0, 100.0), seeds=(0, 1, 2),
+                             cells_lo=2_000, cells_hi=200_000, nodes_lo=41, nodes_hi=121, box_over_radius=2.5),
 }
 
 # DRAM bytes per colour half-sweep of the resident SOR solver at 161^3: one `ncu --set full`
@@ -573,6 +578,135 @@ def run_reference(args) -> dict:
     }
 
 
+# ---- batched sweep (15 spheroids) ----------------------------------------------------------------------
+def batch_specs(w: dict, seed: int) -> list[dict]:
+    """The sweep's instances: (cells, ball radius, grid nodes, spacing, boundary, seed) each."""
+    rng = np.random.default_rng(2026 + seed)
+    density = 1.0e6 / (4.0 / 3.0 * math.pi * 1200.0**3)  # cells per um^3 of the 1M-cell workload
+    lo, hi = math.log(w["cells_lo"]), math.log(w["cells_hi"])
+    specs = []
+    for boundary in w["boundaries"]:
+        for s in w["seeds"]:
+            u = float(rng.random())
+            cells = int(round(math.exp(lo + u * (hi - lo))))
+            radius = (3.0 * cells / (4.0 * math.pi * density)) ** (1.0 / 3.0)
+            nodes = w["nodes_lo"] + 2 * int(round(u * (w["nodes_hi"] - w["nodes_lo"]) / 2))
+            box = w["box_over_radius"] * radius
+            specs.append(dict(cells=cells, ball=radius, nodes=nodes, dx=box / (nodes - 1), boundary=boundary,
+                              seed=1000 * seed + 17 * len(specs) + s))
+    return specs
+
+
+def build_member(spec: dict, P: dict, dev):
+    import torch  # noqa: F401
+
+    from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball
+    from warpbiocell_gb300.cells.mechanics import contact_substep, make_neighbor_grid
+    from warpbiocell_gb300.cells.state import CellPopulation
+    from warpbiocell_gb300.fields.oxygen import OxygenField, OxygenParams
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+    from warpbiocell_gb300.simulation.batch import BatchMember
+
+    pos = uniform_ball(spec["cells"], spec["ball"], seed=spec["seed"])
+    radii = clipped_normal_radii(spec["cells"], 8.0, 0.8, 6.0, 10.0, seed=spec["seed"] + 1)
+    pop = CellPopulation.from_numpy(pos, radii, capacity=3 * spec["cells"], device=dev, seed=spec["seed"])
+    half = 0.5 * (spec["nodes"] - 1) * spec["dx"]
+    geom = GridGeometry(origin=(-half, -half, -half), dx=spec["dx"], shape=(spec["nodes"],) * 3)
+    oxygen = OxygenField(geom, OxygenParams(diffusion_coefficient=DIFFUSION, uptake_max=VMAX, michaelis_k=KM,
+                                            boundary_value=spec["boundary"]), P["settings"], device=dev)
+    grid = make_neighbor_grid(P["contact"], dev)
+    # As the reference's Experiment.run: initial neighbour counts and an initial field solve.
+    contact_substep(pop, grid, P["contact"], dt=0.0)
+    oxygen.update(pop)
+    return BatchMember(pop, grid, oxygen, P["lifecycle"], P["contact"])
+
+
+def run_batched(args) -> dict:
+    import torch
+
+    from warpbiocell_gb300 import _lib
+    from warpbiocell_gb300.simulation.batch import SpheroidBatch
+    from warpbiocell_gb300.simulation.simulator import cell_step
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    w = WORKLOADS[args.workload]
+    P = make_params(dict(box_um=800.0, dx_um=20.0, boundary=38.0))
+    specs = batch_specs(w, args.seed)
+    stepping = P["stepping"]
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    # 15 plain runs, one after another (warm-up steps, then the timed steps of each run).
+    plain = [build_member(sp, P, dev) for sp in specs]
+
+    def run_plain(steps):
+        cell_steps = 0
+        for m in plain:
+            for _ in range(steps):
+                cell_steps += m.population.count
+                cell_step(m.population, m.grid, m.lifecycle, m.contact, stepping, oxygen=m.oxygen)
+        return cell_steps
+
+    run_plain(args.warmup)
+    plain_cells, plain_ms = timed(lambda: run_plain(args.steps))
+
+    # The same 15 runs as one batch: the first warm-up step outside the graph, then capture.
+    members = [build_member(sp, P, dev) for sp in specs]
+    batch = SpheroidBatch(members, stepping)
+    batch.step(1)
+    torch.cuda.synchronize()
+    batch.rebalance()  # the first step's sweep counts weigh the work list
+    batch.capture()
+    if args.warmup > 1:
+        batch.step(args.warmup - 1)
+    _, batch_ms = timed(lambda: batch.step(args.steps))
+    counts = batch.sync()
+    identical = batch.status_codes() == [0] * len(specs)
+    for m, p in zip(members, plain):
+        a, b = m.population, p.population
+        identical = identical and a.count == b.count
+        n = a.count
+        for name in ("position", "radius", "cell_state", "age", "oxygen_local", "rng_state", "velocity",
+                     "neighbor_count"):
+            identical = identical and torch.equal(getattr(a, name)[:n], getattr(b, name)[:n])
+        identical = identical and torch.equal(m.oxygen.field.values, p.oxygen.field.values)
+    reps = batch.reports()
+    steps = max(1, args.steps)
+    value = plain_cells / (batch_ms / 1e3)
+    plain_value = plain_cells / (plain_ms / 1e3)
+    nodes = sum(sp["nodes"] ** 3 for sp in specs)
+    return {
+        "metric": "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)",
+        "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(batch_ms / steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
+        "data": "synthetic (seeded uniform balls, clipped-normal radii)",
+        "config": {"workload": args.workload, "instances": len(specs),
+                   "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
+                   "boundary_mmHg": [sp["boundary"] for sp in specs], "total_grid_nodes": nodes,
+                   "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT,
+                   "parallelism": "one GPU, instances batched"},
+        "sequential": {"value": round(plain_value, 1), "ms_per_step": round(plain_ms / steps, 4),
+                       "what": "the same 15 runs through the plain per-run path (cell_step), one after another"},
+        "speedup_vs_sequential": round(plain_ms / batch_ms, 3),
+        "identical_outputs": bool(identical),
+        "gpu_launches": int(batch.launches_per_step * args.steps),
+        "launches_per_step": int(batch.launches_per_step),
+        "final_counts": counts,
+        "last_solve_sweeps": [r.sweeps for r in reps],
+        "sor_batch": {"tiles": int(batch.sor.total_tiles), "ctas": int(batch.sor.ctas),
+                      "smem_bytes": int(batch.sor.smem_bytes)},
+    }
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -594,6 +728,10 @@ def main() -> None:
     if args.impl == "reference":
         if rank == 0:
             print(json.dumps(run_reference(args)))
+        return
+    if WORKLOADS[args.workload].get("batched"):
+        if rank == 0:
+            print(json.dumps(run_batched(args)))
         return
 
     if world > 1:

@@ -212,10 +212,13 @@ typedef struct wbc_sor_batch {    /* filled by wbc_sor_batch_prepare            
 } wbc_sor_batch;
 
 size_t wbc_sor_batch_plan_bytes(int32_t n);
-/* Tiles every item (CTAs in proportion to its nodes), copies the work list into `plan` (device
+/* Orders the items heaviest first by `weights` (host, one positive value per item, e.g. nodes x
+ * sweeps of the previous solve; NULL = node counts), tiles each with CTAs in proportion to its
+ * weight (raised until the tiles fit in shared memory), copies the work list into `plan` (device
  * memory) and fills `out`. Synchronises `stream`; not for use during stream capture. */
-int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t check_every, int32_t max_sweeps,
-                          double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out, void* stream);
+int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
+                          int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
+                          void* stream);
 /* Solves every item from its field's current values; nothing is read back (capturable). */
 int wbc_sor_batch_solve(const wbc_sor_batch* b, void* stream);
 /* The items' reports (host array of b->items); synchronises. WBC_ERR_TIMEOUT if a solve timed out. */

@@ -227,8 +227,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
                          POINTER(c_float), _P],
     "wbc_sor_batch_plan_bytes": [_I],
-    "wbc_sor_batch_prepare": [_I, POINTER(SorBatchItemC), _I, _I, ctypes.c_double, _P, c_size_t, POINTER(SorBatchC),
-                              _P],
+    "wbc_sor_batch_prepare": [_I, POINTER(SorBatchItemC), _P, _I, _I, ctypes.c_double, _P, c_size_t,
+                              POINTER(SorBatchC), _P],
     "wbc_sor_batch_solve": [POINTER(SorBatchC), _P],
     "wbc_sor_batch_reports": [POINTER(SorBatchC), POINTER(SorReportC), _P],
     "wbc_batch_plan_bytes": [_I, POINTER(BatchInstanceC)],

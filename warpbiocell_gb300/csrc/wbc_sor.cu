@@ -1062,15 +1062,17 @@ static BatchedFn batched_for_lanes(int lanes) {
 }
 
 struct SorBatchLayout {
-    size_t next, args, first, bytes;
+    size_t next, args, first, item, bytes;
 };
 
+// [claim counter | SorArgs per work-list position | tile offsets | item index per position]
 static SorBatchLayout sor_batch_layout(int n) {
     SorBatchLayout L{};
     L.next = 0;
     L.args = 256;
     L.first = L.args + ((n * sizeof(SorArgs) + 255) / 256) * 256;
-    L.bytes = L.first + (n + 1) * sizeof(int32_t);
+    L.item = L.first + (n + 1) * sizeof(int32_t);
+    L.bytes = L.item + n * sizeof(int32_t);
     return L;
 }
 
@@ -1080,8 +1082,9 @@ extern "C" {
 
 size_t wbc_sor_batch_plan_bytes(int32_t n) { return n > 0 ? sor_batch_layout(n).bytes : 0; }
 
-int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t check_every, int32_t max_sweeps,
-                          double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out, void* stream) {
+int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
+                          int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
+                          void* stream) {
     if (n <= 0 || !items || !plan || !out || check_every < 1 || max_sweeps < 1) return WBC_ERR_INVALID;
     const SorBatchLayout L = sor_batch_layout(n);
     if (plan_bytes < L.bytes) return WBC_ERR_WORKSPACE;
@@ -1092,27 +1095,37 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t ch
     }
     const int G = std::min(dev.sms, kMaxCtas);
     const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;
-    double total_nodes = 0.0;
+    // Expected work per item: the caller's weight (e.g. nodes x sweeps of the previous solve), or
+    // its node count. Items go on the work list heaviest first, each with CTAs in proportion to
+    // its work (three times its share of the GPU: the grids rarely all fit in shared memory at
+    // once, and smaller tiles shorten the heaviest solves, which bound the launch), raised until
+    // its tiles fit in shared memory.
+    std::vector<double> work(n);
+    double total_work = 0.0;
     for (int b = 0; b < n; ++b) {
         const wbc_sor_params& p = items[b].params;
         if (p.nx < 3 || p.ny < 3 || p.nz < 3 || !items[b].density || !items[b].field || !items[b].workspace ||
-            (p.has_source && !items[b].source) || reinterpret_cast<uintptr_t>(items[b].workspace) % 16 != 0) {
+            (p.has_source && !items[b].source) || reinterpret_cast<uintptr_t>(items[b].workspace) % 16 != 0 ||
+            (weights && !(weights[b] > 0.0f))) {
             set_error_msg("wbc_sor_batch_prepare: invalid item");
             return WBC_ERR_INVALID;
         }
-        total_nodes += static_cast<double>(p.nx) * p.ny * p.nz;
+        work[b] = weights ? static_cast<double>(weights[b]) : static_cast<double>(p.nx) * p.ny * p.nz;
+        total_work += work[b];
     }
+    std::vector<int32_t> order(n);
+    for (int b = 0; b < n; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
     std::vector<SorArgs> args(n);
     std::vector<int32_t> first(n + 1, 0);
     int lanes = 1, threads = 32;
     bool has_prod = false;
     size_t smem = 0;
-    for (int b = 0; b < n; ++b) {
+    for (int k = 0; k < n; ++k) {
+        const int b = order[k];
         const wbc_sor_batch_item& it = items[b];
         const wbc_sor_params& p = it.params;
-        // CTAs in proportion to the grid's nodes, raised until the tiles fit in shared memory.
-        const double nodes = static_cast<double>(p.nx) * p.ny * p.nz;
-        int share = std::max(1, static_cast<int>(G * nodes / total_nodes));
+        int share = std::min(G, std::max(1, static_cast<int>(3.0 * G * work[b] / total_work + 0.5)));
         SorTiling t{};
         bool fits = false;
         for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 1, 0, 0, &t);
@@ -1121,7 +1134,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t ch
             return WBC_ERR_INVALID;
         }
         char* base = static_cast<char*>(it.workspace);
-        SorArgs& a = args[b];
+        SorArgs& a = args[k];
         a.p = p;
         a.t = t;
         a.fixed = it.fixed;
@@ -1136,7 +1149,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t ch
         a.check_every = check_every;
         a.max_sweeps = max_sweeps;
         a.tolerance = tolerance;
-        first[b + 1] = first[b] + t.tx * t.ty;
+        first[k + 1] = first[k] + t.tx * t.ty;
         lanes = std::max(lanes, t.lanes);
         threads = std::max(threads, t.threads);
         smem = std::max(smem, t.smem);
@@ -1157,6 +1170,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, int32_t ch
     std::vector<char> host(L.bytes, 0);
     std::memcpy(host.data() + L.args, args.data(), n * sizeof(SorArgs));
     std::memcpy(host.data() + L.first, first.data(), (n + 1) * sizeof(int32_t));
+    std::memcpy(host.data() + L.item, order.data(), n * sizeof(int32_t));
     cudaStream_t s = as_stream(stream);
     err = cudaMemcpyAsync(plan, host.data(), L.bytes, cudaMemcpyHostToDevice, s);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);  // `host` goes out of scope
@@ -1208,12 +1222,14 @@ int wbc_sor_batch_reports(const wbc_sor_batch* b, wbc_sor_report* reports, void*
     if (!b || b->items <= 0 || !b->device_plan || !reports) return WBC_ERR_INVALID;
     const SorBatchLayout L = sor_batch_layout(b->items);
     std::vector<SorArgs> args(b->items);
-    std::vector<int32_t> first(b->items + 1);
+    std::vector<int32_t> first(b->items + 1), order(b->items);
     cudaStream_t s = as_stream(stream);
     char* base = static_cast<char*>(b->device_plan);
     cudaError_t err = cudaMemcpyAsync(args.data(), base + L.args, b->items * sizeof(SorArgs), cudaMemcpyDeviceToHost, s);
     if (err == cudaSuccess)
         err = cudaMemcpyAsync(first.data(), base + L.first, (b->items + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(order.data(), base + L.item, b->items * sizeof(int32_t), cudaMemcpyDeviceToHost, s);
     std::vector<SorControl> ctl(b->items);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s);
     for (int i = 0; i < b->items && err == cudaSuccess; ++i)
@@ -1224,16 +1240,17 @@ int wbc_sor_batch_reports(const wbc_sor_batch* b, wbc_sor_report* reports, void*
         return WBC_ERR_CUDA;
     }
     int rc = WBC_OK;
-    for (int i = 0; i < b->items; ++i) {
-        reports[i].sweeps = ctl[i].sweeps;
-        reports[i].residual = ctl[i].residual;
-        reports[i].converged = ctl[i].converged;
-        reports[i].path = 2;
-        reports[i].tiles = first[i + 1] - first[i];
-        reports[i].halo_depth = 1;
-        reports[i].tiles_i = args[i].t.tx;
-        reports[i].tiles_j = args[i].t.ty;
-        if (ctl[i].status != 0) rc = WBC_ERR_TIMEOUT;
+    for (int k = 0; k < b->items; ++k) {
+        wbc_sor_report& r = reports[order[k]];
+        r.sweeps = ctl[k].sweeps;
+        r.residual = ctl[k].residual;
+        r.converged = ctl[k].converged;
+        r.path = 2;
+        r.tiles = first[k + 1] - first[k];
+        r.halo_depth = 1;
+        r.tiles_i = args[k].t.tx;
+        r.tiles_j = args[k].t.ty;
+        if (ctl[k].status != 0) rc = WBC_ERR_TIMEOUT;
     }
     if (rc != WBC_OK) set_error_msg("wbc_sor_batch_reports: a solve timed out");
     return rc;

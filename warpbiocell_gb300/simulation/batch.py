@@ -63,6 +63,7 @@ class SpheroidBatch:
         self.counts = torch.tensor([m.population.count for m in members], dtype=torch.int32, device=self.device)
         self.status = torch.zeros(n, dtype=torch.int32, device=self.device)
         self._graph = None
+        self.launches_per_step = 0
 
         insts = (_lib.BatchInstanceC * n)()
         for k, m in enumerate(members):
@@ -87,9 +88,23 @@ class SpheroidBatch:
         sor_bytes = int(_lib.load().wbc_sor_batch_plan_bytes(n))
         self._sor_plan = torch.empty(sor_bytes, dtype=torch.uint8, device=self.device)
         self.sor = _lib.SorBatchC()
-        _lib.call("wbc_sor_batch_prepare", n, items, int(settings.check_every), int(settings.max_sweeps),
-                  float(settings.tolerance), _lib.ptr(self._sor_plan), sor_bytes, ctypes.byref(self.sor),
-                  _lib.stream(self.device))
+        self._prepare_solver(None)
+
+    def _prepare_solver(self, weights) -> None:
+        n = len(self.members)
+        w = (ctypes.c_float * n)(*weights) if weights is not None else None
+        _lib.call("wbc_sor_batch_prepare", n, self._items, w, int(self.settings.check_every),
+                  int(self.settings.max_sweeps), float(self.settings.tolerance), _lib.ptr(self._sor_plan),
+                  self._sor_plan.numel(), ctypes.byref(self.sor), _lib.stream(self.device))
+
+    def rebalance(self) -> None:
+        """Re-plan the batched solve with each member's last sweep count x grid nodes as its
+        expected work (the heaviest solves start first, with the most CTAs). Drops a captured
+        graph; call :meth:`capture` again."""
+        reports = self.reports()
+        weights = [float(m.oxygen.geometry.node_count) * max(1, r.sweeps) for m, r in zip(self.members, reports)]
+        self._prepare_solver(weights)
+        self._graph = None
 
     def _instance(self, m: BatchMember) -> _lib.BatchInstanceC:
         pop, grid, fld = m.population, m.grid, m.oxygen
@@ -140,6 +155,7 @@ class SpheroidBatch:
     def capture(self) -> None:
         """Record one step as a CUDA graph; later :meth:`step` calls replay it."""
         graph = torch.cuda.CUDAGraph()
+        before = _lib.launch_count()
         stream = torch.cuda.Stream(device=self.device)
         stream.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(stream):
@@ -147,6 +163,7 @@ class SpheroidBatch:
                 self._launch_step()
         torch.cuda.current_stream(self.device).wait_stream(stream)
         self._graph = graph
+        self.launches_per_step = _lib.launch_count() - before  # kernels in one replay
 
     # ---- host view ---------------------------------------------------------------------------------
     def sync(self) -> list[int]:
