@@ -321,6 +321,33 @@ int wbc_network_inherit(int32_t count_before, int32_t n_words, const int32_t* di
 int wbc_network_count_on(int32_t n, int32_t n_words, int32_t n_query, const int32_t* nodes, int32_t living_only,
                          const int32_t* cell_state, const uint64_t* states, int32_t* counts, void* stream);
 
+/* ---- adjoint of the coupled steady state ------------------------------------------------------------
+ * Forward: K contact steps (wbc_contact_substep), a deposit of per-cell uptake capacities, the
+ * steady Michaelis-Menten field (wbc_sor_solve with uptake_max = 1 on the deposited capacities).
+ * Reverse: the hand-written adjoint below. No counterpart in the reference. */
+/* acc[node] += int64(w * weight_i * 2^24 + 0.5) for the trilinear corners of each cell inside the
+ * deposit support (the rule of wbc_deposit); one layer, deterministic. */
+int wbc_deposit_weighted(const wbc_grid_geometry* geom, int32_t n, const float* position, const float* weight,
+                         int64_t* accumulator, void* stream);
+/* out[node] = float(acc[node]) / 2^24 * factor; clear != 0 zeroes acc. */
+int wbc_weighted_convert(int64_t nodes, int64_t* accumulator, float factor, float* out, int32_t clear,
+                         void* stream);
+/* One reverse contact step over the grid built at the step's start positions:
+ * lambda_out = lambda_in + dt J^T lambda_in, vdot[i] = lambda_in_i . v_i / rate. */
+int wbc_adjoint_contact(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                        const float* lambda_in, float* lambda_out, float* vdot, void* stream);
+/* Field adjoint (Dirichlet faces): red-black SOR on (6 + h kappa) mu - sum_nb mu = grad_u from mu's
+ * current values (start from zeros), kappa = U K / (K + u)^2, until max |residual| < tolerance
+ * (checked every check_every sweeps, synchronising); then phi = mu u / (K + u) and
+ * sums = {dL/dK, D dL/dD, dL/dO_b} (device doubles). kappa, phi: float[nodes] scratch/outputs;
+ * residual_bits: one device uint32. */
+int wbc_adjoint_field_solve(const wbc_sor_params* p, const float* u, const float* U, const float* grad_u, float* mu,
+                            float* kappa, int32_t check_every, int32_t max_sweeps, float tolerance, float* phi,
+                            double* sums, uint32_t* residual_bits, wbc_sor_report* report, void* stream);
+/* Per cell: grad_vmax = coef sum_a w_a phi_a, grad_x += coef vmax grad_x(sum_a w_a phi_a). */
+int wbc_adjoint_cells(const wbc_grid_geometry* geom, int32_t n, const float* position, const float* vmax,
+                      const float* phi, float coef, float* grad_vmax, float* grad_x, void* stream);
+
 /* ---- batches: many independent spheroids advanced together ------------------------------------
  * One instance = one population with its hash grid and oxygen grid, described by device pointers
  * into arrays the caller owns (the same arrays the single-population calls take). Every batched

@@ -517,3 +517,24 @@ def full_cell_step(sim: OracleSim, lifecycle, contact, dt_cells: float, dt_mecha
     for _ in range(substeps):
         sim.contact_substep(contact.query_radius, dim, contact.query_radius, contact.rate, dt_mechanics)
     return daughters, reports
+
+
+def adjoint_forward_f64(pos0: np.ndarray, radius: np.ndarray, vmax: np.ndarray, geom: Geometry, steps: int, dt: float,
+                        rate: float, query_radius: float, cell_size: float, dim: int, diffusion: float,
+                        michaelis_k: float, boundary: float, omega: float = 1.8, tolerance: float = 1e-13,
+                        max_sweeps: int = 200000):
+    """FP64 forward of the adjoint model (exact deposit weights, double parameters): returns the
+    steady field (nodes,) and the positions after ``steps`` contact steps."""
+    pos = np.ascontiguousarray(pos0, dtype=np.float64).copy()
+    r = np.ascontiguousarray(radius, dtype=np.float64)
+    v = np.ascontiguousarray(vmax, dtype=np.float64)
+    nx, ny, nz = geom.shape
+    origin = np.ascontiguousarray(geom.origin, dtype=np.float64)
+    field = np.zeros(geom.nodes, dtype=np.float64)
+    lib().orc_adjoint_forward_f64.restype = c_int32
+    sweeps = lib().orc_adjoint_forward_f64(
+        c_int32(pos.shape[0]), P(pos), P(r), P(v), f32(cell_size), c_int32(dim), c_double(query_radius),
+        c_double(rate), c_double(dt), c_int32(steps), c_int32(nx), c_int32(ny), c_int32(nz), P(origin),
+        c_double(geom.dx), c_double(diffusion), c_double(michaelis_k), c_double(boundary), c_double(omega),
+        c_double(tolerance), c_int32(max_sweeps), P(field))
+    return field, pos, int(sweeps)

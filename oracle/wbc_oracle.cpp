@@ -774,4 +774,77 @@ void orc_network_count_on(int32_t n, int32_t n_words, int32_t n_query, const int
     }
 }
 
+// ---- FP64 forward of the adjoint model (finite-difference reference) ------------------------------------
+// K contact steps in double, the per-cell uptake deposit with exact (unquantised) trilinear
+// weights, and the steady Michaelis-Menten field in double with double parameters, Dirichlet
+// faces at `boundary`, red-black SOR (omega) until max |r| / max(6 u, boundary) < tolerance.
+// The GPU model quantises the deposit weights to 2^-24; the reference does not, so central
+// differences of its loss measure the derivative of the exact model.
+int32_t orc_adjoint_forward_f64(int32_t n, double* pos, const double* radius, const double* vmax, float cell_size,
+                                int32_t dim, double query_radius, double rate, double dt, int32_t steps, int32_t nx,
+                                int32_t ny, int32_t nz, const double* origin, double dx, double diffusion,
+                                double michaelis_k, double boundary, double omega, double tolerance,
+                                int32_t max_sweeps, double* field) {
+    std::vector<double> vel(3 * static_cast<size_t>(n));
+    std::vector<int32_t> nc(n);
+    for (int32_t t = 0; t < steps; ++t)
+        orc_contact_substep_f64(n, pos, radius, cell_size, dim, query_radius, rate, dt, vel.data(), nc.data());
+    const int64_t nodes = static_cast<int64_t>(nx) * ny * nz;
+    std::vector<double> U(nodes, 0.0);
+    const double inv_dx = 1.0 / dx, inv_vol = inv_dx * inv_dx * inv_dx;
+    for (int32_t c = 0; c < n; ++c) {
+        const double ux = (pos[3 * c] - origin[0]) * inv_dx, uy = (pos[3 * c + 1] - origin[1]) * inv_dx,
+                     uz = (pos[3 * c + 2] - origin[2]) * inv_dx;
+        const int i0 = static_cast<int>(std::floor(ux)), j0 = static_cast<int>(std::floor(uy)),
+                  k0 = static_cast<int>(std::floor(uz));
+        if (i0 < 0 || j0 < 0 || k0 < 0 || i0 + 1 >= nx || j0 + 1 >= ny || k0 + 1 >= nz) continue;
+        const double fx = ux - i0, fy = uy - j0, fz = uz - k0;
+        for (int di = 0; di < 2; ++di)
+            for (int dj = 0; dj < 2; ++dj)
+                for (int dk = 0; dk < 2; ++dk) {
+                    const double w = (di ? fx : 1.0 - fx) * (dj ? fy : 1.0 - fy) * (dk ? fz : 1.0 - fz);
+                    U[(static_cast<int64_t>(i0 + di) * ny + (j0 + dj)) * nz + (k0 + dk)] += w * vmax[c] * inv_vol;
+                }
+    }
+    const double h = dx * dx / diffusion;
+    for (int64_t a = 0; a < nodes; ++a) field[a] = boundary;
+    auto interior = [&](int i, int j, int k) { return i > 0 && j > 0 && k > 0 && i < nx - 1 && j < ny - 1 && k < nz - 1; };
+    const double ref = boundary > 0.0 ? boundary : 1.0;
+    int32_t sweeps = 0;
+    while (sweeps < max_sweeps) {
+        for (int colour = 0; colour < 2; ++colour) {
+#pragma omp parallel for schedule(static)
+            for (int i = 1; i < nx - 1; ++i)
+                for (int j = 1; j < ny - 1; ++j)
+                    for (int k = 1 + ((colour + i + j + 1) & 1); k < nz - 1; k += 2) {
+                        const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                        const double o = field[a];
+                        const double nb = field[a - static_cast<int64_t>(ny) * nz] + field[a + static_cast<int64_t>(ny) * nz] +
+                                          field[a - nz] + field[a + nz] + field[a - 1] + field[a + 1];
+                        const double gs = nb / (6.0 + h * U[a] / (michaelis_k + o));
+                        field[a] = std::max((1.0 - omega) * o + omega * gs, 0.0);
+                    }
+        }
+        ++sweeps;
+        if (sweeps % 20 != 0) continue;
+        double res = 0.0;
+#pragma omp parallel for reduction(max : res) schedule(static)
+        for (int i = 1; i < nx - 1; ++i)
+            for (int j = 1; j < ny - 1; ++j)
+                for (int k = 1; k < nz - 1; ++k) {
+                    if (!interior(i, j, k)) continue;
+                    const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                    const double o = field[a];
+                    const double nb = field[a - static_cast<int64_t>(ny) * nz] + field[a + static_cast<int64_t>(ny) * nz] +
+                                      field[a - nz] + field[a + nz] + field[a - 1] + field[a + 1];
+                    const double r = nb - (6.0 + h * U[a] / (michaelis_k + o)) * o;
+                    // nodes at the clamp (o = 0 with a negative unclamped update) are settled
+                    if (o == 0.0 && r <= 0.0) continue;
+                    res = std::max(res, std::fabs(r) / std::max(6.0 * o, ref));
+                }
+        if (res < tolerance) break;
+    }
+    return sweeps;
+}
+
 }  // extern "C"

@@ -238,6 +238,12 @@ SIGNATURES: dict[str, list] = {
     "wbc_batch_deposit": [POINTER(BatchC), _P, _P],
     "wbc_batch_sample": [POINTER(BatchC), _P, _P],
     "wbc_batch_lifecycle": [POINTER(BatchC), _P, _P, _P],
+    "wbc_deposit_weighted": [POINTER(GridGeometryC), _I, _P, _P, _P, _P],
+    "wbc_weighted_convert": [c_int64, _P, _F, _P, _I, _P],
+    "wbc_adjoint_contact": [POINTER(NeighborGridC), _I, _F, _F, _F, _P, _P, _P, _P],
+    "wbc_adjoint_field_solve": [POINTER(SorParamsC), _P, _P, _P, _P, _P, _I, _I, _F, _P, _P, _P,
+                                POINTER(SorReportC), _P],
+    "wbc_adjoint_cells": [POINTER(GridGeometryC), _I, _P, _P, _P, _F, _P, _P, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
     "wbc_division_scan_noalloc": [_I, _P, _P, _P, _P],
