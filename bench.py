@@ -58,6 +58,12 @@ WORKLOADS = {
     # 15 spheroids: boundary O2 {10, 20, 38, 60, 100} mmHg x 3 seeds, cell counts log-uniform in
     # [2,000, 200,000] at the 1M-cell workload's density, cubic grids of 41-121 nodes (odd, growing
     # with the count) over a box of 2.5 spheroid radii; advanced as one batch against 15 plain runs.
+    # Adjoint calibration: 100,000 cells in a 500 um ball, 81^3 O2 grid at 15 um, K = 64 contact
+    # steps, per-cell Vmax log-normal (sigma 0.3), loss = squared L2 error of the steady field +
+    # of the cells' distances from their centroid against the model at parameters perturbed by up
+    # to +-20% (seeded).
+    "adjoint_100k_81": dict(adjoint=True, cells=100_000, ball_um=500.0, nodes=81, dx_um=15.0, steps=64,
+                            boundary=38.0, vmax_sigma=0.3),
     "batched_sweep_15": dict(batched=True, boundaries=(10.0, 20.0, 38.0, 60.0, 100.0), seeds=(0, 1, 2),
                              cells_lo=2_000, cells_hi=200_000, nodes_lo=41, nodes_hi=121, box_over_radius=2.5),
 }
@@ -707,6 +713,119 @@ def run_batched(args) -> dict:
     }
 
 
+# ---- adjoint (config D) ----------------------------------------------------------------------------------
+def run_adjoint(args) -> dict:
+    import torch
+
+    from warpbiocell_gb300 import _lib
+    from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball
+    from warpbiocell_gb300.cells.mechanics import ContactParams
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+    from warpbiocell_gb300.simulation.adjoint import AdjointSpheroid, CoupledSteadyState
+
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    torch.cuda.set_device(dev)
+    w = WORKLOADS[args.workload]
+    rng = np.random.default_rng(args.seed + 11)
+    pos = uniform_ball(w["cells"], w["ball_um"], seed=args.seed)
+    radii = clipped_normal_radii(w["cells"], 8.0, 0.8, 6.0, 10.0, seed=args.seed + 1)
+    half = 0.5 * (w["nodes"] - 1) * w["dx_um"]
+    geom = GridGeometry(origin=(-half,) * 3, dx=w["dx_um"], shape=(w["nodes"],) * 3)
+    contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0)
+    model = AdjointSpheroid(torch.from_numpy(pos), torch.from_numpy(radii), geom, w["steps"], DT, contact=contact,
+                            adjoint_tolerance=1e-6, device=dev)
+    vmax = (VMAX * np.exp(w["vmax_sigma"] * rng.standard_normal(w["cells"]))).astype(np.float32)
+    theta = dict(km=KM, diffusion=DIFFUSION, boundary=w["boundary"], stiffness=1.0)
+    pert = {k: v * (1.0 + 0.2 * (2 * rng.random() - 1)) for k, v in theta.items()}
+    vmax_t = torch.from_numpy((vmax * (1.0 + 0.2 * (2 * rng.random(vmax.size) - 1))).astype(np.float32)).to(dev)
+    with torch.no_grad():
+        u_t, x_t = model.forward(vmax_t, pert["km"], pert["diffusion"], pert["boundary"], pert["stiffness"])
+    u_t = u_t.double()
+    rho_t = (x_t.double() - x_t.double().mean(dim=0)).norm(dim=1)
+    v0 = torch.from_numpy(vmax).to(dev)
+
+    def loss_of(u, x):
+        xd = x.double()
+        return ((u.double() - u_t) ** 2).sum() + (((xd - xd.mean(dim=0)).norm(dim=1) - rho_t) ** 2).sum()
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return out, e0.elapsed_time(e1)
+
+    fwd_ms, bwd_ms = [], []
+    launches0 = _lib.launch_count()
+    for rep in range(max(1, args.warmup) + max(1, args.steps)):
+        v = v0.clone().requires_grad_(True)
+        scal = {k: torch.tensor(val, dtype=torch.float64, requires_grad=True) for k, val in theta.items()}
+        (u, x), f_ms = timed(lambda: CoupledSteadyState.apply(v, scal["km"], scal["diffusion"], scal["boundary"],
+                                                                scal["stiffness"], model))
+        loss = loss_of(u, x)
+        _, b_ms = timed(loss.backward)
+        if rep >= max(1, args.warmup):
+            fwd_ms.append(f_ms)
+            bwd_ms.append(b_ms)
+    launches = _lib.launch_count() - launches0
+    grads = {k: float(t.grad) for k, t in scal.items()}
+    grad_v = v.grad.double().cpu().numpy()
+    result = {
+        "metric": "adjoint backward time / forward time (100k cells, 81^3 O2, K=64 contact steps)",
+        "value": round(float(np.median(bwd_ms)) / float(np.median(fwd_ms)), 3), "unit": "x forward",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 forward, fp32 adjoint with fp64 scalar sums",
+        "data": "synthetic (seeded uniform ball, clipped-normal radii, log-normal Vmax)",
+        "config": {"workload": args.workload, **w},
+        "forward_ms": round(float(np.median(fwd_ms)), 3), "backward_ms": round(float(np.median(bwd_ms)), 3),
+        "forward_sweeps": model.last_forward_sweeps, "adjoint_sweeps": model.last_adjoint_sweeps,
+        "adjoint_converged": model.last_adjoint_converged,
+        "gpu_launches": int(launches),
+        "gradients": {**grads, "vmax_norm": float(np.linalg.norm(grad_v))},
+    }
+    if not args.skip_cpu:
+        # Central differences of the FP64 re-run (oracle, double contact steps / exact deposit /
+        # double SOR to 1e-13) on the scalar parameters and one random Vmax direction.
+        sys.path.insert(0, str(ROOT))
+        from oracle import oracle as orc
+
+        orc.set_threads(os.cpu_count() or 1)
+        u64, rho64 = u_t.cpu().numpy(), rho_t.cpu().numpy()
+        og = orc.Geometry(geom.origin, geom.dx, geom.shape)
+
+        def loss64(vm, km, diffusion, boundary, stiffness):
+            field, p, _ = orc.adjoint_forward_f64(pos, radii, vm, og, w["steps"], DT, stiffness, 20.0, 20.0, 128,
+                                                  diffusion, km, boundary)
+            return float(((field - u64) ** 2).sum() + ((np.linalg.norm(p - p.mean(axis=0), axis=1) - rho64) ** 2).sum())
+
+        vm64 = vmax.astype(np.float64)
+        rel = 1e-4
+        errors = {}
+        t0 = time.perf_counter()
+        for name in ("km", "stiffness"):
+            h = rel * theta[name]
+            hi, lo = dict(theta), dict(theta)
+            hi[name] += h
+            lo[name] -= h
+            fd = (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * h)
+            errors[name] = abs(grads[name] - fd) / abs(fd)
+        d = np.where(rng.random(vmax.size) < 0.5, -1.0, 1.0)
+        fd = (loss64(vm64 * (1 + rel * d), **theta) - loss64(vm64 * (1 - rel * d), **theta)) / (2 * rel)
+        errors["vmax_direction"] = abs(float((grad_v * vm64 * d).sum()) - fd) / abs(fd)
+        # the stiffness derivative at two more step sizes (how well the difference itself settles)
+        for r in (1e-3, 1e-5):
+            hi, lo = dict(theta), dict(theta)
+            hi["stiffness"] *= 1 + r
+            lo["stiffness"] *= 1 - r
+            fd = (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * r * theta["stiffness"])
+            errors[f"stiffness_h{r:g}"] = abs(grads["stiffness"] - fd) / abs(fd)
+        result["fp64_central_difference_rel_error"] = {k: float(f"{e:.3g}") for k, e in errors.items()}
+        result["fp64_check_s"] = round(time.perf_counter() - t0, 1)
+    return result
+
+
 def main() -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--gpus", type=int, default=1)
@@ -732,6 +851,10 @@ def main() -> None:
     if WORKLOADS[args.workload].get("batched"):
         if rank == 0:
             print(json.dumps(run_batched(args)))
+        return
+    if WORKLOADS[args.workload].get("adjoint"):
+        if rank == 0:
+            print(json.dumps(run_adjoint(args)))
         return
 
     if world > 1:

@@ -337,10 +337,10 @@ int wbc_weighted_convert(int64_t nodes, int64_t* accumulator, float factor, floa
 int wbc_adjoint_contact(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
                         const float* lambda_in, float* lambda_out, float* vdot, void* stream);
 /* Field adjoint (Dirichlet faces): red-black SOR on (6 + h kappa) mu - sum_nb mu = grad_u from mu's
- * current values (start from zeros), kappa = U K / (K + u)^2, until max |residual| < tolerance
- * (checked every check_every sweeps, synchronising); then phi = mu u / (K + u) and
- * sums = {dL/dK, D dL/dD, dL/dO_b} (device doubles). kappa, phi: float[nodes] scratch/outputs;
- * residual_bits: one device uint32. */
+ * current values (start from zeros), kappa = U K / (K + u)^2, until max |residual| is below
+ * tolerance x max(6 |mu|, |grad_u|) (checked every check_every sweeps, synchronising); then
+ * phi = mu u / (K + u) and sums = {dL/dK, D dL/dD, dL/dO_b} (device doubles). kappa, phi:
+ * float[nodes] scratch/outputs; residual_bits: two device uint32. */
 int wbc_adjoint_field_solve(const wbc_sor_params* p, const float* u, const float* U, const float* grad_u, float* mu,
                             float* kappa, int32_t check_every, int32_t max_sweeps, float tolerance, float* phi,
                             double* sums, uint32_t* residual_bits, wbc_sor_report* report, void* stream);

@@ -25,7 +25,7 @@ def _problem(n=1200, ball=100.0, nodes=25, dx=10.0, steps=9, seed=5):
     geom = GridGeometry(origin=(-half, -half, -half), dx=dx, shape=(nodes,) * 3)
     contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0)
     model = AdjointSpheroid(torch.from_numpy(pos), torch.from_numpy(radii), geom, steps, 0.1, contact=contact,
-                            adjoint_tolerance=1e-7, device=DEV)
+                            adjoint_tolerance=1e-6, device=DEV)
     rng = np.random.default_rng(seed + 2)
     vmax = (VMAX * np.exp(0.3 * rng.standard_normal(n))).astype(np.float32)
     theta = dict(km=1.0, diffusion=7.2e6, boundary=60.0, stiffness=1.0)

@@ -187,12 +187,13 @@ __global__ void k_adjoint_colour(wbc_sor_params p, int colour, const float* __re
     mu[a] = (1.0f - p.omega) * mu[a] + p.omega * gs;
 }
 
-// max_a |sum_nb mu + g_a - (6 + h kappa_a) mu_a| as float bits (non-negative: integer max works).
+// out[0] = max_a |sum_nb mu + g_a - (6 + h kappa_a) mu_a|, out[1] = max_a max(6 |mu_a|, |g_a|), as
+// float bits (non-negative: integer max works).
 __global__ void k_adjoint_residual(wbc_sor_params p, const float* __restrict__ kappa, const float* __restrict__ g,
                                    const float* __restrict__ mu, unsigned int* __restrict__ out) {
     const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
     const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    unsigned int bits = 0u;
+    unsigned int bits = 0u, scale = 0u;
     if (a < nodes) {
         const float ka = kappa[a];
         if (ka >= 0.0f) {
@@ -203,11 +204,18 @@ __global__ void k_adjoint_residual(wbc_sor_params p, const float* __restrict__ k
             const float nb = mu_at(mu, p, i - 1, j, k) + mu_at(mu, p, i + 1, j, k) + mu_at(mu, p, i, j - 1, k) +
                              mu_at(mu, p, i, j + 1, k) + mu_at(mu, p, i, j, k - 1) + mu_at(mu, p, i, j, k + 1);
             bits = __float_as_uint(fabsf(nb + g[a] - (6.0f + p.dx2_over_D * ka) * mu[a]));
+            scale = __float_as_uint(fmaxf(6.0f * fabsf(mu[a]), fabsf(g[a])));
         }
     }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
-    if ((threadIdx.x & 31) == 0) atomicMax(out, bits);
+    for (int d = 16; d > 0; d >>= 1) {
+        bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
+        scale = max(scale, __shfl_xor_sync(0xffffffffu, scale, d));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(out, bits);
+        atomicMax(out + 1, scale);
+    }
 }
 
 // phi_a = mu_a u_a / (K + u_a) and the scalar sums: [0] dL/dK, [1] D dL/dD, [2] dL/dO_b.
@@ -368,18 +376,21 @@ int wbc_adjoint_field_solve(const wbc_sor_params* p, const float* u, const float
             k_adjoint_colour<<<grid_for(half), kThreads, 0, s>>>(*p, 0, kappa, grad_u, mu);
             k_adjoint_colour<<<grid_for(half), kThreads, 0, s>>>(*p, 1, kappa, grad_u, mu);
         }
-        cudaError_t err = cudaMemsetAsync(residual_bits, 0, sizeof(uint32_t), s);
+        cudaError_t err = cudaMemsetAsync(residual_bits, 0, 2 * sizeof(uint32_t), s);
         k_adjoint_residual<<<grid_for(nodes), kThreads, 0, s>>>(*p, kappa, grad_u, mu, residual_bits);
         launches += 2 * chunk + 1;
-        uint32_t bits = 0;
-        if (err == cudaSuccess) err = cudaMemcpyAsync(&bits, residual_bits, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        uint32_t bits[2] = {0, 0};
+        if (err == cudaSuccess) err = cudaMemcpyAsync(bits, residual_bits, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         if (err == cudaSuccess) err = cudaStreamSynchronize(s);
         if (err != cudaSuccess) {
             set_error("wbc_adjoint_field_solve: reading the residual", err);
             return WBC_ERR_CUDA;
         }
         sweeps += chunk;
-        std::memcpy(&residual, &bits, sizeof(float));
+        float r_abs, r_scale;
+        std::memcpy(&r_abs, &bits[0], sizeof(float));
+        std::memcpy(&r_scale, &bits[1], sizeof(float));
+        residual = r_scale > 0.0f ? r_abs / r_scale : 0.0f;
         if (residual < tolerance) break;
     }
     cudaError_t err = cudaMemsetAsync(sums, 0, 3 * sizeof(double), s);

@@ -41,6 +41,8 @@ class AdjointSpheroid:
                  settings: SolverSettings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=20000,
                                                            check_every=20),
                  adjoint_tolerance: float = 1e-6, device=None):
+        """``adjoint_tolerance`` bounds the field adjoint's max residual relative to
+        max(6 |mu|, |dL/du|)."""
         self.device = _lib.resolve_device(device if device is not None else positions.device)
         self.x0 = positions.detach().to(self.device, torch.float32).contiguous()
         self.radii = radii.detach().to(self.device, torch.float32).contiguous()
@@ -122,13 +124,13 @@ class AdjointSpheroid:
         kappa = torch.empty_like(mu)
         phi = torch.empty_like(mu)
         sums = torch.zeros(3, dtype=torch.float64, device=self.device)
-        bits = torch.zeros(1, dtype=torch.int32, device=self.device)
+        bits = torch.zeros(2, dtype=torch.int32, device=self.device)
         report = _lib.SorReportC()
-        scale = float(g.abs().max().item()) or 1.0
         _lib.call("wbc_adjoint_field_solve", ctypes.byref(params), _lib.ptr(field.values), _lib.ptr(sv["uptake"]),
                   _lib.ptr(g), _lib.ptr(mu), _lib.ptr(kappa), int(self.settings.check_every),
-                  int(self.settings.max_sweeps), self.adjoint_tolerance * scale, _lib.ptr(phi), _lib.ptr(sums),
+                  int(self.settings.max_sweeps), self.adjoint_tolerance, _lib.ptr(phi), _lib.ptr(sums),
                   _lib.ptr(bits), ctypes.byref(report), st)
+        self.last_adjoint_converged = bool(report.converged)
         self.last_adjoint_sweeps = int(report.sweeps)
         d_km, d_diffusion_times_d, d_boundary = sums.tolist()
         h = params.dx2_over_D
