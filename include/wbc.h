@@ -108,6 +108,24 @@ typedef struct wbc_grid_geometry {
     float inv_dx;
 } wbc_grid_geometry;
 
+/* ---- tissue region ------------------------------------------------------------------------------
+ * A signed-distance field on its own grid (negative inside) and its node gradient. */
+typedef struct wbc_tissue_region {
+    wbc_grid_geometry geom;
+    const float* sdf;             /* float[nodes]                                                    */
+    const float* gradient;        /* float[nodes][3] (x, y, z)                                       */
+    float wall_rate;              /* ContactParams.wall_rate [1/h]                                   */
+} wbc_tissue_region;
+
+/* wbc_contact_substep plus the region's confinement push before the Euler step
+ * (cells/mechanics.py:75-110 with kernels/geometry_kernels.py:59-79). */
+int wbc_contact_substep_region(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                               const wbc_tissue_region* region, float* position, float* velocity,
+                               int32_t* neighbor_count, void* stream);
+/* Trilinear signed distance at each cell, positions clamped to the grid
+ * (kernels/geometry_kernels.py:46-56, geometry/region.py sample_at). */
+int wbc_sample_sdf(const wbc_tissue_region* region, int32_t n, const float* position, float* out, void* stream);
+
 /* accumulator[state][node] += int64(w * 2^24 + 0.5) for the 8 trilinear corners of each living
  * or dead cell with 0 <= state < 4; cells outside the trilinear support are skipped.
  * Replaces kernels/field_kernels.py:78-116 (deposit_trilinear). The accumulator is not cleared. */

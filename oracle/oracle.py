@@ -538,3 +538,23 @@ def adjoint_forward_f64(pos0: np.ndarray, radius: np.ndarray, vmax: np.ndarray, 
         c_double(geom.dx), c_double(diffusion), c_double(michaelis_k), c_double(boundary), c_double(omega),
         c_double(tolerance), c_int32(max_sweeps), P(field))
     return field, pos, int(sweeps)
+
+
+def contact_substep_region(pos: np.ndarray, radius: np.ndarray, cell_size: float, dim: int, query_radius: float,
+                           rate: float, dt: float, region_geom: Geometry, sdf: np.ndarray, gradient: np.ndarray,
+                           wall_rate: float):
+    """float32 contact substep with the tissue-region push, in place on ``pos``."""
+    assert pos.dtype == np.float32
+    n = pos.shape[0]
+    nc = np.zeros(n, dtype=np.int32)
+    vel = np.zeros((n, 3), dtype=np.float32)
+    r = np.ascontiguousarray(radius, dtype=np.float32)
+    s = np.ascontiguousarray(sdf, dtype=np.float32)
+    g = np.ascontiguousarray(gradient, dtype=np.float32)
+    nx, ny, nz = region_geom.shape
+    o = region_geom.origin
+    lib().orc_contact_substep_region_f32(c_int32(n), P(pos), P(r), f32(cell_size), c_int32(dim), f32(query_radius),
+                                         f32(rate), f32(dt), c_int32(nx), c_int32(ny), c_int32(nz), f32(o[0]),
+                                         f32(o[1]), f32(o[2]), f32(1.0 / region_geom.dx), P(s), P(g), f32(wall_rate),
+                                         P(vel), P(nc))
+    return vel, nc

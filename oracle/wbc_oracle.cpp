@@ -18,6 +18,7 @@
 // (integer atomics, per-cell outputs, red-black colours).
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 #include <cstdint>
 #include <cstring>
 #include <vector>
@@ -183,11 +184,54 @@ inline T tsqrt(T v) {
     return std::sqrt(v);
 }
 
+// Tissue region for the confinement push (kernels/geometry_kernels.py:14-79): signed distance and
+// node gradient (x, y, z per node) on a grid, sampled trilinearly with positions clamped to it.
+struct Region {
+    int32_t nx, ny, nz;
+    float ox, oy, oz, inv_dx;
+    const float* sdf;
+    const float* gradient;
+    float wall_rate;
+};
+
+inline float region_sample(const Region& R, const float* f, int stride, int i0, int j0, int k0, float fx, float fy,
+                           float fz) {
+    auto at = [&](int i, int j, int k) { return f[((static_cast<int64_t>(i) * R.ny + j) * R.nz + k) * stride]; };
+    const float c00 = at(i0, j0, k0) * (1.0f - fx) + at(i0 + 1, j0, k0) * fx;
+    const float c10 = at(i0, j0 + 1, k0) * (1.0f - fx) + at(i0 + 1, j0 + 1, k0) * fx;
+    const float c01 = at(i0, j0, k0 + 1) * (1.0f - fx) + at(i0 + 1, j0, k0 + 1) * fx;
+    const float c11 = at(i0, j0 + 1, k0 + 1) * (1.0f - fx) + at(i0 + 1, j0 + 1, k0 + 1) * fx;
+    return (c00 * (1.0f - fy) + c10 * fy) * (1.0f - fz) + (c01 * (1.0f - fy) + c11 * fy) * fz;
+}
+
+inline void confine(const Region& R, float x, float y, float z, float radius, float& vx, float& vy, float& vz) {
+    const float ux = std::min(std::max((x - R.ox) * R.inv_dx, 0.0f), static_cast<float>(R.nx - 1));
+    const float uy = std::min(std::max((y - R.oy) * R.inv_dx, 0.0f), static_cast<float>(R.ny - 1));
+    const float uz = std::min(std::max((z - R.oz) * R.inv_dx, 0.0f), static_cast<float>(R.nz - 1));
+    const int i0 = std::min(static_cast<int>(std::floor(ux)), R.nx - 2);
+    const int j0 = std::min(static_cast<int>(std::floor(uy)), R.ny - 2);
+    const int k0 = std::min(static_cast<int>(std::floor(uz)), R.nz - 2);
+    const float fx = ux - static_cast<float>(i0), fy = uy - static_cast<float>(j0), fz = uz - static_cast<float>(k0);
+    const float penetration = region_sample(R, R.sdf, 1, i0, j0, k0, fx, fy, fz) + radius;
+    if (penetration <= 0.0f) return;
+    const float nx = region_sample(R, R.gradient, 3, i0, j0, k0, fx, fy, fz);
+    const float ny = region_sample(R, R.gradient + 1, 3, i0, j0, k0, fx, fy, fz);
+    const float nz = region_sample(R, R.gradient + 2, 3, i0, j0, k0, fx, fy, fz);
+    const float length = std::sqrt(nx * nx + ny * ny + nz * nz);
+    if (length < 1.0e-8f) return;
+    const float s = R.wall_rate * penetration / length;
+    vx = vx - s * nx;
+    vy = vy - s * ny;
+    vz = vz - s * nz;
+}
+
 // contact_velocities + integrate_positions (kernels/mechanics_kernels.py:26-67), fused: every
-// velocity is computed from the positions at the start of the substep.
+// velocity is computed from the positions at the start of the substep; with a region (float
+// only), the confinement push of cells/mechanics.py:95-102 before the Euler step.
 template <typename T>
 void contact_substep(int n, T* pos, const T* radius, const float* bin_pos, float cell_size, int dim,
-                     T query_radius, T rate, T dt, T* velocity, int32_t* neighbor_count) {
+                     T query_radius, T rate, T dt, T* velocity, int32_t* neighbor_count,
+                     const Region* region = nullptr) {
     Buckets bk;
     bk.build(n, bin_pos, cell_size, dim);
     std::vector<T> x0(pos, pos + 3 * static_cast<size_t>(n));
@@ -221,6 +265,9 @@ void contact_substep(int n, T* pos, const T* radius, const float* bin_pos, float
                         }
                     }
                 }
+        if constexpr (std::is_same<T, float>::value) {
+            if (region) confine(*region, xi, yi, zi, ri, vx, vy, vz);
+        }
         velocity[3 * i] = vx;
         velocity[3 * i + 1] = vy;
         velocity[3 * i + 2] = vz;
@@ -424,6 +471,16 @@ void orc_contact_substep_f32(int32_t n, float* pos, const float* radius, float c
     std::vector<float> bin_pos(pos, pos + 3 * static_cast<size_t>(n));
     contact_substep<float>(n, pos, radius, bin_pos.data(), cell_size, dim, query_radius, rate, dt, velocity,
                            neighbor_count);
+}
+
+void orc_contact_substep_region_f32(int32_t n, float* pos, const float* radius, float cell_size, int32_t dim,
+                                    float query_radius, float rate, float dt, int32_t rnx, int32_t rny, int32_t rnz,
+                                    float rox, float roy, float roz, float rinv_dx, const float* sdf,
+                                    const float* gradient, float wall_rate, float* velocity, int32_t* neighbor_count) {
+    const Region R{rnx, rny, rnz, rox, roy, roz, rinv_dx, sdf, gradient, wall_rate};
+    std::vector<float> bin_pos(pos, pos + 3 * static_cast<size_t>(n));
+    contact_substep<float>(n, pos, radius, bin_pos.data(), cell_size, dim, query_radius, rate, dt, velocity,
+                           neighbor_count, &R);
 }
 
 // FP64 re-run: same pairs and order (buckets from the float32 image of the positions).

@@ -56,6 +56,15 @@ class GridGeometryC(ctypes.Structure):
     ]
 
 
+class TissueRegionC(ctypes.Structure):
+    _fields_ = [
+        ("geom", GridGeometryC),
+        ("sdf", c_void_p),
+        ("gradient", c_void_p),
+        ("wall_rate", c_float),
+    ]
+
+
 class SorParamsC(ctypes.Structure):
     _fields_ = [
         ("nx", c_int32),
@@ -244,6 +253,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_adjoint_field_solve": [POINTER(SorParamsC), _P, _P, _P, _P, _P, _I, _I, _F, _P, _P, _P,
                                 POINTER(SorReportC), _P],
     "wbc_adjoint_cells": [POINTER(GridGeometryC), _I, _P, _P, _P, _F, _P, _P, _P],
+    "wbc_contact_substep_region": [POINTER(NeighborGridC), _I, _F, _F, _F, POINTER(TissueRegionC), _P, _P, _P, _P],
+    "wbc_sample_sdf": [POINTER(TissueRegionC), _I, _P, _P, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_division_scan": [_I, _P, _P, _P, _P, c_size_t, _P],
     "wbc_division_scan_noalloc": [_I, _P, _P, _P, _P],

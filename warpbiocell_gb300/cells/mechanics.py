@@ -67,16 +67,23 @@ def make_neighbor_grid(params: ContactParams, device, dim: int = 128) -> Neighbo
 
 def contact_substep(population, grid: NeighborGrid, params: ContactParams, dt: float, region=None) -> None:
     """One explicit substep: rebuild the grid, gather contact velocities, move the cells."""
-    if region is not None:
-        raise NotImplementedError("tissue-region confinement is not part of this build")
     n = population.count
     if n == 0:
         return
     grid.build(population)
     with profiling.stage("contact"):
-        _lib.call("wbc_contact_substep", ctypes.byref(grid.struct), n, float(params.query_radius), float(params.rate),
-                  float(dt), _lib.ptr(population.position), _lib.ptr(population.velocity),
-                  _lib.ptr(population.neighbor_count), _lib.stream(population.device))
+        if region is None:
+            _lib.call("wbc_contact_substep", ctypes.byref(grid.struct), n, float(params.query_radius),
+                      float(params.rate), float(dt), _lib.ptr(population.position), _lib.ptr(population.velocity),
+                      _lib.ptr(population.neighbor_count), _lib.stream(population.device))
+        else:
+            if region.device != population.device:
+                raise RuntimeError("population and tissue region must live on the same device")
+            native = region.native(params.wall_rate)
+            _lib.call("wbc_contact_substep_region", ctypes.byref(grid.struct), n, float(params.query_radius),
+                      float(params.rate), float(dt), ctypes.byref(native), _lib.ptr(population.position),
+                      _lib.ptr(population.velocity), _lib.ptr(population.neighbor_count),
+                      _lib.stream(population.device))
 
 
 def relax_contacts(population, grid: NeighborGrid, params: ContactParams, dt: float, substeps: int, region=None) -> None:

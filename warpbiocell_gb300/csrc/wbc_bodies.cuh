@@ -58,13 +58,62 @@ __device__ __forceinline__ void bin_order_cell(int i, const float* __restrict__ 
     sorted_xyzr[s + rank] = make_float4(p[0], p[1], p[2], radius[i]);
 }
 
-// Sorted slot t: neighbour count, overlap-repulsion velocity and the Euler step of its cell.
+// Tissue-region confinement (kernels/geometry_kernels.py:59-79): with phi the trilinear signed
+// distance at the cell (negative inside, position clamped to the grid), p = phi + r; if p > 0 the
+// velocity loses wall_rate * p / |n| * n, n the trilinear node gradient of the distance.
+__device__ __forceinline__ float region_sample(const wbc_grid_geometry& g, const float* __restrict__ f, int stride,
+                                              int i0, int j0, int k0, float fx, float fy, float fz) {
+    const int64_t sy = g.nz, sx = static_cast<int64_t>(g.ny) * g.nz;
+    const int64_t b = i0 * sx + j0 * sy + k0;
+    auto at = [&](int64_t node) { return f[node * stride]; };
+    const float c00 = at(b) * (1.0f - fx) + at(b + sx) * fx;
+    const float c10 = at(b + sy) * (1.0f - fx) + at(b + sx + sy) * fx;
+    const float c01 = at(b + 1) * (1.0f - fx) + at(b + sx + 1) * fx;
+    const float c11 = at(b + sy + 1) * (1.0f - fx) + at(b + sx + sy + 1) * fx;
+    return (c00 * (1.0f - fy) + c10 * fy) * (1.0f - fz) + (c01 * (1.0f - fy) + c11 * fy) * fz;
+}
+
+__device__ __forceinline__ void region_cell(const wbc_grid_geometry& g, float x, float y, float z, int& i0, int& j0,
+                                            int& k0, float& fx, float& fy, float& fz) {
+    const float ux = fminf(fmaxf((x - g.origin_x) * g.inv_dx, 0.0f), static_cast<float>(g.nx - 1));
+    const float uy = fminf(fmaxf((y - g.origin_y) * g.inv_dx, 0.0f), static_cast<float>(g.ny - 1));
+    const float uz = fminf(fmaxf((z - g.origin_z) * g.inv_dx, 0.0f), static_cast<float>(g.nz - 1));
+    i0 = min(static_cast<int>(floorf(ux)), g.nx - 2);
+    j0 = min(static_cast<int>(floorf(uy)), g.ny - 2);
+    k0 = min(static_cast<int>(floorf(uz)), g.nz - 2);
+    fx = ux - static_cast<float>(i0);
+    fy = uy - static_cast<float>(j0);
+    fz = uz - static_cast<float>(k0);
+}
+
+__device__ __forceinline__ void confine(const wbc_tissue_region& R, float x, float y, float z, float radius,
+                                        float& vx, float& vy, float& vz) {
+    int i0, j0, k0;
+    float fx, fy, fz;
+    region_cell(R.geom, x, y, z, i0, j0, k0, fx, fy, fz);
+    const float penetration = region_sample(R.geom, R.sdf, 1, i0, j0, k0, fx, fy, fz) + radius;
+    if (penetration <= 0.0f) return;
+    const float nx = region_sample(R.geom, R.gradient, 3, i0, j0, k0, fx, fy, fz);
+    const float ny = region_sample(R.geom, R.gradient + 1, 3, i0, j0, k0, fx, fy, fz);
+    const float nz = region_sample(R.geom, R.gradient + 2, 3, i0, j0, k0, fx, fy, fz);
+    const float length = sqrtf(nx * nx + ny * ny + nz * nz);
+    if (length < 1.0e-8f) return;
+    const float s = R.wall_rate * penetration / length;
+    vx = vx - s * nx;
+    vy = vy - s * ny;
+    vz = vz - s * nz;
+}
+
+// Sorted slot t: neighbour count, overlap-repulsion velocity (plus the region's push when REGION)
+// and the Euler step of its cell.
+template <bool REGION = false>
 __device__ __forceinline__ void contact_slot(BucketMap map, int t, const int32_t* __restrict__ bucket_start,
                                              const int32_t* __restrict__ bucket_count,
                                              const int32_t* __restrict__ sorted_id,
                                              const float4* __restrict__ sorted_xyzr, float query_radius, float rate,
                                              float dt, float* __restrict__ position, float* __restrict__ velocity,
-                                             int32_t* __restrict__ neighbor_count) {
+                                             int32_t* __restrict__ neighbor_count,
+                                             const wbc_tissue_region* region = nullptr) {
     const float4 me = sorted_xyzr[t];
     const int i = sorted_id[t];
     const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
@@ -97,6 +146,7 @@ __device__ __forceinline__ void contact_slot(BucketMap map, int t, const int32_t
             }
         }
     }
+    if (REGION) confine(*region, me.x, me.y, me.z, me.w, vx, vy, vz);
     const int64_t o = 3 * static_cast<int64_t>(i);
     velocity[o + 0] = vx;
     velocity[o + 1] = vy;

@@ -47,16 +47,29 @@ __global__ void k_bin_order(int32_t n, const float* __restrict__ position, const
 }
 
 // One thread per sorted slot t (so a warp works on neighbouring cells and shares buckets).
+template <bool REGION>
 __global__ void __launch_bounds__(256) k_contact(BucketMap map, int32_t n, const int32_t* __restrict__ bucket_start,
                                                  const int32_t* __restrict__ bucket_count,
                                                  const int32_t* __restrict__ sorted_id,
                                                  const float4* __restrict__ sorted_xyzr, float query_radius, float rate,
                                                  float dt, float* __restrict__ position, float* __restrict__ velocity,
-                                                 int32_t* __restrict__ neighbor_count) {
+                                                 int32_t* __restrict__ neighbor_count, wbc_tissue_region region) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n)
-        contact_slot(map, t, bucket_start, bucket_count, sorted_id, sorted_xyzr, query_radius, rate, dt, position,
-                     velocity, neighbor_count);
+        contact_slot<REGION>(map, t, bucket_start, bucket_count, sorted_id, sorted_xyzr, query_radius, rate, dt,
+                             position, velocity, neighbor_count, &region);
+}
+
+// Trilinear signed distance at each cell, positions clamped to the grid (geometry_kernels.py:46-56).
+__global__ void k_sample_sdf(wbc_tissue_region R, int32_t n, const float* __restrict__ position,
+                             float* __restrict__ out) {
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    const float* p = position + 3 * static_cast<int64_t>(c);
+    int i0, j0, k0;
+    float fx, fy, fz;
+    region_cell(R.geom, p[0], p[1], p[2], i0, j0, k0, fx, fy, fz);
+    out[c] = region_sample(R.geom, R.sdf, 1, i0, j0, k0, fx, fy, fz);
 }
 
 static bool grid_ok(const wbc_neighbor_grid* g) {
@@ -104,11 +117,41 @@ int wbc_contact_substep(const wbc_neighbor_grid* grid, int32_t n, float query_ra
         return WBC_ERR_INVALID;
     }
     BucketMap map = make_map(grid->cell_size, grid->dim);
-    k_contact<<<grid_for(n), 256, 0, as_stream(stream)>>>(
+    k_contact<false><<<grid_for(n), 256, 0, as_stream(stream)>>>(
         map, n, grid->bucket_start, grid->bucket_count, grid->sorted_id,
         reinterpret_cast<const float4*>(grid->sorted_xyzr), query_radius, rate, dt, position, velocity,
-        neighbor_count);
+        neighbor_count, wbc_tissue_region{});
     return check_launch("wbc_contact_substep");
+}
+
+static bool region_ok(const wbc_tissue_region* r) {
+    return r && r->sdf && r->gradient && r->geom.nx >= 2 && r->geom.ny >= 2 && r->geom.nz >= 2 && r->wall_rate >= 0.0f;
+}
+
+int wbc_contact_substep_region(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                               const wbc_tissue_region* region, float* position, float* velocity,
+                               int32_t* neighbor_count, void* stream) {
+    if (!grid_ok(grid) || !region_ok(region) || n < 0 || n > grid->capacity ||
+        (n > 0 && (!position || !velocity || !neighbor_count)))
+        return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    if (!(query_radius <= grid->cell_size)) {
+        set_error_msg("wbc_contact_substep_region: query_radius exceeds the grid's cell_size");
+        return WBC_ERR_INVALID;
+    }
+    BucketMap map = make_map(grid->cell_size, grid->dim);
+    k_contact<true><<<grid_for(n), 256, 0, as_stream(stream)>>>(
+        map, n, grid->bucket_start, grid->bucket_count, grid->sorted_id,
+        reinterpret_cast<const float4*>(grid->sorted_xyzr), query_radius, rate, dt, position, velocity,
+        neighbor_count, *region);
+    return check_launch("wbc_contact_substep_region");
+}
+
+int wbc_sample_sdf(const wbc_tissue_region* region, int32_t n, const float* position, float* out, void* stream) {
+    if (!region_ok(region) || n < 0 || (n > 0 && (!position || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_sample_sdf<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(*region, n, position, out);
+    return check_launch("wbc_sample_sdf");
 }
 
 }  // extern "C"
