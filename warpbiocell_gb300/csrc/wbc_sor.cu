@@ -169,7 +169,36 @@ struct Sweep {
     int64_t sx;
     float K, h, omega, one_minus_omega;
     bool zclamp;  // Neumann z faces: the k-neighbours of the end nodes are mirrored
+    bool fast;    // K, h and every coefficient of this tile pass the fixed range tests below
 };
+
+// Operand ranges of the update's two divisions, cu = u / (K + o) and gs = a2 / (6 + h cu), for the
+// fast correctly rounded quotient (div_fast_range: both operands within [2^-60, 2^60], numerator
+// possibly zero). Split into a part fixed for the whole solve and a per-node part:
+//  * fixed: K in [2^-60, 2^57], h in [2^-60, 2^60], and every coefficient u of the tile either
+//    marks a node that is not updated (u < 0), is +-0, or lies in [2^-60, 2^60] with
+//    h u / K <= 2^57;
+//  * per node: the old value o in [+0, 2^58] (as unsigned bits: no negative, -0 or NaN), and the
+//    numerator a2 = +0 or within [2^-60, 2^60].
+// Then K + o lies in [K, 2^59], h cu <= 2^58 (cu <= u / K up to two roundings) so 6 + h cu lies
+// in [6, 2^59], and both quotients are within the normal range. A +-0 coefficient gives cu = +-0
+// and 6 + h cu = 6 either way.
+__device__ __forceinline__ bool solve_constants_in_range(float K, float h) {
+    return K >= 0x1p-60f && K <= 0x1p57f && h >= 0x1p-60f && h <= 0x1p60f;
+}
+
+__device__ __forceinline__ bool coefficient_in_range(float u, float K, float h) {
+    if (!(u >= 0.0f) || u == 0.0f) return true;
+    return u >= 0x1p-60f && u <= 0x1p60f &&
+           static_cast<double>(h) * static_cast<double>(u) <= 0x1p57 * static_cast<double>(K);
+}
+
+__device__ __forceinline__ bool old_value_in_range(float o) { return __float_as_uint(o) <= 0x5c800000u; }  // 2^58
+
+__device__ __forceinline__ bool numerator_in_range(float a2) {
+    const unsigned int b = __float_as_uint(a2);
+    return b == 0u || b - 0x21800000u <= 0x5d800000u - 0x21800000u;  // +0 or [2^-60, 2^60]
+}
 
 // Per (box column, colour) entry of the column table in shared memory:
 // x = offset of entry 0 of the parity the colour updates, y = the same for the other parity,
@@ -201,7 +230,7 @@ __device__ __forceinline__ void load_column(const Sweep& w, const int2* list, in
 // column (pv points at entry lane + kp - 1), with Neumann z faces they are clamped to the column
 // ends (the mirror rule k = -1 -> 1, k = nz -> nz - 2). Every lane computes; only nodes with a
 // coefficient (not a Dirichlet face, a pinned node or past the column end) are written, and the
-// IEEE division replaces the fast one only where an operand is outside its range.
+// IEEE division replaces the fast one only where the range tests above do not hold.
 template <bool HAS_PROD, bool ZCLAMP, int LANES>
 __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
                                             int kp, int last, int64_t gbase, unsigned long long* xrow, int cnt,
@@ -216,7 +245,7 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
         const bool active = du[r] >= 0.0f;
         const float o = po[off];
         const float b1 = w.K + o;
-        float cc = div_rn_fast(du[r], b1);
+        float cc = div_rn_fast_nonneg_zero(du[r], b1);
         float prod = 0.0f;
         if (HAS_PROD) {
             if (active) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
@@ -231,12 +260,15 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
             vhi = pv[off + 1];
         }
         const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
-        const float a2 = nb + w.h * prod;
+        // Without production h * 0 = +0 and nb + 0 = nb except for nb = -0, which the range test
+        // sends to the exact branch below.
+        float a2 = HAS_PROD ? nb + w.h * prod : nb;
         float b2 = 6.0f + w.h * cc;
-        float gs = div_rn_fast(a2, b2);
-        if (active && !(div_fast_range(du[r], b1) && div_fast_range(a2, b2))) {
+        float gs = div_rn_fast_nonneg_zero(a2, b2);
+        if (active && !(w.fast && old_value_in_range(o) && numerator_in_range(a2))) {
             cc = __fdiv_rn(du[r], b1);
             b2 = 6.0f + w.h * cc;
+            a2 = nb + w.h * prod;
             gs = __fdiv_rn(a2, b2);
         }
         const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
@@ -535,7 +567,9 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
         L.mir = base + 4 * nbox;
         L.upd_end = reinterpret_cast<int*>(base + 5 * nbox);
     }
+    __shared__ int s_outside_range;
     if (threadIdx.x < 12) s_counts[threadIdx.x] = 0;
+    if (threadIdx.x == 0) s_outside_range = solve_constants_in_range(w.K, w.h) ? 0 : 1;
     __syncthreads();
     const int box_rows = ai + 2 * H, box_cols = aj + 2 * H;
     auto dist_of = [&](int li, int lj) {
@@ -623,6 +657,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
                 float v = -1.0f;
                 if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
                 a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+                if (!coefficient_in_range(v, w.K, w.h)) s_outside_range = 1;
             }
         }
     }
@@ -646,6 +681,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
     // The ring columns' coefficients (and edge rows) are written by their owners: one global
     // barrier first.
     bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles);
+    w.fast = s_outside_range == 0;  // read after the barrier's __syncthreads
 
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
