@@ -1,0 +1,162 @@
+"""Experiment configuration, the YAML subset reader and sweep specifications (reference:
+tests/test_config.py, tests/test_sweep.py): host logic only, no device."""
+
+import math
+
+import numpy as np
+import pytest
+
+from warpbiocell_gb300.simulation import yaml_subset
+from warpbiocell_gb300.simulation.config import (ConfigError, ExperimentConfig, apply_overrides, config_from_dict,
+                                                 load_config)
+from warpbiocell_gb300.simulation.sweep import SweepSpec, batchable, build_run_config, load_sweep
+from warpbiocell_gb300.metrics.timeseries import onset, onset_summary
+
+CONFIG_TEXT = """\
+name: small_spheroid   # provenance comments travel with the file
+simulation:
+  duration_h: 2.0
+  dt_cells_h: 0.5
+  dt_mechanics_h: 0.05
+  seed: 3
+cells:
+  initial_count: 200
+  max_cells: 5000
+  radius_um: 8.0
+mechanics:
+  stiffness: 10.0
+  damping: 1.0
+  margin_um: 2.0
+lifecycle:
+  division_rate_per_h: 0.2
+  hypoxia_threshold_mmHg: 8.0
+oxygen:
+  diffusion_um2_per_h: 7.2e6     # YAML 1.1 reads this as a string; the loader converts it
+  uptake_state_factors: {hypoxic: 0.5}
+  grid:
+    box_um: 400.0
+    dx_um: 20.0
+  solver: {omega: 1.8, tolerance: 1.0e-5, max_sweeps: 2000, check_every: 10}
+species:
+  - name: glucose
+    unit: mM
+    diffusion_um2_per_h: 2.16e6
+    uptake_max_by_state: {proliferative: 1.2e4, quiescent: 1.2e4, hypoxic: 1.2e4}
+  - name: lactate
+    production_by_state: {hypoxic: 2.4e4}
+    production_source: glucose
+output:
+  metrics_every_h: 0.5
+  figures: false
+"""
+
+
+def test_yaml_subset_reads_block_and_flow_collections():
+    data = yaml_subset.safe_load(CONFIG_TEXT)
+    assert data["name"] == "small_spheroid"
+    assert data["simulation"] == {"duration_h": 2.0, "dt_cells_h": 0.5, "dt_mechanics_h": 0.05, "seed": 3}
+    assert float(data["oxygen"]["diffusion_um2_per_h"]) == 7.2e6
+    assert data["oxygen"]["uptake_state_factors"] == {"hypoxic": 0.5}
+    assert data["oxygen"]["solver"]["max_sweeps"] == 2000
+    assert [s["name"] for s in data["species"]] == ["glucose", "lactate"]
+    assert data["species"][1]["production_source"] == "glucose"
+    assert data["output"]["figures"] is False
+    assert yaml_subset.scalar("[20, 38, 60]") == [20, 38, 60]
+    assert yaml_subset.scalar("null") is None and yaml_subset.scalar("'a: b'") == "a: b"
+    text = yaml_subset.safe_dump({"a": {"b": [1, 2], "c": "x y"}, "d": [{"e": 1}], "f": None})
+    assert yaml_subset.safe_load(text) == {"a": {"b": [1, 2], "c": "x y"}, "d": [{"e": 1}], "f": None}
+
+
+def test_load_config_builds_parameter_objects(tmp_path):
+    path = tmp_path / "c.yaml"
+    path.write_text(CONFIG_TEXT)
+    cfg = load_config(path, overrides=["oxygen.boundary_mmHg=60", "cells.max_cells=6000"])
+    assert cfg.oxygen.boundary_mmHg == 60.0 and cfg.cells.max_cells == 6000
+    assert cfg.oxygen.diffusion_um2_per_h == 7.2e6 and cfg.n_steps == 4
+    assert cfg.has_glucose
+    st = cfg.stepping()
+    assert st.mechanics_substeps == 10
+    contact = cfg.contact_params()
+    assert contact.query_radius == 2 * 8.0 + 2.0 and contact.rate == 10.0
+    lc = cfg.lifecycle_params()
+    assert lc.division_rate == 0.2 and lc.glucose_threshold == 0.0
+    species = cfg.species_params()
+    assert [s.name for s in species] == ["glucose", "lactate"] and species[1].production_source == "glucose"
+    assert cfg.grid_geometry().shape == (21, 21, 21)
+    assert cfg.solver_settings().check_every == 10
+    warnings = cfg.validate()
+    assert isinstance(warnings, list)
+    assert config_from_dict(cfg.to_dict()) == cfg  # round trip through plain dicts
+
+
+def test_config_errors():
+    with pytest.raises(ConfigError, match="unknown keys"):
+        config_from_dict({"cells": {"max_cell": 10}})
+    with pytest.raises(ConfigError, match="expected an integer"):
+        config_from_dict({"cells": {"max_cells": 1.5}})
+    with pytest.raises(ConfigError, match="expected true/false"):
+        config_from_dict({"output": {"figures": "yes please"}})
+    with pytest.raises(ConfigError, match="does not fit"):
+        config_from_dict({"cells": {"initial_count": 100000, "max_cells": 200000}}).validate()
+    with pytest.raises(ConfigError, match="unique"):
+        config_from_dict({"species": [{"name": "glucose"}, {"name": "glucose"}]}).validate()
+    with pytest.raises(ConfigError, match="earlier species"):
+        config_from_dict({"species": [{"name": "lactate", "production_source": "glucose"}]}).validate()
+    with pytest.raises(ConfigError, match="network.enabled"):
+        config_from_dict({"lifecycle": {"phenotype_model": "network"}}).validate()
+    with pytest.raises(ValueError, match="rate\\*dt"):
+        config_from_dict({"mechanics": {"stiffness": 100.0}, "simulation": {"dt_mechanics_h": 0.025}}).validate()
+    with pytest.raises(ConfigError, match="section.key=value"):
+        apply_overrides({}, ["no_equals_sign"])
+    warnings = config_from_dict({"lifecycle": {"division_rate_per_h": 1.0}, "cells": {"max_cells": 2000}}).validate()
+    assert any("exponential growth" in w for w in warnings)
+
+
+def test_geometry_config_validation():
+    cfg = config_from_dict({"geometry": {"enabled": True, "shape": "ellipsoid", "radii_um": [120.0, 90.0, 60.0]},
+                            "cells": {"max_cells": 5000}, "oxygen": {"grid": {"box_um": 400.0}}})
+    cfg.validate()
+    assert cfg.tissue_shape().bounds[1][0] == 120.0
+    with pytest.raises(ConfigError, match="one-voxel margin"):
+        config_from_dict({"geometry": {"enabled": True, "shape": "sphere", "radii_um": [395.0]}}).validate()
+    with pytest.raises(ConfigError, match="sphere, ellipsoid"):
+        config_from_dict({"geometry": {"enabled": True, "shape": "cube"}}).validate()
+
+
+def test_sweep_spec_runs_labels_and_configs(tmp_path):
+    spec_path = tmp_path / "s.yaml"
+    spec_path.write_text("name: o2\nseeds: [0, 1]\noverrides:\n  simulation.duration_h: 1.0\n"
+                         "grid:\n  oxygen.boundary_mmHg: [20, 38.5]\n")
+    spec = load_sweep(spec_path)
+    runs = spec.runs()
+    assert [label for label, _ in runs] == ["boundary_mmHg=20_seed=0", "boundary_mmHg=20_seed=1",
+                                            "boundary_mmHg=38.5_seed=0", "boundary_mmHg=38.5_seed=1"]
+    base = yaml_subset.safe_load(CONFIG_TEXT)
+    base.pop("species")
+    base["oxygen"].pop("uptake_state_factors")
+    configs = [build_run_config(base, spec, label, values) for label, values in runs]
+    assert configs[2].oxygen.boundary_mmHg == 38.5 and configs[1].simulation.seed == 1
+    assert configs[0].simulation.duration_h == 1.0 and configs[3].name == "boundary_mmHg=38.5_seed=1"
+    assert batchable(configs)
+    assert not batchable([config_from_dict(yaml_subset.safe_load(CONFIG_TEXT))])
+    with pytest.raises(ConfigError):
+        SweepSpec(name="x", grid={"oxygen.boundary_mmHg": []})
+    with pytest.raises(ConfigError):
+        SweepSpec(name="")
+
+
+def test_onsets():
+    rows = [{"time_h": 0.0, "hypoxic_cells": 0, "dead_cells": 0, "spheroid_radius_um": 50.0},
+            {"time_h": 1.0, "hypoxic_cells": 3, "dead_cells": 0, "spheroid_radius_um": 60.0},
+            {"time_h": 2.0, "hypoxic_cells": 5, "dead_cells": 1, "spheroid_radius_um": 70.0}]
+    assert onset(rows, "hypoxic_cells") == (1.0, 60.0)
+    s = onset_summary(rows)
+    assert s["necrosis_onset_time_h"] == 2.0 and s["necrosis_onset_radius_um"] == 70.0
+    assert all(math.isnan(v) for v in onset(rows[:1], "dead_cells"))
+
+
+def test_default_config_matches_documented_defaults():
+    cfg = ExperimentConfig()
+    assert cfg.oxygen.boundary_mmHg == 38.0 and cfg.oxygen.solver.max_sweeps == 2000
+    assert np.isclose(cfg.lifecycle.division_rate_per_h, 0.0289)
+    assert cfg.mechanics.wall_rate_per_h == 10.0 and cfg.output.shell_width_um == 20.0
