@@ -224,6 +224,22 @@ __device__ __forceinline__ void load_column(const Sweep& w, const int2* list, in
     for (int r = 0; r < LANES; ++r) du[r] = lane + 32 * r < cnt ? crow[32 * r] : -1.0f;
 }
 
+// The update's quotient with IEEE divisions, for operands outside the fast quotient's range. Out
+// of line, so the rarely taken branch to it stays a branch instead of predicated code in every
+// node's path.
+__device__ __noinline__ float gs_exact(float u, float b1, float nb, float prod, float h) {
+    const float cc = __fdiv_rn(u, b1);
+    const float b2 = 6.0f + h * cc;
+    return __fdiv_rn(nb + h * prod, b2);
+}
+
+// The relative residual of one node with IEEE divisions (out of line, as gs_exact).
+__device__ __noinline__ float residual_exact(float u, float b1, float nb, float prod, float h, float o, float den) {
+    const float cc = __fdiv_rn(u, b1);
+    const float res = nb + h * prod - (6.0f + h * cc) * o;
+    return __fdiv_rn(fabsf(res), den);
+}
+
 // Entries m = lane + 32 r of one parity column: `po` points at entry `lane`, the four lateral
 // neighbours are po -+ si (i) and po -+ M (j). The k-neighbours of entry m are entries m + kp - 1
 // and m + kp of the other parity: with Dirichlet z faces every updated node has both inside the
@@ -265,12 +281,7 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
         float a2 = HAS_PROD ? nb + w.h * prod : nb;
         float b2 = 6.0f + w.h * cc;
         float gs = div_rn_fast_nonneg_zero(a2, b2);
-        if (active && !(w.fast && old_value_in_range(o) && numerator_in_range(a2))) {
-            cc = __fdiv_rn(du[r], b1);
-            b2 = 6.0f + w.h * cc;
-            a2 = nb + w.h * prod;
-            gs = __fdiv_rn(a2, b2);
-        }
+        if (active && !(w.fast && old_value_in_range(o) && numerator_in_range(a2))) gs = gs_exact(du[r], b1, nb, prod, w.h);
         const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
         if (active) po[off] = v;
         // An edge column publishes every entry (unchanged ones too) with this half-sweep's tag.
@@ -362,11 +373,8 @@ __device__ __forceinline__ unsigned int residual_nodes(const SorArgs& a, const S
         float res = nb + w.h * prod - (6.0f + w.h * cc) * o;
         const float den = fmaxf(6.0f * o, a.p.reference);
         float val = div_rn_fast(fabsf(res), den);
-        if (active && !(div_fast_range(du[r], b1) && div_fast_range(fabsf(res), den))) {
-            cc = __fdiv_rn(du[r], b1);
-            res = nb + w.h * prod - (6.0f + w.h * cc) * o;
-            val = __fdiv_rn(fabsf(res), den);
-        }
+        if (active && !(div_fast_range(du[r], b1) && div_fast_range(fabsf(res), den)))
+            val = residual_exact(du[r], b1, nb, prod, w.h, o, den);
         if (active) bits = max(bits, __float_as_uint(val));
     }
     return bits;
