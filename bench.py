@@ -70,8 +70,8 @@ WORKLOADS = {
 
 # DRAM bytes per colour half-sweep of the resident SOR solver at 161^3: one `ncu --set full`
 # capture of k_sor_resident (the benchmark's initial solve, 780 sweeps = 1560 half-sweeps) read
-# and wrote 37.1 MB in total, tile load, coefficient copy and write-back included.
-SOR_DRAM_BYTES_PER_HALF_SWEEP = 23760.0
+# and wrote 36.9 MB in total, tile load, coefficient copy and write-back included.
+SOR_DRAM_BYTES_PER_HALF_SWEEP = 23620.0
 
 DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
 VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
