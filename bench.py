@@ -347,7 +347,58 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     }
     if rank == 0 and not args.skip_cpu:
         result["cpu_baseline"], result["parity_full_size"] = cpu_sample_and_parity(pop, ox, grid, P, step, network)
+    if rank == 0 and not P["species"]:
+        result["scatter_reference"] = scatter_reference(pop, P["geom"])
     return result
+
+
+def scatter_reference(pop, geom) -> dict:
+    """The deposit's scatter alone, done by a library kernel: torch's index_add_ of the same 8 int64
+    fixed-point contributions per cell (corner node indices and weights computed beforehand, not
+    timed) into a [4 states x nodes] int64 array, i.e. the same number of 64-bit atomic adds over
+    the same footprint. A bound for any atomic-scatter deposit, against which k_deposit (which
+    also reads the cells and computes the weights) is compared."""
+    import torch
+
+    n = pop.count
+    pos = pop.position[:n].double()
+    state = pop.cell_state[:n].long()
+    nx, ny, nz = geom.shape
+    u = (pos - torch.tensor(geom.origin, dtype=torch.float64, device=pos.device)) / geom.dx
+    i0 = torch.floor(u).long()
+    f = u - i0.double()
+    ok = ((i0 >= 0).all(1) & (i0[:, 0] + 1 < nx) & (i0[:, 1] + 1 < ny) & (i0[:, 2] + 1 < nz) & (state >= 0) &
+          (state < 4))
+    i0, f, state = i0[ok], f[ok], state[ok]
+    idx, val = [], []
+    nodes = nx * ny * nz
+    for di in (0, 1):
+        for dj in (0, 1):
+            for dk in (0, 1):
+                w = ((f[:, 0] if di else 1 - f[:, 0]) * (f[:, 1] if dj else 1 - f[:, 1]) *
+                     (f[:, 2] if dk else 1 - f[:, 2]))
+                node = ((i0[:, 0] + di) * ny + (i0[:, 1] + dj)) * nz + (i0[:, 2] + dk)
+                idx.append(state * nodes + node)
+                val.append(torch.floor(w * 16777216.0 + 0.5).long())
+    idx = torch.cat(idx)
+    val = torch.cat(val)
+    acc = torch.zeros(4 * nodes, dtype=torch.int64, device=pos.device)
+    times = []
+    for rep in range(4):
+        acc.zero_()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        acc.index_add_(0, idx, val)
+        b.record()
+        torch.cuda.synchronize()
+        if rep:
+            times.append(a.elapsed_time(b))
+    ms = float(np.median(times))
+    return {"what": "torch index_add_ of the same 8 int64 contributions per cell into [4, nodes] int64 "
+                    "(indices precomputed, untimed)", "adds": int(idx.numel()), "us": round(ms * 1e3, 2),
+            "adds_per_s": round(idx.numel() / (ms / 1e3), 1)}
 
 
 def _population_to_oracle(pop):
@@ -475,7 +526,13 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
         moved = stage_bytes("deposit", cells_per_step, nodes, 1) + stage_bytes("convert", cells_per_step, nodes, 1)
         deposit_roofline = {"bound": "hbm", "achieved": round(compulsory / (ms / 1e3) / 1e9, 1), "peak": peak,
                             "unit": "GB/s", "frac": round(compulsory / (ms / 1e3) / 1e9 / peak, 4),
-                            "moved_GBps": round(moved / (ms / 1e3) / 1e9, 1), "us_per_step": round(ms * 1e3, 2)}
+                            "moved_GBps": round(moved / (ms / 1e3) / 1e9, 1), "us_per_step": round(ms * 1e3, 2),
+                            "deposit_us_per_step": round(stages["deposit"]["ms"] / steps * 1e3, 2),
+                            "convert_us_per_step": round(stages["convert"]["ms"] / steps * 1e3, 2)}
+        if "scatter_reference" in r0:
+            ref = dict(r0["scatter_reference"])
+            ref["k_deposit_adds_per_s"] = round(8.0 * cells_per_step / (stages["deposit"]["ms"] / steps / 1e3), 1)
+            deposit_roofline["scatter_reference"] = ref
     breakdown = {k: {"ms_per_step": round(v["ms"] / steps, 4), "launches_per_step": v["launches"] / steps,
                      "GB/s": round(stage_bytes(k, cells_per_step, nodes, int(v["launches"] / steps)) /
                                    (v["ms"] / steps / 1e3) / 1e9, 1) if v["ms"] > 0 and k != "sor" else None}
