@@ -684,18 +684,25 @@ def build_member(spec: dict, P: dict, dev):
     return BatchMember(pop, grid, oxygen, P["lifecycle"], P["contact"])
 
 
-def run_batched(args) -> dict:
+def run_batched(args, rank: int = 0, world: int = 1) -> dict:
+    """The batched sweep; with several ranks the instances are sharded (no collective on the data
+    path): each rank batches its share, balanced by simulation.sweep.partition_runs."""
     import torch
 
     from warpbiocell_gb300 import _lib
     from warpbiocell_gb300.simulation.batch import SpheroidBatch
     from warpbiocell_gb300.simulation.simulator import cell_step
+    from warpbiocell_gb300.simulation.sweep import partition_runs
 
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     w = WORKLOADS[args.workload]
     P = make_params(dict(box_um=800.0, dx_um=20.0, boundary=38.0))
-    specs = batch_specs(w, args.seed)
+    all_specs = batch_specs(w, args.seed)
+    if world > len(all_specs):
+        raise SystemExit(f"{world} ranks for {len(all_specs)} instances: some ranks would have nothing to run")
+    share = partition_runs([float(sp["cells"] + sp["nodes"] ** 3) for sp in all_specs], world)[rank]
+    specs = [all_specs[i] for i in share]
     stepping = P["stepping"]
 
     def timed(fn):
@@ -742,13 +749,34 @@ def run_batched(args) -> dict:
             identical = identical and torch.equal(getattr(a, name)[:n], getattr(b, name)[:n])
         identical = identical and torch.equal(m.oxygen.field.values, p.oxygen.field.values)
     reps = batch.reports()
+    if world > 1:
+        import torch.distributed as dist
+
+        part = {"plain_cells": plain_cells, "plain_ms": plain_ms, "batch_ms": batch_ms, "identical": bool(identical),
+                "counts": counts, "sweeps": [r.sweeps for r in reps], "launches": int(batch.launches_per_step),
+                "share": share}
+        gathered = [None] * world
+        dist.all_gather_object(gathered, part)
+        plain_cells = sum(g["plain_cells"] for g in gathered)
+        plain_ms = max(g["plain_ms"] for g in gathered)
+        batch_ms = max(g["batch_ms"] for g in gathered)
+        identical = all(g["identical"] for g in gathered)
+        order = [i for g in gathered for i in g["share"]]
+        counts = [c for g in gathered for c in g["counts"]]
+        counts = [c for _, c in sorted(zip(order, counts))]
+        last_sweeps = [s_ for _, s_ in sorted(zip(order, [x for g in gathered for x in g["sweeps"]]))]
+        launches = sum(g["launches"] for g in gathered)
+        specs = all_specs
+    else:
+        last_sweeps = [r.sweeps for r in reps]
+        launches = int(batch.launches_per_step)
     steps = max(1, args.steps)
     value = plain_cells / (batch_ms / 1e3)
     plain_value = plain_cells / (plain_ms / 1e3)
     nodes = sum(sp["nodes"] ** 3 for sp in specs)
     return {
         "metric": "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)",
-        "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(batch_ms / steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
         "data": "synthetic (seeded uniform balls, clipped-normal radii)",
@@ -756,15 +784,17 @@ def run_batched(args) -> dict:
                    "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
                    "boundary_mmHg": [sp["boundary"] for sp in specs], "total_grid_nodes": nodes,
                    "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT,
-                   "parallelism": "one GPU, instances batched"},
+                   "parallelism": "one GPU, instances batched" if world == 1 else
+                   f"{world} GPUs, instances sharded by rank and batched on each"},
         "sequential": {"value": round(plain_value, 1), "ms_per_step": round(plain_ms / steps, 4),
-                       "what": "the same 15 runs through the plain per-run path (cell_step), one after another"},
+                       "what": "the same runs through the plain per-run path (cell_step), one after another "
+                               "(on each rank, its share)"},
         "speedup_vs_sequential": round(plain_ms / batch_ms, 3),
         "identical_outputs": bool(identical),
-        "gpu_launches": int(batch.launches_per_step * args.steps),
-        "launches_per_step": int(batch.launches_per_step),
+        "gpu_launches": int(launches * args.steps),
+        "launches_per_step": int(launches),
         "final_counts": counts,
-        "last_solve_sweeps": [r.sweeps for r in reps],
+        "last_solve_sweeps": last_sweeps,
         "sor_batch": {"tiles": int(batch.sor.total_tiles), "ctas": int(batch.sor.ctas),
                       "smem_bytes": int(batch.sor.smem_bytes)},
     }
@@ -906,8 +936,19 @@ def main() -> None:
             print(json.dumps(run_reference(args)))
         return
     if WORKLOADS[args.workload].get("batched"):
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+            dist.init_process_group("nccl")
+        out = run_batched(args, rank, world)
         if rank == 0:
-            print(json.dumps(run_batched(args)))
+            print(json.dumps(out))
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
         return
     if WORKLOADS[args.workload].get("adjoint"):
         if rank == 0:

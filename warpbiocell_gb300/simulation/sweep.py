@@ -19,6 +19,12 @@ and the final metrics row.
 launch for all field solves) when every run is a plain oxygen run (no extra species, network or
 tissue region) with the same solver settings and time steps; each member's states are
 bit-identical to its run alone. Otherwise the runs go one after another as in the reference.
+
+Under ``torch.distributed`` (one process per GPU, e.g. ``torchrun``) the runs are independent, so
+the sweep is sharded by run: :func:`partition_runs` gives each rank a share balanced on the
+estimated work of :func:`run_cost` (cell-steps plus node-steps), each rank runs its share (batched
+where possible) into the same sweep directory, and rank 0 gathers the summary rows, which are the
+only data that crosses ranks, and writes ``summary.csv`` and ``metadata.json`` in sweep order.
 """
 
 from __future__ import annotations
@@ -29,6 +35,7 @@ import dataclasses
 import datetime as dt
 import itertools
 import json
+import math
 import shutil
 import time
 from dataclasses import dataclass, field
@@ -118,6 +125,46 @@ def batchable(configs) -> bool:
     return True
 
 
+def run_cost(config) -> float:
+    """Estimated work of one run: cell-steps of its initial population plus node-steps of its
+    field grids (a node update per sweep costs about a thousandth of a cell-step and warm solves
+    take hundreds of sweeps, so one node-step weighs about one cell-step)."""
+    steps = max(1, int(round(config.simulation.duration_h / config.simulation.dt_cells_h)))
+    nodes = 0
+    if config.oxygen.enabled:
+        n = int(math.ceil(config.oxygen.grid.box_um / config.oxygen.grid.dx_um)) + 1
+        nodes = n ** 3 * (1 + len(config.species))
+    return float(steps) * float(config.cells.initial_count + nodes)
+
+
+def partition_runs(costs: list[float], world: int) -> list[list[int]]:
+    """Run indices per rank: longest run first onto the least loaded rank (lowest rank on ties),
+    each share in sweep order. Deterministic, so every rank computes the same partition."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    loads = [0.0] * world
+    parts: list[list[int]] = [[] for _ in range(world)]
+    for i in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        r = min(range(world), key=lambda r: (loads[r], r))
+        parts[r].append(i)
+        loads[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def _rank_world(rank: int | None, world: int | None) -> tuple[int, int]:
+    if rank is not None and world is not None:
+        return rank, world
+    import torch.distributed as dist
+
+    if dist.is_available() and dist.is_initialized():
+        return dist.get_rank(), dist.get_world_size()
+    return 0, 1
+
+
+def _run_experiment(config, run_dir: Path, device):
+    return Experiment(config, device=device).run(run_dir, log=None)
+
+
 class Sweep:
     def __init__(self, spec: SweepSpec, base: dict, base_path: Path | None = None, sweep_path: Path | None = None):
         self.spec = spec
@@ -129,7 +176,14 @@ class Sweep:
             config.validate()
 
     def run(self, out_dir: str | Path, device: str | None = None, figures: bool = False,
-            log: Callable[[str], None] | None = None, batched: bool = False) -> list[dict]:
+            log: Callable[[str], None] | None = None, batched: bool = False, rank: int | None = None,
+            world: int | None = None) -> list[dict]:
+        """Run every configuration and return the summary rows in sweep order. ``rank``/``world``
+        default to the initialised ``torch.distributed`` group (else one process); with
+        ``world > 1`` this process runs its share of the runs, see :func:`partition_runs`."""
+        rank, world = _rank_world(rank, world)
+        if world > 1:
+            return self._run_sharded(Path(out_dir), device, figures, log, batched, rank, world)
         out_dir = Path(out_dir)
         out_dir.mkdir(parents=True, exist_ok=True)
         if self.sweep_path is not None:
@@ -155,10 +209,7 @@ class Sweep:
             writer.writeheader()
 
             def finish(label, values, config, result, run_dir):
-                row = {"label": label, "run_dir": str(run_dir), "seed": config.simulation.seed,
-                       **{k: values[k] for k in self.spec.grid_keys}, "status": result.status,
-                       "wall_s": result.wall_s, **onset_summary(result.metrics),
-                       **{f"final_{k}": v for k, v in result.metrics[-1].items()}}
+                row = self._row(label, values, config, result, run_dir)
                 rows.append(row)
                 writer.writerow(row)
                 f.flush()
@@ -177,10 +228,65 @@ class Sweep:
                 for index, (label, values, config) in enumerate(configs, start=1):
                     if log:
                         log(f"[{index}/{len(configs)}] {label}")
-                    result = Experiment(config, device=device).run(out_dir / label, log=None)
+                    result = _run_experiment(config, out_dir / label, device)
                     finish(label, values, config, result, out_dir / label)
         metadata["finished"] = dt.datetime.now(dt.timezone.utc).isoformat()
         (out_dir / "metadata.json").write_text(json.dumps(metadata, indent=2, default=str))
+        return rows
+
+    def _row(self, label, values, config, result, run_dir) -> dict:
+        return {"label": label, "run_dir": str(run_dir), "seed": config.simulation.seed,
+                **{k: values[k] for k in self.spec.grid_keys}, "status": result.status, "wall_s": result.wall_s,
+                **onset_summary(result.metrics), **{f"final_{k}": v for k, v in result.metrics[-1].items()}}
+
+    def _run_sharded(self, out_dir: Path, device, figures, log, batched, rank: int, world: int) -> list[dict]:
+        import os
+
+        import torch.distributed as dist
+
+        if device is None and torch.cuda.is_available():
+            device = f"cuda:{int(os.environ.get('LOCAL_RANK', rank)) % torch.cuda.device_count()}"
+        out_dir.mkdir(parents=True, exist_ok=True)
+        started = dt.datetime.now(dt.timezone.utc).isoformat()
+        configs = []
+        for label, values, config in self.configs:
+            if not figures:
+                config = dataclasses.replace(config, output=dataclasses.replace(config.output, figures=False))
+            configs.append((label, values, config))
+        use_batch = batched and batchable([c for _, _, c in configs])
+        mine = partition_runs([run_cost(c) for _, _, c in configs], world)[rank]
+        done: list[tuple[int, dict]] = []
+        if mine:
+            if use_batch:
+                results = run_batched([configs[i][2] for i in mine], [out_dir / configs[i][0] for i in mine],
+                                      device=device, log=log)
+            else:
+                results = [_run_experiment(configs[i][2], out_dir / configs[i][0], device) for i in mine]
+            for i, result in zip(mine, results):
+                label, values, config = configs[i]
+                done.append((i, self._row(label, values, config, result, out_dir / label)))
+                if log:
+                    log(f"    [rank {rank}] {label}: {result.status}  cells={result.metrics[-1]['cells']}")
+        gathered: list = [None] * world
+        dist.all_gather_object(gathered, done)
+        rows = [row for _, row in sorted((item for part in gathered for item in part), key=lambda t: t[0])]
+        if rank == 0:
+            if self.sweep_path is not None:
+                shutil.copyfile(self.sweep_path, out_dir / "sweep.yaml")
+            if self.base_path is not None:
+                shutil.copyfile(self.base_path, out_dir / "base_config.yaml")
+            columns = ["label", "run_dir", "seed", *self.spec.grid_keys, "status", "wall_s", *ONSET_COLUMNS,
+                       *[f"final_{c}" for c in METRIC_COLUMNS]]
+            with (out_dir / "summary.csv").open("w", newline="") as f:
+                writer = csv.DictWriter(f, fieldnames=columns)
+                writer.writeheader()
+                for row in rows:
+                    writer.writerow(row)
+            metadata = {"name": self.spec.name, "started": started,
+                        "finished": dt.datetime.now(dt.timezone.utc).isoformat(),
+                        "spec": dataclasses.asdict(self.spec), "batched": use_batch, "world": world,
+                        "runs": [{"label": r["label"], "status": r["status"], "wall_s": r["wall_s"]} for r in rows]}
+            (out_dir / "metadata.json").write_text(json.dumps(metadata, indent=2, default=str))
         return rows
 
 
