@@ -307,6 +307,14 @@ typedef struct wbc_network_program {
     const int32_t* start;        /* per node                                                         */
     const int32_t* length;       /* per node                                                         */
     const int32_t* updatable;    /* node ids of the non-input nodes                                  */
+    /* Optional truth tables, all three null or all three set. For node i with table_arity[i] = a
+     * in [0, 6], its logic value is bit  sum_j state(table_inputs[6 i + j]) << j  of
+     * table_bits[i]; table_arity[i] = -1 evaluates node i's program instead. The tables must be
+     * the programs' Boolean functions (network/model.py derives them by running each program's
+     * postfix semantics over every input pattern), so both routes give the same bits. */
+    const int32_t* table_arity;
+    const int32_t* table_inputs; /* 6 per node                                                       */
+    const uint64_t* table_bits;
 } wbc_network_program;
 
 /* Zero the words, then node i ON when randf < p_on[i] (kernels/network_kernels.py:81-95). */

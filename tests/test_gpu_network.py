@@ -83,9 +83,12 @@ def _oracle_program(rt):
     return orc.program({k: v.cpu().numpy() for k, v in rt._arrays.items()}, rt.network.n_nodes)
 
 
+@pytest.mark.parametrize("tables", [True, False], ids=["truth-tables", "programs"])
 @pytest.mark.parametrize("mode, kw", [("synchronous", {"updates_per_step": 5}), ("asynchronous", {"updates_per_step": 300}),
                                       ("maboss", {"time_units_per_h": 8.0})])
-def test_all_update_modes_bitwise_equal_oracle(golden, mode, kw):
+def test_all_update_modes_bitwise_equal_oracle(golden, mode, kw, tables):
+    """Both evaluation routes of the kernels (every MicroC node by its truth table, the runtime's
+    default, or every node by running its postfix program) against the oracle's interpreter."""
     net = microc_network(golden)
     n = 4000
     pop = _population(n, seed=13)
@@ -98,6 +101,9 @@ def test_all_update_modes_bitwise_equal_oracle(golden, mode, kw):
               InputClamp(net.names[2], "constant", 1.0), InputClamp(net.names[3], "glucose", 4.5, above=False))
     rt = NetworkRuntime(NetworkParams(net, update=mode, inputs=clamps, **kw), pop.capacity, device=DEV,
                         species_names=("oxygen", "glucose"))
+    assert (rt._tables["arity"].cpu().numpy()[rt._arrays["updatable"].cpu().numpy()] >= 0).all()
+    if not tables:
+        rt.program.table_arity = rt.program.table_inputs = rt.program.table_bits = None
     rt.initialize(pop)
     # oracle mirror of initialize + 3 x step (clamp -> update -> fates)
     prog, keep = _oracle_program(rt)

@@ -191,3 +191,55 @@ def test_cpu_device_is_refused():
 
     with pytest.raises(RuntimeError):
         _lib.resolve_device("cpu")
+
+
+def _table_step(tables, updatable, row):
+    out = row.copy()
+    for node in updatable:
+        k = int(tables["arity"][node])
+        assert k >= 0
+        idx = sum(int(row[tables["inputs"][6 * node + j]]) << j for j in range(k))
+        out[node] = bool((int(tables["bits"][node]) >> idx) & 1)
+    return out
+
+
+def test_truth_tables_reproduce_reference_microc_steps_and_programs(golden):
+    """Every MicroC node reads at most 5 nodes, so all 81 get truth tables; a step by table lookup
+    reproduces the reference's synchronous steps, and on random states every table agrees with its
+    program run with the kernels' postfix semantics (what the GPU evaluates either way)."""
+    from warpbiocell_gb300.network.model import run_postfix, truth_tables
+
+    g = golden("network_microc")
+    ops, args, start, length = g["prog_ops"], g["prog_args"], g["prog_start"], g["prog_length"]
+    upd = sorted(g["prog_updatable"].tolist())
+    tables = truth_tables(ops, args, start, length, g["prog_updatable"], len(g["names"]))
+    assert (tables["arity"][upd] >= 0).all()
+    for row, expected in zip(g["states"], g["step1"]):
+        np.testing.assert_array_equal(_table_step(tables, upd, row), expected)
+    rng = np.random.default_rng(5)
+    for _ in range(64):
+        row = rng.random(len(g["names"])) < 0.5
+        for node in upd:
+            o = ops[start[node]:start[node] + length[node]].tolist()
+            a = args[start[node]:start[node] + length[node]].tolist()
+            assert _table_step(tables, [node], row)[node] == bool(run_postfix(o, a, {i: int(v) for i, v in enumerate(row)}))
+
+
+def test_truth_tables_of_random_networks_match_expressions():
+    """Random 2-4 input truth-table networks: every updatable node gets a table equal to its DNF
+    expression (the reference evaluator) on random states; the limit of 6 inputs is honoured."""
+    from warpbiocell_gb300.network.random_network import random_truth_table_network
+
+    net = random_truth_table_network(106, seed=3)
+    arrays = net.programs()
+    tables = net.truth_tables(arrays)
+    upd = arrays["updatable"].tolist()
+    assert (tables["arity"][upd] >= 0).all() and tables["arity"].max() <= 6
+    rng = np.random.default_rng(11)
+    for _ in range(64):
+        row = rng.random(net.n_nodes) < 0.5
+        np.testing.assert_array_equal(_table_step(tables, upd, row)[upd], net.targets(row)[upd])
+    small = net.truth_tables(arrays, max_inputs=2)
+    assert (small["arity"] <= 2).all() and (small["arity"] == -1).any()
+    with pytest.raises(ValueError):
+        net.truth_tables(arrays, max_inputs=7)

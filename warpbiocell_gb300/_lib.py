@@ -203,6 +203,9 @@ class NetworkProgramC(ctypes.Structure):
         ("start", c_void_p),
         ("length", c_void_p),
         ("updatable", c_void_p),
+        ("table_arity", c_void_p),
+        ("table_inputs", c_void_p),
+        ("table_bits", c_void_p),
     ]
 
 

@@ -3,7 +3,10 @@
 // The state words of a cell stay in registers for the whole launch (all update sweeps), and the
 // postfix programs (ops/args/start/length, shared by every cell) are staged once per block in
 // shared memory; every lane of a warp walks the same program, so the interpreter never
-// diverges. Evaluation follows kernels/network_kernels.py:50-78: a boolean stack in one uint64,
+// diverges. A node whose program reads at most 6 distinct nodes is evaluated from its truth table
+// instead (when the caller passes tables): its input bits form an index into a 64-bit table, a
+// handful of operations against one interpreter step per postfix op (the random 2-4 input
+// networks compile to DNF programs of tens of ops per node). Evaluation follows kernels/network_kernels.py:50-78: a boolean stack in one uint64,
 // top = bit 0. Update semantics: synchronous (:157-175, every updatable node from the old state),
 // asynchronous (:135-154, uniform random single-node picks from the cell's stream) and MaBoSS
 // Gillespie (:178-245, with the project's log for the waiting times).
@@ -77,6 +80,9 @@ struct Words {
 struct Program {
     const int32_t* ops;    // shared or global
     const int32_t* args;
+    const int32_t* tarity;   // shared: per node, table inputs (0..6) or -1; null = no tables
+    const int32_t* tinputs;  // shared: 6 per node
+    const int32_t* tbits;    // shared: per node, the 64-bit table as two 32-bit halves (low first)
     const int32_t* start;  // global
     const int32_t* length;
     const int32_t* updatable;
@@ -110,21 +116,56 @@ __device__ __forceinline__ uint64_t eval_program(const Program& p, int node, con
     return stack & 1ull;
 }
 
-// Stage ops/args in shared memory when they fit; returns the program view for this block.
+// A node's logic value: from its truth table when it has one, else by running its program.
+template <int W>
+__device__ __forceinline__ uint64_t eval_node(const Program& p, int node, const Words<W>& s) {
+    if (p.tarity) {
+        const int arity = p.tarity[node];
+        if (arity >= 0) {
+            const int32_t* in = p.tinputs + 6 * node;
+            unsigned int idx = 0u;
+            for (int j = 0; j < arity; ++j) idx |= static_cast<unsigned int>(s.get(in[j])) << j;
+            const unsigned int half = static_cast<unsigned int>(p.tbits[2 * node + (idx >> 5)]);
+            return (half >> (idx & 31u)) & 1u;
+        }
+    }
+    return eval_program<W>(p, node, s);
+}
+
+// Stage the truth tables (when present) and ops/args (when they fit) in shared memory; returns the
+// program view for this block. Layout: arity [n_nodes], inputs [6 n_nodes], table halves
+// [2 n_nodes], then ops [n_ops] and args [n_ops].
 __device__ __forceinline__ Program stage_program(const wbc_network_program& g, int32_t* smem, bool use_smem) {
     Program p;
+    int32_t* base = smem;
+    p.tarity = p.tinputs = p.tbits = nullptr;
+    const bool tables = g.table_arity != nullptr;
+    if (tables) {
+        const int nn = g.n_nodes;
+        for (int t = threadIdx.x; t < nn; t += blockDim.x) {
+            base[t] = g.table_arity[t];
+            const uint64_t b = g.table_bits[t];
+            base[7 * nn + 2 * t] = static_cast<int32_t>(static_cast<uint32_t>(b));
+            base[7 * nn + 2 * t + 1] = static_cast<int32_t>(static_cast<uint32_t>(b >> 32));
+        }
+        for (int t = threadIdx.x; t < 6 * nn; t += blockDim.x) base[nn + t] = g.table_inputs[t];
+        p.tarity = base;
+        p.tinputs = base + nn;
+        p.tbits = base + 7 * nn;
+        base += 9 * nn;
+    }
     if (use_smem) {
         for (int t = threadIdx.x; t < g.n_ops; t += blockDim.x) {
-            smem[t] = g.ops[t];
-            smem[g.n_ops + t] = g.args[t];
+            base[t] = g.ops[t];
+            base[g.n_ops + t] = g.args[t];
         }
-        __syncthreads();
-        p.ops = smem;
-        p.args = smem + g.n_ops;
+        p.ops = base;
+        p.args = base + g.n_ops;
     } else {
         p.ops = g.ops;
         p.args = g.args;
     }
+    if (tables || use_smem) __syncthreads();
     p.start = g.start;
     p.length = g.length;
     p.updatable = g.updatable;
@@ -145,7 +186,7 @@ __global__ void k_update_sync(wbc_network_program g, int32_t n, int32_t sweeps, 
         Words<W> next = cur;
         for (int k = 0; k < p.n_updatable; ++k) {
             const int node = __ldg(p.updatable + k);
-            next.set(node, eval_program<W>(p, node, cur));
+            next.set(node, eval_node<W>(p, node, cur));
         }
         cur = next;
     }
@@ -167,7 +208,7 @@ __global__ void k_update_async(wbc_network_program g, int32_t n, int32_t n_updat
     for (int k = 0; k < n_updates; ++k) {
         const int pick = min(static_cast<int>(randf(rng, inc) * static_cast<float>(m)), m - 1);
         const int node = __ldg(p.updatable + pick);
-        cur.set(node, eval_program<W>(p, node, cur));
+        cur.set(node, eval_node<W>(p, node, cur));
     }
     rng_state[c] = rng;
     cur.store(states, c);
@@ -202,7 +243,7 @@ __global__ void k_update_maboss(wbc_network_program g, int32_t n, float duration
         float total = 0.0f;
         for (int k = 0; k < m; ++k) {
             const int node = __ldg(p.updatable + k);
-            const uint64_t l = eval_program<W>(p, node, cur);
+            const uint64_t l = eval_node<W>(p, node, cur);
             if (l) logic.set(k, 1ull);
             total += node_rate(cur.get(node), l, node, up_t, up_f, down_t, down_f);
         }
@@ -314,12 +355,14 @@ static bool program_ok(const wbc_network_program* g) {
         g->n_updatable < 0 || g->n_updatable > g->n_nodes || !g->ops || !g->args || !g->start || !g->length ||
         (g->n_updatable > 0 && !g->updatable))
         return false;
-    return true;
+    const int tables = (g->table_arity != nullptr) + (g->table_inputs != nullptr) + (g->table_bits != nullptr);
+    return tables == 0 || tables == 3;
 }
 
 static size_t program_smem(const wbc_network_program* g, bool* use) {
     *use = g->n_ops <= kMaxProgram;
-    return *use ? 2 * sizeof(int32_t) * static_cast<size_t>(g->n_ops) : 0;
+    const size_t tables = g->table_arity ? 9 * sizeof(int32_t) * static_cast<size_t>(g->n_nodes) : 0;
+    return tables + (*use ? 2 * sizeof(int32_t) * static_cast<size_t>(g->n_ops) : 0);
 }
 
 }  // namespace wbc

@@ -106,6 +106,12 @@ class BooleanNetwork:
             "p_on": np.array([n.p_on for n in self.nodes], dtype=f32),
         }
 
+    def truth_tables(self, programs: dict[str, np.ndarray] | None = None, max_inputs: int = 6) -> dict[str, np.ndarray]:
+        """The truth tables of this network's programs (see :func:`truth_tables`)."""
+        arrays = programs if programs is not None else self.programs()
+        return truth_tables(arrays["ops"], arrays["args"], arrays["start"], arrays["length"], arrays["updatable"],
+                            self.n_nodes, max_inputs)
+
     def targets(self, state: np.ndarray) -> np.ndarray:
         """Logic value of every node for a boolean state vector (inputs keep their state)."""
         mapping = {name: bool(state[i]) for name, i in self.index.items()}
@@ -309,3 +315,59 @@ def load_network(path: str | Path, cfg: str | Path | None = None) -> BooleanNetw
     if path.suffix == ".bnd":
         return read_bnd(path, cfg)
     raise NetworkError(f"unknown network format {path.suffix!r} (use .bnd or .bnet)")
+
+
+_MASK64 = (1 << 64) - 1
+
+
+def run_postfix(ops: list[int], args: list[int], value: dict[int, int]) -> int:
+    """One program on one state, with the kernels' stack semantics (kernels/network_kernels.py:50-78
+    as restated in csrc/wbc_network.cu): a 64-bit stack word, top = bit 0; VAR and CONST push (a
+    CONST pushes its argument as a 64-bit two's-complement word), NOT flips the top, AND / OR pop
+    the top and combine it into the new top; unknown opcodes do nothing."""
+    stack = 0
+    for op, a in zip(ops, args):
+        if op == 0:
+            stack = ((stack << 1) | value[a]) & _MASK64
+        elif op == 4:
+            stack = ((stack << 1) | (a & _MASK64)) & _MASK64
+        elif op == 1:
+            stack ^= 1
+        elif op == 2:
+            top = stack & 1
+            stack >>= 1
+            stack = (stack & ~1 & _MASK64) | ((stack & 1) & top)
+        elif op == 3:
+            top = stack & 1
+            stack >>= 1
+            stack = (stack & ~1 & _MASK64) | ((stack & 1) | top)
+    return stack & 1
+
+
+def truth_tables(ops, args, start, length, updatable, n_nodes: int, max_inputs: int = 6) -> dict[str, np.ndarray]:
+    """Per node, the truth table of its postfix program when the node is updatable and its program
+    reads at most ``max_inputs`` (<= 6) distinct nodes: ``arity`` (-1 = no table), ``inputs`` (6
+    node ids per node, unused ones 0) and ``bits`` (bit b = the program's value when input j holds
+    bit j of b). Every entry comes from running the program with the kernels' postfix semantics
+    (:func:`run_postfix`), so a table and its program agree on every state."""
+    if not 0 <= max_inputs <= 6:
+        raise ValueError("max_inputs must be within [0, 6]")
+    arity = np.full(n_nodes, -1, dtype=np.int32)
+    inputs = np.zeros((n_nodes, 6), dtype=np.int32)
+    bits = np.zeros(n_nodes, dtype=np.uint64)
+    for node in sorted({int(u) for u in np.asarray(updatable).tolist()}):
+        if length[node] == 0:
+            continue
+        o = [int(v) for v in ops[start[node]:start[node] + length[node]]]
+        a = [int(v) for v in args[start[node]:start[node] + length[node]]]
+        reads = sorted({arg for op, arg in zip(o, a) if op == 0})
+        if len(reads) > max_inputs or any(not 0 <= r < n_nodes for r in reads):
+            continue
+        table = 0
+        for pattern in range(1 << len(reads)):
+            value = {r: (pattern >> j) & 1 for j, r in enumerate(reads)}
+            table |= run_postfix(o, a, value) << pattern
+        arity[node] = len(reads)
+        inputs[node, :len(reads)] = reads
+        bits[node] = table
+    return {"arity": arity, "inputs": inputs.reshape(-1), "bits": bits}

@@ -96,11 +96,19 @@ class NetworkRuntime:
         self._fate_counts = torch.zeros(4, dtype=torch.int32, device=self.device)
         self.species_names = tuple(species_names)
         a = self._arrays
+        # Truth tables of the nodes with at most 6 inputs (the kernels evaluate those by lookup,
+        # the others by running their programs; both give the program's value).
+        tables = self.network.truth_tables(arrays)
+        self._tables = {"arity": torch.from_numpy(tables["arity"]).to(self.device),
+                        "inputs": torch.from_numpy(tables["inputs"]).to(self.device),
+                        "bits": torch.from_numpy(tables["bits"].view(np.int64)).to(self.device)}
+        t = self._tables
         self._program = _lib.NetworkProgramC(
             n_nodes=self.network.n_nodes, n_words=self.network.n_words, n_ops=int(a["ops"].numel()),
             n_updatable=int(a["updatable"].numel()), ops=_lib.ptr(a["ops"]), args=_lib.ptr(a["args"]),
             start=_lib.ptr(a["start"]), length=_lib.ptr(a["length"]),
-            updatable=_lib.ptr(a["updatable"]) if a["updatable"].numel() else None)
+            updatable=_lib.ptr(a["updatable"]) if a["updatable"].numel() else None,
+            table_arity=_lib.ptr(t["arity"]), table_inputs=_lib.ptr(t["inputs"]), table_bits=_lib.ptr(t["bits"]))
         self._build_clamps()
 
     # ---- input mapping -----------------------------------------------------------------------
