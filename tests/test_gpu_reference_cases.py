@@ -335,3 +335,203 @@ def test_growing_spheroid_develops_hypoxia_and_keeps_a_viable_rim():
     assert np.mean(s[outer] == int(CellState.DEAD)) < 0.05
     assert np.mean(s[inner] != int(CellState.PROLIFERATIVE)) > 0.9
     assert np.mean(s[outer] == int(CellState.PROLIFERATIVE)) > np.mean(s[inner] == int(CellState.PROLIFERATIVE))
+
+
+# ---- species (reference tests/test_species.py) ----------------------------------------------------------
+def _mixed_population(n, hypoxic_fraction=0.4, seed=1):
+    pos = spherical_cluster(n, R, spacing_factor=1.0, jitter=0.1, seed=seed)
+    states = np.full(n, int(CellState.PROLIFERATIVE), dtype=np.int32)
+    r = np.linalg.norm(pos, axis=1)
+    states[r < np.quantile(r, hypoxic_fraction)] = int(CellState.HYPOXIC)
+    states[::17] = int(CellState.DEAD)
+    return CellPopulation.from_numpy(pos, np.full(n, R), device=DEV, states=states)
+
+
+def _glucose_lactate(glucose_boundary=5.0):
+    from warpbiocell_gb300.fields.species import SpeciesParams
+
+    glucose = SpeciesParams("glucose", "mM", diffusion=2.4e5, michaelis_k=0.04, boundary_value=glucose_boundary,
+                            uptake_max=(3.0e4, 3.0e4, 4.5e5, 0.0))
+    lactate = SpeciesParams("lactate", "mM", diffusion=2.4e5, michaelis_k=1.0, boundary_value=1.0,
+                            production=(0.0, 0.0, 9.0e5, 0.0), production_source="glucose")
+    return glucose, lactate
+
+
+def test_per_state_densities_conserve_cells_and_combine_with_state_factors():
+    from warpbiocell_gb300.fields.densities import CellDensities
+
+    pop = _mixed_population(500)
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    densities = CellDensities(geom, device=DEV)
+    densities.deposit(pop)
+    dens = densities.numpy()
+    assert abs(densities.total_numpy().sum() * geom.voxel_volume - 500) < 1e-3
+    out = OxygenField(geom, OxygenParams(), device=DEV, densities=densities, uptake_state_factors={"hypoxic": 0.5})
+    out.combine()
+    np.testing.assert_allclose(out.density.cpu().numpy(), dens[0] + dens[1] + 0.5 * dens[2], rtol=1e-6, atol=1e-9)
+
+
+def test_species_chain_consumes_glucose_and_produces_lactate():
+    from warpbiocell_gb300.fields.metabolism import MetabolicFields
+
+    geom = GridGeometry(origin=(-60.0, -60.0, -60.0), dx=15.0, shape=(9, 9, 9))
+    pop = _mixed_population(150, hypoxic_fraction=0.5, seed=4)
+    settings = SolverSettings(omega=1.5, tolerance=1e-6, max_sweeps=50000, check_every=10)
+    fields = MetabolicFields(geom, OxygenParams(), list(_glucose_lactate()), settings, device=DEV)
+    report = fields.update(pop)
+    assert report.converged and set(report.reports) == {"oxygen", "glucose", "lactate"}
+    assert fields["glucose"].numpy().min() < 4.9
+    assert fields["lactate"].numpy().max() > 1.05
+    assert pop.glucose_numpy().min() < 5.0 and pop.local_numpy("lactate").max() > 1.0
+
+
+def test_no_glycolytic_cells_means_no_lactate_and_no_glucose_means_no_production():
+    from warpbiocell_gb300.fields.metabolism import MetabolicFields
+
+    geom = GridGeometry.centered_cube(300.0, 20.0)
+    glucose, lactate = _glucose_lactate()
+    pos = spherical_cluster(300, R, seed=2)
+    pop = CellPopulation.from_numpy(pos, np.full(300, R), device=DEV)  # all proliferative
+    fields = MetabolicFields(geom, OxygenParams(), [glucose, lactate], device=DEV)
+    fields.update(pop)
+    np.testing.assert_allclose(fields["lactate"].numpy(), 1.0, atol=1e-6)
+    starved, _ = _glucose_lactate(glucose_boundary=0.0)
+    fields = MetabolicFields(geom, OxygenParams(), [starved, lactate], device=DEV)
+    fields.update(_mixed_population(300, hypoxic_fraction=1.0, seed=2))
+    np.testing.assert_allclose(fields["lactate"].numpy(), 1.0, atol=1e-6)
+
+
+def test_metabolic_fields_validate_species_order_and_names():
+    from warpbiocell_gb300.fields.metabolism import MetabolicFields
+    from warpbiocell_gb300.fields.species import SpeciesField, SpeciesParams
+
+    geom = GridGeometry.centered_cube(200.0, 20.0)
+    lactate = SpeciesParams("lactate", "mM", diffusion=1.0e5, michaelis_k=1.0, boundary_value=1.0,
+                            production=(0.0, 0.0, 1.0, 0.0), production_source="glucose")
+    with pytest.raises(ValueError, match="earlier species"):
+        MetabolicFields(geom, OxygenParams(), [lactate], device=DEV)
+    with pytest.raises(ValueError, match="duplicate"):
+        MetabolicFields(geom, OxygenParams(), [SpeciesParams("oxygen", "mmHg", 1.0e5, 1.0, 1.0)], device=DEV)
+    ox = OxygenField(geom, OxygenParams(), device=DEV)
+    assert isinstance(ox, SpeciesField) and ox.name == "oxygen" and ox.species.unit == "mmHg"
+    assert ox.params.boundary_value == 38.0 and ox.species.uptake_weights == (1.0, 1.0, 1.0, 0.0)
+
+
+def test_lifecycle_glucose_rules():
+    n = 400
+    pos = spherical_cluster(n, R, seed=0)
+    pop = CellPopulation.from_numpy(pos, np.full(n, R), capacity=3 * n, device=DEV)
+    pop.oxygen_local[:n].fill_(1.0)  # anoxic everywhere; glucose for the first half only
+    pop.glucose_local[: n // 2].fill_(5.0)
+    pop.glucose_local[n // 2:n].fill_(0.1)
+    lifecycle_step(pop, LifecycleParams(division_rate=0.0, anoxic_death_rate=1.0e3, hypoxia_threshold=8.0,
+                                        death_threshold=2.0, glucose_threshold=4.0, glucose_death_threshold=0.5,
+                                        necrosis_requires_glucose=True, inhibition_threshold=NO_INHIBITION), dt=1.0)
+    s = pop.states_numpy()
+    assert np.all(s[: n // 2] == int(CellState.HYPOXIC))  # anoxic but fed
+    assert np.all(s[n // 2:] == int(CellState.DEAD))  # anoxic and starved
+    # glucose ramps the division rate: none at 0.5 mM, full at 5 mM (oxygen ample)
+    pop = CellPopulation.from_numpy(pos, np.full(n, R), capacity=3 * n, device=DEV)
+    pop.oxygen_local[:n].fill_(30.0)
+    pop.glucose_local[:n].fill_(0.5)
+    params = LifecycleParams(division_rate=1.0e3, hypoxia_threshold=8.0, death_threshold=2.0, glucose_threshold=4.0,
+                             glucose_death_threshold=0.5, inhibition_threshold=NO_INHIBITION)
+    assert lifecycle_step(pop, params, dt=1.0) == 0
+    pop.glucose_local[:n].fill_(5.0)
+    assert lifecycle_step(pop, params, dt=1.0) == n
+
+
+# ---- networks (reference tests/test_network.py) ----------------------------------------------------------
+def _flags_population(n, flags, seed=0):
+    pos = spherical_cluster(n, R, spacing_factor=1.0, jitter=0.1, seed=seed)
+    pop = CellPopulation.from_numpy(pos, np.full(n, R), capacity=3 * n, device=DEV, seed=seed)
+    pop.fate_flags[:n].copy_(torch.as_tensor(flags, dtype=torch.int32, device=DEV))
+    return pop
+
+
+def test_network_mode_divides_only_with_proliferation_on():
+    n = 400
+    flags = np.zeros(n, dtype=np.int32)
+    flags[: n // 2] = 1  # proliferation
+    flags[n // 4: n // 2] |= 4  # ... with growth arrest too
+    pop = _flags_population(n, flags)
+    created = lifecycle_step(pop, LifecycleParams(division_rate=1.0e3, inhibition_threshold=NO_INHIBITION,
+                                                  phenotype_model="network"), dt=1.0)
+    assert created == n // 4
+    s = pop.states_numpy()[:n]
+    assert np.all(s[: n // 4] == int(CellState.PROLIFERATIVE))
+    assert np.all(s[n // 4:] == int(CellState.QUIESCENT))
+
+
+def test_network_mode_death_rates_and_rules_mode_ignores_fates():
+    n = 30000
+    flags = np.zeros(n, dtype=np.int32)
+    flags[: n // 3] = 2  # apoptosis
+    flags[n // 3: 2 * n // 3] = 8  # necrosis
+    pop = _flags_population(n, flags, seed=5)
+    lifecycle_step(pop, LifecycleParams(division_rate=0.0, phenotype_model="network", apoptosis_rate=0.5,
+                                        necrosis_rate=1.0e3), dt=1.0)
+    dead = pop.states_numpy()[:n] == int(CellState.DEAD)
+    assert abs(dead[: n // 3].mean() - (1.0 - np.exp(-0.5))) < 0.02
+    assert dead[n // 3: 2 * n // 3].all() and not dead[2 * n // 3:].any()
+    pop = _flags_population(200, np.full(200, 8, dtype=np.int32))  # necrosis everywhere, rules mode
+    lifecycle_step(pop, LifecycleParams(division_rate=0.0, necrosis_rate=1.0e3), dt=1.0)
+    assert not (pop.states_numpy()[:200] == int(CellState.DEAD)).any()
+
+
+def test_microc_network_fates_follow_the_environment(golden):
+    """The MicroC model: necrosis only without oxygen and glucose; under hypoxia with glucose the
+    glycolytic switch keeps ATP up and proliferation unchanged."""
+    from tests._networks import microc_network
+    from warpbiocell_gb300.network.runtime import InputClamp, NetworkParams, NetworkRuntime
+
+    net = microc_network(golden)
+    n = 3000
+    pos = spherical_cluster(n, R, spacing_factor=1.0, jitter=0.1, seed=8)
+    pop = CellPopulation.from_numpy(pos, np.full(n, R), capacity=3 * n, device=DEV, seed=8)
+    pop.local_field("lactate")  # zero lactate at every cell
+    clamps = (InputClamp("Oxygen_supply", "oxygen", 15.7), InputClamp("Glucose_supply", "glucose", 4.0),
+              InputClamp("MCT1_stimulus", "lactate", 1.5), InputClamp("EGFR_stimulus", "constant", 1.0),
+              InputClamp("cMET_stimulus", "constant", 1.0), InputClamp("FGFR_stimulus", "constant", 1.0))
+    rt = NetworkRuntime(NetworkParams(net, update="asynchronous", updates_per_step=400, inputs=clamps), pop.capacity,
+                        device=DEV, species_names=("oxygen", "glucose", "lactate"))
+
+    def run(o2, glc):
+        pop.oxygen_local.fill_(o2)
+        pop.glucose_local.fill_(glc)
+        rt.initialize(pop)
+        for _ in range(20):
+            rt.step(pop, dt_h=0.25)
+        counts = {k: v / n for k, v in rt.fate_counts(pop).items()}
+        s = rt.states_numpy(pop)
+        idx = net.index
+        return counts, s[:, idx["glycoATP"]].mean(), s[:, idx["mitoATP"]].mean(), s[:, idx["ATP_Production_Rate"]].mean()
+
+    normoxia, _, mito_n, _ = run(30.0, 5.0)
+    hypoxia, glyco_h, mito_h, atp_h = run(5.0, 5.0)
+    starved, _, _, atp_s = run(5.0, 1.0)
+    assert normoxia["necrosis"] == 0.0
+    assert 0.1 < normoxia["proliferation"] < 0.35 and 0.05 < normoxia["apoptosis"] < 0.35
+    assert mito_h < 0.05 < mito_n and glyco_h > 0.9 and atp_h > 0.9
+    assert abs(hypoxia["proliferation"] - normoxia["proliferation"]) < 0.08
+    assert starved["necrosis"] > 0.95 and starved["proliferation"] < 0.02 and atp_s < 0.05
+
+
+def test_maboss_network_dynamics_are_reproducible(golden):
+    from tests._networks import microc_network
+    from warpbiocell_gb300.network.runtime import InputClamp, NetworkParams, NetworkRuntime
+
+    net = microc_network(golden, rates=True)
+    runs = []
+    for _ in range(2):
+        pos = spherical_cluster(500, R, spacing_factor=1.0, jitter=0.1, seed=21)
+        pop = CellPopulation.from_numpy(pos, np.full(500, R), capacity=1500, device=DEV, seed=21)
+        rt = NetworkRuntime(NetworkParams(net, update="maboss", time_units_per_h=8.0,
+                                          inputs=(InputClamp("EGFR_stimulus", "constant", 1.0),)),
+                            pop.capacity, device=DEV)
+        rt.initialize(pop)
+        for _ in range(4):
+            rt.step(pop, dt_h=0.25)
+        runs.append(rt.states_numpy(pop))
+    assert np.array_equal(runs[0], runs[1])
+    assert runs[0].any(axis=0).sum() > 10  # the chain actually moved nodes
