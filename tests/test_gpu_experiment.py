@@ -99,3 +99,28 @@ def test_capacity_stop_is_reported():
     result = Experiment(cfg).run()
     assert result.status == "capacity_exceeded"
     assert result.metrics[-1]["cells"] <= 320
+
+
+def test_on_metrics_observer_receives_every_row():
+    """Reference tests/test_experiment.py: the observer sees every metrics row as it is made."""
+    rows = []
+    result = Experiment(config_from_dict(_base())).run(on_metrics=rows.append)
+    assert [r["time_h"] for r in rows] == [r["time_h"] for r in result.metrics] == [0.0, 0.5, 1.0, 1.5, 2.0]
+    assert rows[-1]["cells"] == result.summary["cells"]
+
+
+def test_in_memory_runs_are_reproducible_and_seed_dependent():
+    a = Experiment(config_from_dict(_base())).run()
+    b = Experiment(config_from_dict(_base())).run()
+    c = Experiment(config_from_dict(_base(simulation__seed=4))).run()
+    for key in ("cells", "dead_cells", "spheroid_radius_um", "oxygen_cells_min_mmHg"):
+        np.testing.assert_array_equal(a.metric(key), b.metric(key))
+    assert a.summary["cells"] != c.summary["cells"] or a.summary["spheroid_radius_um"] != c.summary["spheroid_radius_um"]
+
+
+def test_oxygen_can_be_disabled(tmp_path):
+    result = Experiment(config_from_dict(_base(oxygen__enabled=False))).run(tmp_path / "run")
+    assert result.status == "completed"
+    assert result.summary["hypoxic_cells"] == 0
+    assert np.isnan(result.summary["oxygen_cells_min_mmHg"])
+    assert (tmp_path / "run" / "metrics.csv").exists()
