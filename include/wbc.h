@@ -197,6 +197,15 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
                   const int32_t* fixed, const float* density, const float* production, const float* source,
                   float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
                   const wbc_sor_tuning* tuning, void* stream);
+/* Self-test of the solver's bounded device waits (no counterpart in the reference): runs the grid
+ * barrier of the resident solver `rounds` times on `ctas` expected CTAs, of which `ctas - missing`
+ * are launched (cooperatively, one small CTA each; ctas <= the SM count). With missing = 0 the
+ * barriers complete and WBC_OK is returned; with missing > 0 the missing CTAs never arrive, every
+ * launched CTA stops polling after its bound (about a second), and WBC_ERR_TIMEOUT is returned with
+ * the device context intact. `workspace` (at least the control block and barrier flags of
+ * wbc_sor_solve_workspace_bytes, 16-byte aligned) is cleared first. Synchronises `stream`. */
+int wbc_sor_wait_selftest(int32_t ctas, int32_t missing, int32_t rounds, void* workspace, size_t workspace_bytes,
+                          void* stream);
 /* Times the resident solver on a copy of `field` (into `scratch_field`, nx*ny*nz floats) for
  * 2 * check_every sweeps under each candidate tuning (halo depths 1, 2, 4; per depth the tile grid
  * with the fewest columns per tile, its transpose and the squarest grid) and returns the fastest in

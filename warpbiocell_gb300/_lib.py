@@ -234,6 +234,7 @@ SIGNATURES: dict[str, list] = {
     "wbc_sor_sweeps": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P],
     "wbc_ftcs_step": [POINTER(SorParamsC), _F, _P, _P, _P, _P, _P, _P, _P],
     "wbc_sor_solve_workspace_bytes": [POINTER(SorParamsC)],
+    "wbc_sor_wait_selftest": [_I, _I, _I, _P, c_size_t, _P],
     "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, POINTER(SorReportC), _P,
                       c_size_t, _I, POINTER(SorTuningC), _P],
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),

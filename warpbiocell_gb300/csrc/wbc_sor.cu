@@ -807,6 +807,19 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
     sor_tile<HAS_PROD, LANES, H>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
 }
 
+// The solver's grid barrier alone, for the self-test of the bounded waits: `ntiles` tiles are
+// expected, gridDim.x of them run. With gridDim.x < ntiles the missing tiles never arrive, every
+// launched CTA gives up after its bounded polls, and the control block's status says so.
+__global__ void k_barrier_selftest(SorControl* ctl, unsigned int* flags, int ntiles, int rounds) {
+    unsigned int epoch = 0;
+    for (int r = 0; r < rounds; ++r) {
+        if (!grid_barrier(ctl, flags, epoch, static_cast<int>(blockIdx.x), ntiles)) {
+            if (threadIdx.x == 0) atomicExch(&ctl->status, 1);
+            return;
+        }
+    }
+}
+
 // ---- batched solves ----------------------------------------------------------------------------------
 // One persistent launch solves many grids. A CTA claims the next tile of the work list (the tiles
 // of item 0, then of item 1, ...) and runs it until that item's solve ends, then claims again.
@@ -1377,6 +1390,40 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
     if (pick >= 0) {
         *best = cands[pick];
         if (best_us_per_sweep) *best_us_per_sweep = best_ms[pick] * 1000.0f / sweeps;
+    }
+    return WBC_OK;
+}
+
+int wbc_sor_wait_selftest(int32_t ctas, int32_t missing, int32_t rounds, void* workspace, size_t workspace_bytes,
+                          void* stream) {
+    if (ctas < 1 || ctas > kMaxCtas || missing < 0 || missing >= ctas || rounds < 1 || !workspace)
+        return WBC_ERR_INVALID;
+    if (workspace_bytes < header_bytes() || reinterpret_cast<uintptr_t>(workspace) % 16 != 0) return WBC_ERR_WORKSPACE;
+    const DeviceInfo dev = device_info();
+    if (ctas > dev.sms) {
+        set_error_msg("wbc_sor_wait_selftest: more CTAs than SMs");
+        return WBC_ERR_INVALID;
+    }
+    cudaStream_t s = as_stream(stream);
+    char* base = static_cast<char*>(workspace);
+    SorControl* ctl = reinterpret_cast<SorControl*>(base);
+    unsigned int* flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
+    cudaError_t err = cudaMemsetAsync(base, 0, header_bytes(), s);
+    int launched = ctas - missing;
+    void* params[] = {&ctl, &flags, &ctas, &rounds};
+    if (err == cudaSuccess)
+        err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(k_barrier_selftest), dim3(launched), dim3(64),
+                                          params, 0, s);
+    SorControl host{};
+    if (err == cudaSuccess) err = cudaMemcpyAsync(&host, ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, s);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+    if (err != cudaSuccess) {
+        set_error("wbc_sor_wait_selftest", err);
+        return WBC_ERR_CUDA;
+    }
+    if (host.status != 0) {
+        set_error_msg("wbc_sor_wait_selftest: a grid barrier timed out");
+        return WBC_ERR_TIMEOUT;
     }
     return WBC_OK;
 }
