@@ -240,9 +240,11 @@ typedef struct wbc_sor_batch {    /* filled by wbc_sor_batch_prepare            
 
 size_t wbc_sor_batch_plan_bytes(int32_t n);
 /* Orders the items heaviest first by `weights` (host, one positive value per item, e.g. nodes x
- * sweeps of the previous solve; NULL = node counts), tiles each with CTAs in proportion to its
- * weight (raised until the tiles fit in shared memory), copies the work list into `plan` (device
- * memory) and fills `out`. Synchronises `stream`; not for use during stream capture. */
+ * sweeps of the previous solve; NULL = node counts) and groups them into waves whose tiles fit on
+ * the GPU at once, each item tiled with CTAs in proportion to its weight within its wave (when an
+ * item cannot be tiled that way: in proportion to its weight over all items, raised until the
+ * tiles fit in shared memory), copies the work list into `plan` (device memory) and fills `out`.
+ * Synchronises `stream`; not for use during stream capture. */
 int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
                           int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
                           void* stream);

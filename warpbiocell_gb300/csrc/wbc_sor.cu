@@ -1173,6 +1173,41 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     std::vector<int32_t> order(n);
     for (int b = 0; b < n; ++b) order[b] = b;
     std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
+    // First choice: waves. Heaviest first, items join the current wave while every item of the wave
+    // can be tiled with floor(G x its share of the wave's work) CTAs in shared memory and the
+    // wave's tiles fit on the GPU at once; then a new wave starts. A wave's items start together
+    // and, their CTAs being proportional to their work, end together, so the next wave's tiles are
+    // claimed when a whole wave of CTAs frees up. If some item cannot be tiled that way, the
+    // proportional plan below is used instead.
+    std::vector<SorTiling> tiling(n);
+    bool waves = true;
+    {
+        auto plan_wave = [&](int lo, int hi, bool commit) {
+            double w = 0.0;
+            for (int k = lo; k < hi; ++k) w += work[order[k]];
+            int tiles = 0;
+            for (int k = lo; k < hi; ++k) {
+                const int b = order[k];
+                const int share = std::max(1, static_cast<int>(G * work[b] / w));
+                SorTiling t{};
+                if (!choose_tiling(items[b].params, share, limit, 1, 0, 0, &t)) return false;
+                tiles += t.tx * t.ty;
+                if (commit) tiling[k] = t;
+            }
+            return tiles <= G;
+        };
+        int lo = 0;
+        while (lo < n && waves) {
+            int hi = lo + 1;
+            if (!plan_wave(lo, hi, false)) {
+                waves = false;
+                break;
+            }
+            while (hi < n && plan_wave(lo, hi + 1, false)) ++hi;
+            plan_wave(lo, hi, true);
+            lo = hi;
+        }
+    }
     std::vector<SorArgs> args(n);
     std::vector<int32_t> first(n + 1, 0);
     int lanes = 1, threads = 32;
@@ -1182,13 +1217,15 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
         const int b = order[k];
         const wbc_sor_batch_item& it = items[b];
         const wbc_sor_params& p = it.params;
-        int share = std::min(G, std::max(1, static_cast<int>(3.0 * G * work[b] / total_work + 0.5)));
-        SorTiling t{};
-        bool fits = false;
-        for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 1, 0, 0, &t);
-        if (!fits) {
-            set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
-            return WBC_ERR_INVALID;
+        SorTiling t = tiling[k];
+        if (!waves) {
+            int share = std::min(G, std::max(1, static_cast<int>(3.0 * G * work[b] / total_work + 0.5)));
+            bool fits = false;
+            for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 1, 0, 0, &t);
+            if (!fits) {
+                set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
+                return WBC_ERR_INVALID;
+            }
         }
         char* base = static_cast<char*>(it.workspace);
         SorArgs& a = args[k];
