@@ -182,8 +182,8 @@ typedef struct wbc_sor_tuning {
     int32_t tiles_i, tiles_j;
 } wbc_sor_tuning;
 
-/* Scratch bytes wbc_sor_solve needs for this grid (control block, halo exchange buffers and the
- * coefficient copy); the workspace must be 16-byte aligned. */
+/* Scratch bytes wbc_sor_solve needs for this grid (control block, halo exchange buffers, the
+ * coefficient copy and the production-term copy); the workspace must be 16-byte aligned. */
 size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p);
 /* Solve to the residual tolerance from the field's current values (warm start), checking the
  * residual every `check_every` sweeps and stopping at `max_sweeps`: the sweep count, residual and

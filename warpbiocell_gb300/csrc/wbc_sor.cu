@@ -76,6 +76,7 @@ struct SorArgs {
     int check_every;
     int max_sweeps;
     double tolerance;  // compared in double, as the reference compares float(residual) < tolerance
+    float* pcopy;      // [2][nx][ny][M] production term of every updated node (production, source)
 };
 
 constexpr unsigned kBarrierPolls = 1u << 21;  // L2 round trips: about a second
@@ -249,7 +250,7 @@ __device__ __noinline__ float residual_exact(float u, float b1, float nb, float 
 // IEEE division replaces the fast one only where the range tests above do not hold.
 template <bool HAS_PROD, bool ZCLAMP, int LANES>
 __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
-                                            int kp, int last, int64_t gbase, unsigned long long* xrow, int cnt,
+                                            int kp, int last, const float* prow, unsigned long long* xrow, int cnt,
                                             unsigned int tag, const float (&du)[LANES]) {
     const float* pim = po - w.si;
     const float* pip = po + w.si;
@@ -264,7 +265,7 @@ __device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, fl
         float cc = div_rn_fast_nonneg_zero(du[r], b1);
         float prod = 0.0f;
         if (HAS_PROD) {
-            if (active) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+            if (active) prod = prow[off];
         }
         float vlo, vhi;
         if (ZCLAMP) {
@@ -298,14 +299,13 @@ __device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, i
     const int last = e.w >> 11;
     float* po = w.s + e.x + lane;
     const float* oth = w.s + e.y;
-    int64_t gbase = 0;
-    if (HAS_PROD) gbase = (c.y >> 16) * w.sx + static_cast<int64_t>(c.y & 0xffff) * w.nz;
+    const float* prow = HAS_PROD ? a.pcopy + e.z + lane : nullptr;
     unsigned long long* xrow = tag ? reinterpret_cast<unsigned long long*>(w.xchg) + e.z + lane : nullptr;
     const int cnt = (e.w >> 1) & 1023;
     if (w.zclamp)
-        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, xrow, cnt, tag, du);
+        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, prow, xrow, cnt, tag, du);
     else
-        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, xrow, cnt, tag,
+        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, prow, xrow, cnt, tag,
                                             du);
 }
 
@@ -342,7 +342,7 @@ __device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, 
 // r = nb + h prod - (6 + h c) u (field_kernels.py:215-243), as float bits (all values are >= 0).
 template <bool HAS_PROD, bool ZCLAMP, int LANES>
 __device__ __forceinline__ unsigned int residual_nodes(const SorArgs& a, const Sweep& w, const float* po,
-                                                       const float* pv, int lane, int kp, int last, int64_t gbase,
+                                                       const float* pv, int lane, int kp, int last, const float* prow,
                                                        const float (&du)[LANES]) {
     const float* pim = po - w.si;
     const float* pip = po + w.si;
@@ -358,7 +358,7 @@ __device__ __forceinline__ unsigned int residual_nodes(const SorArgs& a, const S
         float cc = div_rn_fast(du[r], b1);
         float prod = 0.0f;
         if (HAS_PROD) {
-            if (active) prod = prod_term(a, gbase + 2 * (lane + off) + kp);
+            if (active) prod = prow[off];
         }
         float vlo, vhi;
         if (ZCLAMP) {
@@ -392,10 +392,9 @@ __device__ __forceinline__ unsigned int residual_column(const SorArgs& a, const 
     const int last = e.w >> 11;
     const float* po = w.s + e.x + lane;
     const float* oth = w.s + e.y;
-    int64_t gbase = 0;
-    if (HAS_PROD) gbase = (c.y >> 16) * w.sx + static_cast<int64_t>(c.y & 0xffff) * w.nz;
-    if (w.zclamp) return residual_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, gbase, du);
-    return residual_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, gbase, du);
+    const float* prow = HAS_PROD ? a.pcopy + e.z + lane : nullptr;
+    if (w.zclamp) return residual_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, prow, du);
+    return residual_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, prow, du);
 }
 
 // Reads the parity `colour` updated in each listed halo column once every entry carries `tag`
@@ -664,7 +663,11 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
                                   (p.bc_z == 0 && (k == 0 || k == nz - 1));
                 float v = -1.0f;
                 if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
-                a.coeff[((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1)] = v;
+                const int64_t at = ((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1);
+                a.coeff[at] = v;
+                // The production term is fixed for the solve: computed once here (only where a node
+                // is updated, as the update itself would) instead of in every sweep.
+                if (HAS_PROD) a.pcopy[at] = v >= 0.0f ? prod_term(a, idx) : 0.0f;
                 if (!coefficient_in_range(v, w.K, w.h)) s_outside_range = 1;
             }
         }
@@ -970,7 +973,8 @@ static size_t plane_bytes(const wbc_sor_params& p) {
 
 static size_t header_bytes() { return sizeof(SorControl) + kMaxCtas * sizeof(unsigned int); }
 
-size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 3 * plane_bytes(p) + 256; }
+// [control block + barrier flags][exchange: 2 planes][coefficient copy][production copy]
+size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 4 * plane_bytes(p) + 256; }
 
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
@@ -1041,6 +1045,7 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     }
     SorArgs args{p,    t,     fixed, density, production, source,      field,
                  xchg, coeff, ctl,   flags,   check_every, max_sweeps, tolerance};
+    args.pcopy = reinterpret_cast<float*>(base + header_bytes() + 3 * plane_bytes(p));
     void* params[] = {&args};
     err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(t.tx * t.ty), dim3(t.threads), params,
                                       t.smem, stream);
@@ -1238,6 +1243,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
         a.field = it.field;
         a.xchg = reinterpret_cast<float*>(base + header_bytes());
         a.coeff = reinterpret_cast<float*>(base + header_bytes() + 2 * plane_bytes(p));
+        a.pcopy = reinterpret_cast<float*>(base + header_bytes() + 3 * plane_bytes(p));
         a.ctl = reinterpret_cast<SorControl*>(base);
         a.flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
         a.check_every = check_every;
