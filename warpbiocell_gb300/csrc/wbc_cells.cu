@@ -87,7 +87,7 @@ int wbc_division_scan(int32_t n, const int32_t* divide_flag, int32_t* division_o
 namespace wbc {
 namespace {
 constexpr int64_t kNoAllocPartials = WBC_NOALLOC_SCAN_MAX_CELLS / kScanTileItems + 1;
-__device__ __align__(256) int32_t g_noalloc_partials[kNoAllocPartials];
+static __device__ __align__(256) int32_t g_noalloc_partials[kNoAllocPartials];
 static_assert(WBC_NOALLOC_SCAN_MAX_CELLS % kScanTileItems == 0, "whole tiles");
 
 constexpr int kMaxDevices = 64;
