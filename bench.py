@@ -21,7 +21,8 @@ Arms:
                      restatement (oracle/) with every host thread, on the same workload.
 
 Multi-GPU (torchrun, --gpus N): independent replicas, one per GPU (no data-path collective; the
-only collectives are the timing barrier and the max/sum reductions of the result).
+only collectives are the timing barrier and the max/sum reductions of the result); the batched
+sweep workload shards its instances over the ranks instead (simulation.sweep.partition_runs).
 """
 
 from __future__ import annotations

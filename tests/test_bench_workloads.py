@@ -1,0 +1,59 @@
+"""The benchmark's synthetic workloads (host logic, no device): the seeded inputs have the shapes,
+sizes and distributions of the configurations they stand in for, and the unit conversions match
+the reference's parameters (per-hour rates, um, mmHg um^3/h uptake)."""
+
+import math
+
+import numpy as np
+import pytest
+
+import bench
+
+
+def test_unit_conversions():
+    # 2000 um^2/s -> um^2/h; 20 amol/s over an O2 solubility of 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
+    assert bench.DIFFUSION == pytest.approx(7.2e6)
+    assert bench.VMAX == pytest.approx(5.5385e7, rel=1e-4)
+    assert bench.DT == pytest.approx(0.1)  # 6 min
+
+
+@pytest.mark.parametrize("name, cells, ball", [("spheroid_10k_41", 10_000, 250.0), ("spheroid_100k_81", 100_000, 600.0)])
+def test_cells_fill_the_ball_with_clipped_normal_radii(name, cells, ball):
+    w = bench.WORKLOADS[name]
+    pos, radii = bench.make_cells(w, seed=0)
+    assert pos.shape == (cells, 3) and radii.shape == (cells,)
+    r = np.linalg.norm(pos.astype(np.float64), axis=1)
+    assert r.max() <= ball * (1 + 1e-6)
+    # uniform in the ball: the fraction within half the radius is 1/8
+    assert abs(np.mean(r < 0.5 * ball) - 0.125) < 0.02
+    assert radii.min() >= 6.0 and radii.max() <= 10.0
+    assert abs(radii.mean() - 8.0) < 0.05 and abs(radii.std() - 0.8) < 0.05
+    pos2, radii2 = bench.make_cells(w, seed=0)
+    assert np.array_equal(pos, pos2) and np.array_equal(radii, radii2)  # seeded
+
+
+def test_headline_workload_matches_its_configuration():
+    w = bench.WORKLOADS["spheroid_1M_161"]
+    assert (w["cells"], w["ball_um"], w["dx_um"], w["boundary"]) == (1_000_000, 1200.0, 15.0, 100.0)
+    P = bench.make_params(w)
+    assert P["geom"].shape == (161, 161, 161) and P["geom"].dx == 15.0
+    s = P["settings"]
+    assert (s.omega, s.tolerance) == (1.8, 1e-6)
+    assert P["contact"].query_radius == pytest.approx(20.0)  # 20 um hash cells
+    assert P["stepping"].mechanics_substeps == 1
+    assert P["lifecycle"].division_rate == pytest.approx(math.log(2.0) / 24.0)
+    assert (P["lifecycle"].hypoxia_threshold, P["lifecycle"].death_threshold) == (5.0, 1.0)
+
+
+def test_batched_sweep_instances_follow_the_sweep_definition():
+    w = bench.WORKLOADS["batched_sweep_15"]
+    specs = bench.batch_specs(w, seed=0)
+    assert len(specs) == 15
+    assert sorted({s["boundary"] for s in specs}) == [10.0, 20.0, 38.0, 60.0, 100.0]
+    cells = np.array([s["cells"] for s in specs])
+    assert cells.min() >= 2_000 and cells.max() <= 200_000 and len(set(cells.tolist())) > 10  # uneven
+    nodes = np.array([s["nodes"] for s in specs])
+    assert nodes.min() >= 41 and nodes.max() <= 121 and np.all(nodes % 2 == 1)
+    for s in specs:  # the box spans 2.5 spheroid radii
+        assert (s["nodes"] - 1) * s["dx"] == pytest.approx(2.5 * s["ball"], rel=1e-9)
+    assert bench.batch_specs(w, seed=0) == specs  # seeded
