@@ -4,7 +4,6 @@ inheritance against the oracle, bit for bit (reference tests: test_network.py:12
 bitwise CPU==CUDA checks of test_gpu.py:288-312)."""
 
 import ctypes
-from pathlib import Path
 
 import numpy as np
 import pytest
