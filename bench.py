@@ -642,6 +642,80 @@ def run_reference(args) -> dict:
     }
 
 
+def run_reference_batched(args) -> dict:
+    """The sweep as the reference runs it: its instances one after another on the host (the
+    reference's Sweep runs one Experiment per configuration). A bounded sample: rounds of one step
+    of every instance, until the steps are done or the time budget is spent."""
+    from oracle import oracle as orc
+    from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball
+    from warpbiocell_gb300.fields.oxygen import OxygenParams, species_params
+
+    w = WORKLOADS[args.workload]
+    P = make_params(dict(box_um=800.0, dx_um=20.0, boundary=38.0))
+    specs = batch_specs(w, args.seed)
+    contact, stepping = P["contact"], P["stepping"]
+    runs = []
+    for sp in specs:
+        pos = uniform_ball(sp["cells"], sp["ball"], seed=sp["seed"])
+        radii = clipped_normal_radii(sp["cells"], 8.0, 0.8, 6.0, 10.0, seed=sp["seed"] + 1)
+        sim = orc.OracleSim.from_numpy(pos, radii, capacity=3 * sp["cells"], seed=sp["seed"])
+        half = 0.5 * (sp["nodes"] - 1) * sp["dx"]
+        og = orc.Geometry((-half,) * 3, sp["dx"], (sp["nodes"],) * 3)
+        s = species_params(OxygenParams(diffusion_coefficient=DIFFUSION, uptake_max=VMAX, michaelis_k=KM,
+                                        boundary_value=sp["boundary"]))
+        species = [orc.OracleSpecies(og, (0, 0, 0), s.boundary_value, s.diffusion, s.uptake_max, s.michaelis_k,
+                                     P["settings"], production=s.production, name=s.name)]
+        sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
+        orc.metabolic_update(sim, species, {})  # initial field solve, as the reference's Experiment.run
+        runs.append((sim, species))
+    threads = orc.num_threads()
+
+    def step(sim, species):
+        orc.full_cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, species, {})
+
+    for _ in range(args.warmup):
+        for sim, species in runs:
+            step(sim, species)
+    cells, done = 0, 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for sim, species in runs:
+            cells += sim.count
+            step(sim, species)
+        done += 1
+        if time.perf_counter() - t0 > args.reference_budget_s:
+            break
+    elapsed = time.perf_counter() - t0
+    value = cells / elapsed
+    sample = (f"{done} rounds of one full cell step of each of the {len(runs)} instances, one instance after "
+              f"another, by the C++ restatement of the reference kernels (WarpBioCell's Warp CPU path cannot "
+              f"run here: warp-lang is absent) on {threads} OpenMP threads")
+    unit = "cell-steps/s"
+    return {
+        "metric": "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)",
+        "value": round(value, 1), "unit": unit, "n_gpus": 0, "steps": done, "warmup": args.warmup,
+        "ms_per_step": round(elapsed * 1e3 / max(1, done), 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
+        "data": "synthetic (seeded uniform balls, clipped-normal radii)",
+        "config": {"workload": args.workload, "instances": len(specs),
+                   "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
+                   "boundary_mmHg": [sp["boundary"] for sp in specs]},
+        "impl": "reference",
+        "cpu_baseline": {"value": round(value, 1), "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 1), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def reference_unavailable(args) -> dict | None:
+    """The line the reference arm prints for a workload whose metric has no CPU counterpart."""
+    if WORKLOADS[args.workload].get("adjoint"):
+        return {"impl": "reference",
+                "unavailable": "the adjoint workload's metric (backward time over forward time) is timed on the "
+                               "reference's Warp tape, which needs warp-lang (absent); the C++ restatement has "
+                               "no reverse pass (it re-runs the forward in FP64 for central differences only)"}
+    return None
+
+
 # ---- batched sweep (15 spheroids) ----------------------------------------------------------------------
 def batch_specs(w: dict, seed: int) -> list[dict]:
     """The sweep's instances: (cells, ball radius, grid nodes, spacing, boundary, seed) each."""
@@ -934,7 +1008,10 @@ def main() -> None:
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
         if rank == 0:
-            print(json.dumps(run_reference(args)))
+            out = reference_unavailable(args)
+            if out is None:
+                out = run_reference_batched(args) if WORKLOADS[args.workload].get("batched") else run_reference(args)
+            print(json.dumps(out))
         return
     if WORKLOADS[args.workload].get("batched"):
         if world > 1:

@@ -57,3 +57,14 @@ def test_batched_sweep_instances_follow_the_sweep_definition():
     for s in specs:  # the box spans 2.5 spheroid radii
         assert (s["nodes"] - 1) * s["dx"] == pytest.approx(2.5 * s["ball"], rel=1e-9)
     assert bench.batch_specs(w, seed=0) == specs  # seeded
+
+
+def test_reference_arm_names_its_route_for_every_workload():
+    import argparse
+
+    for name in bench.WORKLOADS:
+        out = bench.reference_unavailable(argparse.Namespace(workload=name))
+        if bench.WORKLOADS[name].get("adjoint"):
+            assert out["impl"] == "reference" and "warp-lang" in out["unavailable"]
+        else:
+            assert out is None  # timed by the C++ restatement
