@@ -630,6 +630,17 @@ def run_reference(args) -> dict:
     value = cells / elapsed
     sample = (f"{done} full cell steps of the workload by the C++ restatement of the reference kernels "
               f"(WarpBioCell's Warp CPU path cannot run here: warp-lang is absent) on {threads} OpenMP threads")
+    # One more step on one thread: the reference's Warp CPU mode runs its kernels single-threaded.
+    orc.set_threads(1)
+    try:
+        n1 = sim.count
+        t1 = time.perf_counter()
+        step()
+        one_s = time.perf_counter() - t1
+    finally:
+        orc.set_threads(threads)
+    single = {"value": round(n1 / one_s, 1), "unit": UNIT, "cores": 1,
+              "sample": f"the next full cell step ({n1} cells) on one thread; {one_s:.2f} s"}
     return {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": done, "warmup": args.warmup,
         "ms_per_step": round(elapsed * 1e3 / max(1, done), 3), "higher_is_better": True, "scaling": "weak",
@@ -637,9 +648,26 @@ def run_reference(args) -> dict:
         "data": "synthetic (seeded uniform ball, clipped-normal radii)",
         "config": {"workload": args.workload, **w, "grid_nodes": g.node_count},
         "impl": "reference",
-        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "single_thread": single, "host": host_cpu()},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+
+
+def host_cpu() -> dict:
+    """The host's logical CPU count, architecture and model name (from lscpu where it is present)."""
+    import platform
+
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return {"cpu_count": os.cpu_count(), "machine": platform.machine(), "model": model}
 
 
 def run_reference_batched(args) -> dict:

@@ -68,3 +68,9 @@ def test_reference_arm_names_its_route_for_every_workload():
             assert out["impl"] == "reference" and "warp-lang" in out["unavailable"]
         else:
             assert out is None  # timed by the C++ restatement
+
+
+def test_host_cpu_record():
+    host = bench.host_cpu()
+    assert host["cpu_count"] >= 1 and host["machine"]
+    assert host["model"] is None or isinstance(host["model"], str)
