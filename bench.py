@@ -792,7 +792,6 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     path): each rank batches its share, balanced by simulation.sweep.partition_runs."""
     import torch
 
-    from warpbiocell_gb300 import _lib
     from warpbiocell_gb300.simulation.batch import SpheroidBatch
     from warpbiocell_gb300.simulation.simulator import cell_step
     from warpbiocell_gb300.simulation.sweep import partition_runs

@@ -16,7 +16,7 @@ expressions the reference passes to its kernels.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_double, c_float, c_int32, c_int64, c_void_p
+from ctypes import c_double, c_float, c_int32, c_int64, c_void_p
 from dataclasses import dataclass, field
 
 import numpy as np

@@ -4,7 +4,6 @@ include/wbc.h declares, with the signatures the Python binding expects. No compu
 import ctypes
 import re
 import subprocess
-from pathlib import Path
 
 import pytest
 

@@ -3,8 +3,6 @@ estimate) against IEEE division: the refined reciprocal exhaustively over every 
 accepts, seeded operand pairs of every class on the device, and a batch against numpy's float32
 division on the host."""
 
-import ctypes
-
 import numpy as np
 import pytest
 import torch

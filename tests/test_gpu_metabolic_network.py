@@ -6,7 +6,6 @@ simulation/simulator.py:58-81 with fields/metabolism.py:99-111 and network/runti
 
 import numpy as np
 import pytest
-import torch
 
 from oracle import oracle as orc
 from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball

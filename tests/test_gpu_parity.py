@@ -5,8 +5,6 @@ slots, network states, SOR sweeps, positions), and against the reference's golde
 closed forms with the reference's own tolerances. Every test is marked ``gpu``.
 """
 
-import ctypes
-
 import numpy as np
 import pytest
 import torch

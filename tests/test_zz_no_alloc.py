@@ -7,8 +7,6 @@ library. This file is collected last on purpose: if it fails, a run that stops a
 failure has already run every other test. It must pass alone in a fresh process too.
 """
 
-import ctypes
-
 import numpy as np
 import pytest
 import torch
