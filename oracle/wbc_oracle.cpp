@@ -194,6 +194,7 @@ struct Region {
     float wall_rate;
 };
 
+// Trilinear sample of the region's SDF / gradient grid (kernels/geometry_kernels.py:16-44).
 inline float region_sample(const Region& R, const float* f, int stride, int i0, int j0, int k0, float fx, float fy,
                            float fz) {
     auto at = [&](int i, int j, int k) { return f[((static_cast<int64_t>(i) * R.ny + j) * R.nz + k) * stride]; };
@@ -204,6 +205,7 @@ inline float region_sample(const Region& R, const float* f, int stride, int i0, 
     return (c00 * (1.0f - fy) + c10 * fy) * (1.0f - fz) + (c01 * (1.0f - fy) + c11 * fy) * fz;
 }
 
+// Wall push of a cell outside the tissue region (kernels/geometry_kernels.py:59-79).
 inline void confine(const Region& R, float x, float y, float z, float radius, float& vx, float& vy, float& vz) {
     const float ux = std::min(std::max((x - R.ox) * R.inv_dx, 0.0f), static_cast<float>(R.nx - 1));
     const float uy = std::min(std::max((y - R.oy) * R.inv_dx, 0.0f), static_cast<float>(R.ny - 1));
@@ -353,6 +355,7 @@ void sor_sweeps(const SorParams& p, int sweeps, const int32_t* fixed, const T* d
     }
 }
 
+// kernels/field_kernels.py:153-182 (clamped trilinear, lerp x then y then z)
 template <typename T>
 void sample(int nx, int ny, int nz, T ox, T oy, T oz, T inv_dx, const T* field, int n, const T* pos, T* out) {
 #pragma omp parallel for schedule(static)
@@ -385,12 +388,14 @@ struct Program {
     const int32_t *ops, *args, *start, *length, *updatable;
 };
 
+// get_bit / set_bit on the packed words (kernels/network_kernels.py:35-47).
 inline uint64_t get_bit(const uint64_t* w, int idx) { return (w[idx >> 6] >> (idx & 63)) & 1ull; }
 inline void set_bit(uint64_t* w, int idx, uint64_t v) {
     const uint64_t mask = 1ull << (idx & 63);
     w[idx >> 6] = v ? (w[idx >> 6] | mask) : (w[idx >> 6] & ~mask);
 }
 
+// Postfix program of one node on a one-word bit stack (kernels/network_kernels.py:50-78).
 uint64_t eval_program(const Program& p, int node, const uint64_t* s) {
     uint64_t stack = 0;
     const int b = p.start[node], len = p.length[node];
@@ -415,6 +420,7 @@ uint64_t eval_program(const Program& p, int node, const uint64_t* s) {
     return stack & 1ull;
 }
 
+// Transition rate of one node in the MaBoSS chain (kernels/network_kernels.py:178-245).
 inline float node_rate(uint64_t on, uint64_t logic, int node, const float* ut, const float* uf, const float* dt_,
                        const float* df) {
     if (on == 0ull) return logic ? ut[node] : uf[node];
@@ -446,6 +452,8 @@ void orc_rng_init(int32_t seed, uint32_t* state, int64_t capacity) {
     for (int64_t i = 0; i < capacity; ++i) state[i] = rng_start(seed, static_cast<uint32_t>(i));
 }
 
+// Draws from the project's own streams, as wp.randf / wp.sample_unit_sphere_surface are used at
+// kernels/cell_kernels.py:129,151,183 (Warp's generator itself is not restated).
 void orc_rng_uniform(int32_t n, int32_t draws, uint32_t* state, float* out) {
     for (int i = 0; i < n; ++i) {
         const uint32_t inc = rng_increment(static_cast<uint32_t>(i));
@@ -457,6 +465,7 @@ void orc_rng_sphere(int32_t n, uint32_t* state, float* out) {
     for (int i = 0; i < n; ++i) unit_sphere(state[i], rng_increment(static_cast<uint32_t>(i)), out[3 * i], out[3 * i + 1], out[3 * i + 2]);
 }
 
+// The project's exp / log (wp.exp at kernels/cell_kernels.py:128,150).
 void orc_expf(int32_t n, const float* x, float* out) {
     for (int i = 0; i < n; ++i) out[i] = proj_expf(x[i]);
 }
@@ -473,6 +482,7 @@ void orc_contact_substep_f32(int32_t n, float* pos, const float* radius, float c
                            neighbor_count);
 }
 
+// The contact substep with the confinement push (cells/mechanics.py:75-110, kernels/geometry_kernels.py:59-79).
 void orc_contact_substep_region_f32(int32_t n, float* pos, const float* radius, float cell_size, int32_t dim,
                                     float query_radius, float rate, float dt, int32_t rnx, int32_t rny, int32_t rnz,
                                     float rox, float roy, float roz, float rinv_dx, const float* sdf,
@@ -599,6 +609,7 @@ static inline float oxygen_factor(float o, float hyp, float death) {
     return (o - death) / (hyp - death);
 }
 
+// kernels/cell_kernels.py:77-154 as launched by cells/lifecycle.py:96-132
 void orc_lifecycle_decide(const LifecycleParams* pp, int32_t n, int32_t* cell_state, float* age,
                           const int32_t* neighbor_count, const float* oxygen_local, const float* glucose_local,
                           const int32_t* fate_flags, uint32_t* rng_state, int32_t* divide_flag) {
@@ -656,6 +667,7 @@ int32_t orc_division_scan(int32_t n, const int32_t* flags, int32_t* offsets) {
     return run;
 }
 
+// kernels/cell_kernels.py:157-200
 void orc_place_daughters(int32_t count, float placement_factor, const int32_t* divide_flag, const int32_t* division_offset,
                          float* position, float* radius, int32_t* cell_state, int32_t* cell_type, float* age,
                          float* oxygen_local, float* glucose_local, uint32_t* rng_state, float* velocity,
@@ -691,12 +703,14 @@ void orc_place_daughters(int32_t count, float placement_factor, const int32_t* d
     }
 }
 
+// kernels/cell_kernels.py:203-208
 void orc_count_states(int32_t n, const int32_t* cell_state, int32_t* counts) {
     for (int i = 0; i < n; ++i)
         if (cell_state[i] >= 0 && cell_state[i] < 4) counts[cell_state[i]]++;
 }
 
 // ---- networks -----------------------------------------------------------------------------------------
+// kernels/network_kernels.py:81-95
 void orc_network_initialize(const Program* p, int32_t n, const float* p_on, uint32_t* rng_state, uint64_t* states) {
     for (int c = 0; c < n; ++c) {
         uint32_t rng = rng_state[c];
@@ -709,6 +723,7 @@ void orc_network_initialize(const Program* p, int32_t n, const float* p_on, uint
     }
 }
 
+// kernels/network_kernels.py:98-132
 void orc_network_clamp_inputs(int32_t n, int32_t n_words, int32_t n_clamps, const int32_t* node, const int32_t* source,
                               const float* threshold, const int32_t* above, const float* oxygen, const float* glucose,
                               const float* extra_a, const float* extra_b, uint64_t* states) {
@@ -729,6 +744,7 @@ void orc_network_clamp_inputs(int32_t n, int32_t n_words, int32_t n_clamps, cons
     }
 }
 
+// kernels/network_kernels.py:157-175 (every updatable node from the old state)
 void orc_network_update_sync(const Program* p, int32_t n, int32_t sweeps, uint64_t* states) {
 #pragma omp parallel for schedule(static)
     for (int c = 0; c < n; ++c) {
@@ -745,6 +761,7 @@ void orc_network_update_sync(const Program* p, int32_t n, int32_t sweeps, uint64
     }
 }
 
+// kernels/network_kernels.py:135-154
 void orc_network_update_async(const Program* p, int32_t n, int32_t n_updates, uint32_t* rng_state, uint64_t* states) {
 #pragma omp parallel for schedule(static)
     for (int c = 0; c < n; ++c) {
@@ -761,6 +778,7 @@ void orc_network_update_async(const Program* p, int32_t n, int32_t n_updates, ui
     }
 }
 
+// kernels/network_kernels.py:178-245
 void orc_network_update_maboss(const Program* p, int32_t n, float duration, int32_t max_events, const float* ut,
                                const float* uf, const float* dt_, const float* df, uint32_t* rng_state,
                                uint64_t* states) {
@@ -799,6 +817,7 @@ void orc_network_update_maboss(const Program* p, int32_t n, float duration, int3
     }
 }
 
+// kernels/network_kernels.py:248-268
 void orc_network_read_fates(int32_t n, int32_t n_words, int32_t np, int32_t na, int32_t ng, int32_t nn,
                             const uint64_t* states, int32_t* fate_flags) {
     for (int c = 0; c < n; ++c) {
@@ -812,6 +831,7 @@ void orc_network_read_fates(int32_t n, int32_t n_words, int32_t np, int32_t na, 
     }
 }
 
+// kernels/network_kernels.py:271-284
 void orc_network_inherit(int32_t count_before, int32_t n_words, const int32_t* divide_flag,
                          const int32_t* division_offset, uint64_t* states) {
     for (int i = 0; i < count_before; ++i) {
@@ -821,6 +841,7 @@ void orc_network_inherit(int32_t count_before, int32_t n_words, const int32_t* d
     }
 }
 
+// kernels/network_kernels.py:287-302
 void orc_network_count_on(int32_t n, int32_t n_words, int32_t n_query, const int32_t* nodes, int32_t living_only,
                           const int32_t* cell_state, const uint64_t* states, int32_t* counts) {
     for (int c = 0; c < n; ++c) {
