@@ -58,3 +58,34 @@ def test_host_only_entry_points_work_without_a_gpu(lib):
     # argument validation happens before any CUDA call
     assert lib.wbc_rng_init(0, None, 10, None) == -1
     assert lib.wbc_deposit(None, 0, None, None, None, None) == -1
+
+
+def test_status_codes_match_the_header():
+    from warpbiocell_gb300 import _lib
+
+    defines = dict(re.findall(r"#define (WBC_(?:OK|ERR_[A-Z]+))\s+\(?(-?\d+)\)?", HEADER.read_text()))
+    assert set(defines) >= {"WBC_OK", "WBC_ERR_INVALID", "WBC_ERR_CAPACITY", "WBC_ERR_CUDA", "WBC_ERR_TIMEOUT",
+                            "WBC_ERR_WORKSPACE"}
+    for name, value in defines.items():
+        assert getattr(_lib, name) == int(value), name
+
+
+def test_status_codes_map_to_the_reference_exceptions(lib):
+    from warpbiocell_gb300 import _lib
+
+    _lib.check(_lib.WBC_OK, "ok")
+    with pytest.raises(ValueError):  # parameter problems are ValueError, as in the reference's dataclasses
+        _lib.check(_lib.WBC_ERR_INVALID, "wbc_x")
+    for rc in (_lib.WBC_ERR_CUDA, _lib.WBC_ERR_WORKSPACE, _lib.WBC_ERR_TIMEOUT):
+        with pytest.raises(_lib.LibraryError):
+            _lib.check(rc, "wbc_x")
+    assert issubclass(_lib.LibraryError, RuntimeError)
+
+
+def test_noalloc_scan_limit_is_reported_before_any_device_work(lib):
+    # The size check comes first, so the (never dereferenced) host addresses are not touched.
+    buf = (ctypes.c_int32 * 2)()
+    addr = ctypes.addressof(buf)
+    rc = lib.wbc_division_scan_noalloc((1 << 25) + 1, addr, addr, addr, None)
+    assert rc == -1
+    assert b"WBC_NOALLOC_SCAN_MAX_CELLS" in lib.wbc_last_error()
