@@ -2,6 +2,7 @@
 tests/test_config.py, tests/test_sweep.py): host logic only, no device."""
 
 import math
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -160,3 +161,29 @@ def test_default_config_matches_documented_defaults():
     assert cfg.oxygen.boundary_mmHg == 38.0 and cfg.oxygen.solver.max_sweeps == 2000
     assert np.isclose(cfg.lifecycle.division_rate_per_h, 0.0289)
     assert cfg.mechanics.wall_rate_per_h == 10.0 and cfg.output.shell_width_um == 20.0
+
+
+REFERENCE_CONFIGS = Path("/root/reference/configs")
+
+
+@pytest.mark.skipif(not REFERENCE_CONFIGS.is_dir(), reason="the reference's configuration files are not on this machine")
+def test_reference_configuration_files_load_with_their_values():
+    """Every shipped configuration of the reference loads through the YAML subset reader, with the
+    values its files state (configs/*.yaml, configs/sweeps/oxygen_boundary.yaml)."""
+    base = {p.name: load_config(p) for p in sorted(REFERENCE_CONFIGS.glob("*.yaml"))}
+    assert set(base) == {"microc_oxygen.yaml", "tumor_in_ellipsoid.yaml", "tumor_spheroid.yaml",
+                         "tumor_spheroid_metabolic.yaml", "tumor_spheroid_network.yaml"}
+    for name, c in base.items():
+        assert c.simulation.dt_cells_h == 0.25 and c.simulation.seed == 0 and c.cells.max_cells == 200000, name
+        assert c.oxygen.grid.dx_um == 20.0, name
+    assert base["tumor_spheroid.yaml"].simulation.duration_h == 168.0
+    assert base["tumor_spheroid.yaml"].oxygen.boundary_mmHg == 38.0
+    assert base["microc_oxygen.yaml"].oxygen.boundary_mmHg == 50.0
+    ell = base["tumor_in_ellipsoid.yaml"]
+    assert ell.simulation.duration_h == 96.0 and ell.geometry.shape == "ellipsoid" and ell.geometry.seed_fill
+    met = base["tumor_spheroid_metabolic.yaml"]
+    assert [s.boundary_value for s in met.species] == [5.0, 1.0]
+    net = base["tumor_spheroid_network.yaml"]
+    assert net.network.enabled and net.network.update == "asynchronous" and net.network.updates_per_step == 200
+    spec = load_sweep(REFERENCE_CONFIGS / "sweeps" / "oxygen_boundary.yaml")
+    assert len(list(spec.runs())) == 15  # 5 boundary values x seeds [0, 1, 2]
