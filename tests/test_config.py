@@ -163,6 +163,54 @@ def test_default_config_matches_documented_defaults():
     assert cfg.mechanics.wall_rate_per_h == 10.0 and cfg.output.shell_width_um == 20.0
 
 
+
+def test_config_errors_name_the_offending_key():
+    # reference: tests/test_config.py:30-41 (unknown keys and type errors carry their dotted path)
+    with pytest.raises(ConfigError, match=r"config\.oxygen: unknown keys \['boundary_mmhg'\]"):
+        config_from_dict({"oxygen": {"boundary_mmhg": 40.0}})
+    for section, key, bad in (("cells", "initial_count", 12.5), ("oxygen", "enabled", "yes"),
+                              ("simulation", "device", 0)):
+        with pytest.raises(ConfigError, match=f"{section}.{key}"):
+            config_from_dict({section: {key: bad}})
+
+
+def test_numeric_strings_are_floats_and_words_are_not():
+    # reference: tests/test_config.py:44-50 (a YAML reader may hand over 7.2e6 as a string)
+    cfg = config_from_dict({"oxygen": {"diffusion_um2_per_h": "7.2e6"}})
+    assert cfg.oxygen.diffusion_um2_per_h == 7.2e6
+    with pytest.raises(ConfigError):
+        config_from_dict({"oxygen": {"diffusion_um2_per_h": "fast"}})
+
+
+def test_overrides_are_typed_like_yaml_values():
+    # reference: tests/test_config.py:53-63
+    data = {"oxygen": {"boundary_mmHg": 38.0}}
+    apply_overrides(data, ["oxygen.boundary_mmHg=150", "oxygen.grid.box_um=1200", "oxygen.enabled=false",
+                           "name=culture"])
+    cfg = config_from_dict(data)
+    assert (cfg.oxygen.boundary_mmHg, cfg.oxygen.grid.box_um, cfg.name) == (150.0, 1200.0, "culture")
+    assert cfg.oxygen.enabled is False
+
+
+def test_inconsistent_setups_are_caught_and_tight_budgets_warned():
+    # reference: tests/test_config.py:66-74
+    with pytest.raises(ConfigError, match="does not fit"):
+        config_from_dict({"cells": {"initial_count": 50_000}, "oxygen": {"grid": {"box_um": 400.0}}}).validate()
+    with pytest.raises(ValueError, match="overshoot"):
+        config_from_dict({"simulation": {"dt_mechanics_h": 0.1}}).validate()
+    with pytest.raises(ConfigError):
+        config_from_dict({"cells": {"initial_count": 10, "max_cells": 5}}).validate()
+    warnings = config_from_dict({"cells": {"initial_count": 1000, "max_cells": 2000},
+                                 "simulation": {"duration_h": 240.0}}).validate()
+    assert any("max_cells" in w for w in warnings)
+
+
+def test_disabled_oxygen_zeroes_the_lifecycle_oxygen_thresholds():
+    # reference: tests/test_config.py:77-80
+    params = config_from_dict({"oxygen": {"enabled": False}}).lifecycle_params()
+    assert params.hypoxia_threshold == 0.0 and params.death_threshold == 0.0
+
+
 REFERENCE_CONFIGS = Path("/root/reference/configs")
 
 

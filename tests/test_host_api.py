@@ -243,3 +243,44 @@ def test_truth_tables_of_random_networks_match_expressions():
     assert (small["arity"] <= 2).all() and (small["arity"] == -1).any()
     with pytest.raises(ValueError):
         net.truth_tables(arrays, max_inputs=7)
+
+
+def test_population_rejects_bad_shapes_before_any_device_work():
+    # reference: tests/test_state.py:21-27 (shape checks come before the device is resolved)
+    from warpbiocell_gb300.cells.state import CellPopulation
+
+    for pos, radii, kw in ((np.zeros((4, 2)), np.ones(4), {}), (np.zeros((4, 3)), np.ones(3), {}),
+                           (np.zeros((4, 3)), np.ones(4), {"capacity": 2})):
+        with pytest.raises(ValueError):
+            CellPopulation.from_numpy(pos, radii, **kw)
+
+
+def test_grid_geometry_helpers_and_solver_settings_validation():
+    # reference: tests/test_fields_numerical.py:145-157
+    from warpbiocell_gb300.fields.diffusion import SolverSettings
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    assert geom.shape == (21, 21, 21)
+    assert geom.origin == (-200.0, -200.0, -200.0) and geom.upper == (200.0, 200.0, 200.0)
+    inside = geom.contains(np.array([[0.0, 0.0, 0.0], [199.0, -199.0, 0.0], [201.0, 0.0, 0.0]]))
+    np.testing.assert_array_equal(inside, [True, True, False])
+    with pytest.raises(ValueError):
+        GridGeometry(origin=(0, 0, 0), dx=0.0, shape=(4, 4, 4))
+    with pytest.raises(ValueError):
+        SolverSettings(omega=2.0)
+
+
+def test_explicit_step_refuses_an_unstable_dt():
+    # reference: tests/test_fields_numerical.py:138-142 (checked before any device work)
+    from types import SimpleNamespace
+
+    from warpbiocell_gb300.fields.diffusion import UptakeKinetics, explicit_step, max_stable_dt
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+
+    field = SimpleNamespace(geometry=GridGeometry.centered_cube(100.0, 20.0))
+    kinetics = UptakeKinetics(diffusion=7.2e6, uptake_max=5.5e7, michaelis_k=1.0)
+    limit = max_stable_dt(field, kinetics)
+    assert limit == pytest.approx(20.0**2 / (6.0 * 7.2e6))
+    with pytest.raises(ValueError, match="stability"):
+        explicit_step(field, None, kinetics, 1.5 * limit, None)
