@@ -25,7 +25,7 @@ MODULES = ["cells/state.py", "cells/mechanics.py", "cells/lifecycle.py", "cells/
            "fields/oxygen.py", "fields/scalar_field.py", "fields/species.py", "network/expression.py",
            "network/model.py", "network/runtime.py", "simulation/config.py", "simulation/experiment.py",
            "simulation/simulator.py", "simulation/sweep.py", "geometry/region.py", "geometry/seeding.py",
-           "geometry/shapes.py", "io/checkpoints.py", "io/run_output.py", "metrics/population.py",
+           "geometry/shapes.py", "geometry/masks.py", "io/checkpoints.py", "io/run_output.py", "metrics/population.py",
            "metrics/timeseries.py"]
 
 

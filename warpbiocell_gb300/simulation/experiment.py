@@ -34,7 +34,7 @@ from warpbiocell_gb300.io.checkpoints import (load_checkpoint, restore_fields, r
                                              save_checkpoint)
 from warpbiocell_gb300.io.run_output import RunOutput
 from warpbiocell_gb300.metrics.population import population_summary, radial_profile, shell_radii
-from warpbiocell_gb300.simulation.config import ConfigError, ExperimentConfig
+from warpbiocell_gb300.simulation.config import ExperimentConfig
 from warpbiocell_gb300.simulation.simulator import cell_step
 
 
@@ -152,8 +152,14 @@ class Experiment:
     # ---- construction ----------------------------------------------------------------------------
     def _build_region(self) -> TissueRegion:
         g = self.config.geometry
-        if g.shape == "mask":
-            raise ConfigError("geometry.shape = mask needs a NIfTI reader (nibabel), which is not available")
+        if g.shape == "mask":  # reference: simulation/experiment.py:141-145
+            from warpbiocell_gb300.geometry.masks import load_nifti_mask, region_from_mask
+            from warpbiocell_gb300.simulation.config import _resolve_path
+
+            path = _resolve_path(g.mask_file, self.base_dir)
+            mask, voxel = load_nifti_mask(path, g.mask_label)
+            return region_from_mask(mask, voxel, self.config.grid_geometry(), mask_origin=tuple(g.mask_origin_um),
+                                    device=self.device, name=Path(g.mask_file).name)
         return TissueRegion.from_shape(self.config.tissue_shape(), self.config.grid_geometry(), device=self.device)
 
     def _initial_positions(self) -> np.ndarray:
