@@ -211,6 +211,39 @@ def test_disabled_oxygen_zeroes_the_lifecycle_oxygen_thresholds():
     assert params.hypoxia_threshold == 0.0 and params.death_threshold == 0.0
 
 
+
+def test_network_section_validation():
+    # reference: tests/test_experiment.py:166-180 (input sources must be fields of the run, input
+    # nodes must exist, and a network without phenotype_model = network only runs alongside the rules)
+    from tests.conftest import GOLDEN
+
+    with pytest.raises(ConfigError):
+        config_from_dict({"lifecycle": {"phenotype_model": "network"}}).validate()
+    data = {"network": {"enabled": True, "file": str(GOLDEN / "toy_network.bnd"), "cfg": str(GOLDEN / "toy_network.cfg"),
+                        "inputs": [{"node": "Signal", "source": "lactate", "threshold": 1.0}]}}
+    with pytest.raises(ConfigError):
+        config_from_dict(data).validate()  # no lactate field in this run
+    data["network"]["inputs"][0]["source"] = "oxygen"
+    data["network"]["inputs"].append({"node": "Nope", "source": "constant"})
+    with pytest.raises(ConfigError):
+        config_from_dict(data).validate()  # no such node
+    data["network"]["inputs"].pop()
+    assert any("phenotype_model = rules" in w for w in config_from_dict(data).validate())
+
+
+def test_species_section_validation():
+    # reference: tests/test_species.py:179-192
+    with pytest.raises(ConfigError, match="unique"):
+        config_from_dict({"species": [{"name": "oxygen"}]}).validate()
+    with pytest.raises(ConfigError, match=r"species\[0\]"):
+        config_from_dict({"species": [{"name": "glucose", "diffusion_um2_per_h": "fast"}]})
+    assert any("glucose" in w for w in config_from_dict({"lifecycle": {"necrosis_requires_glucose": True}}).validate())
+    # without a glucose species the lifecycle ignores the glucose rules
+    params = config_from_dict({"lifecycle": {"glucose_threshold_mM": 4.0,
+                                             "necrosis_requires_glucose": True}}).lifecycle_params()
+    assert params.glucose_threshold == 0.0 and params.necrosis_requires_glucose is False
+
+
 REFERENCE_CONFIGS = Path("/root/reference/configs")
 
 

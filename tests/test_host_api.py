@@ -284,3 +284,12 @@ def test_explicit_step_refuses_an_unstable_dt():
     assert limit == pytest.approx(20.0**2 / (6.0 * 7.2e6))
     with pytest.raises(ValueError, match="stability"):
         explicit_step(field, None, kinetics, 1.5 * limit, None)
+
+
+def test_lifecycle_network_fields_and_time_step_are_validated():
+    # reference: tests/test_network.py:364-368, tests/test_simulator.py:76-81
+    for kw in ({"phenotype_model": "graph"}, {"apoptosis_rate": -1.0}, {"necrosis_rate": -1.0}):
+        with pytest.raises(ValueError):
+            LifecycleParams(**kw)
+    with pytest.raises(ValueError):
+        TimeStepping(dt_cells=0.0)
