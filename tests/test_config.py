@@ -219,7 +219,8 @@ def test_network_section_validation():
 
     with pytest.raises(ConfigError):
         config_from_dict({"lifecycle": {"phenotype_model": "network"}}).validate()
-    data = {"network": {"enabled": True, "file": str(GOLDEN / "toy_network.bnd"), "cfg": str(GOLDEN / "toy_network.cfg"),
+    data = {"network": {"enabled": True, "file": str(GOLDEN / "toy_network.bnd"),
+                        "cfg": str(GOLDEN / "toy_network.cfg"),
                         "inputs": [{"node": "Signal", "source": "lactate", "threshold": 1.0}]}}
     with pytest.raises(ConfigError):
         config_from_dict(data).validate()  # no lactate field in this run
@@ -247,7 +248,8 @@ def test_species_section_validation():
 REFERENCE_CONFIGS = Path("/root/reference/configs")
 
 
-@pytest.mark.skipif(not REFERENCE_CONFIGS.is_dir(), reason="the reference's configuration files are not on this machine")
+@pytest.mark.skipif(not REFERENCE_CONFIGS.is_dir(),
+                    reason="the reference's configuration files are not on this machine")
 def test_reference_configuration_files_load_with_their_values():
     """Every shipped configuration of the reference loads through the YAML subset reader, with the
     values its files state (configs/*.yaml, configs/sweeps/oxygen_boundary.yaml)."""

@@ -222,7 +222,8 @@ def test_truth_tables_reproduce_reference_microc_steps_and_programs(golden):
         for node in upd:
             o = ops[start[node]:start[node] + length[node]].tolist()
             a = args[start[node]:start[node] + length[node]].tolist()
-            assert _table_step(tables, [node], row)[node] == bool(run_postfix(o, a, {i: int(v) for i, v in enumerate(row)}))
+            values = {i: int(v) for i, v in enumerate(row)}
+            assert _table_step(tables, [node], row)[node] == bool(run_postfix(o, a, values))
 
 
 def test_truth_tables_of_random_networks_match_expressions():
