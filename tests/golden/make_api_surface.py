@@ -20,7 +20,8 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REFERENCE = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
-MODULES = ["cells/state.py", "cells/mechanics.py", "cells/lifecycle.py", "cells/model.py", "cells/initialization.py",
+MODULES = ["device.py", "cells/state.py", "cells/mechanics.py", "cells/lifecycle.py", "cells/model.py",
+           "cells/initialization.py",
            "spatial/neighbors.py", "fields/densities.py", "fields/diffusion.py", "fields/metabolism.py",
            "fields/oxygen.py", "fields/scalar_field.py", "fields/species.py", "network/expression.py",
            "network/model.py", "network/runtime.py", "simulation/config.py", "simulation/experiment.py",

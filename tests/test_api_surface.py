@@ -34,7 +34,7 @@ def _extra_have_defaults(fn, n_ref: int) -> bool:
 
 
 def test_surface_fixture_covers_the_model_api():
-    assert len(SURFACE) == 27
+    assert len(SURFACE) == 28
     assert sum(len(v) for v in SURFACE.values()) >= 100
     for key in ("cells.state", "cells.mechanics", "cells.lifecycle", "spatial.neighbors", "fields.oxygen",
                 "fields.diffusion", "network.runtime", "simulation.simulator", "simulation.experiment"):

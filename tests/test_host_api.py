@@ -294,3 +294,15 @@ def test_lifecycle_network_fields_and_time_step_are_validated():
             LifecycleParams(**kw)
     with pytest.raises(ValueError):
         TimeStepping(dt_cells=0.0)
+
+
+def test_device_module_refuses_the_cpu():
+    # reference: device.py (resolve_device / cuda_available / synchronize); no CPU path here
+    import torch
+
+    from warpbiocell_gb300 import device
+
+    assert device.cuda_available() == torch.cuda.is_available()
+    with pytest.raises(RuntimeError):
+        device.resolve_device("cpu")
+    device.synchronize("cpu")  # nothing is queued on the host
