@@ -243,3 +243,48 @@ def test_oracle_every_cell_divides_once_into_its_slot(golden):
     np.testing.assert_allclose(np.linalg.norm(daughters - parents, axis=1), 8.0, rtol=1e-5)
     np.testing.assert_allclose(0.5 * (daughters + parents), pos, atol=1e-5)
     assert np.all(sim.age[:n] == 1.0) and np.all(sim.age[n:2 * n] == 0.0)
+
+
+def test_full_cell_steps_do_not_depend_on_the_thread_count():
+    """The oracle is timed on one thread and on all host threads; both must give the same bits
+    (contact per cell, exact integer deposit, red-black sweeps, max-residual, sequential scan)."""
+    import math
+
+    from warpbiocell_gb300.cells.initialization import clipped_normal_radii, uniform_ball
+    from warpbiocell_gb300.cells.lifecycle import LifecycleParams
+    from warpbiocell_gb300.cells.mechanics import ContactParams
+    from warpbiocell_gb300.fields.diffusion import SolverSettings
+    from warpbiocell_gb300.fields.oxygen import OxygenParams, species_params
+    from warpbiocell_gb300.fields.scalar_field import GridGeometry
+
+    n = 3000
+    pos = uniform_ball(n, 180.0, seed=4)
+    radii = clipped_normal_radii(n, 8.0, 0.8, 6.0, 10.0, seed=5)
+    geom = GridGeometry.centered_cube(600.0, 20.0)
+    og = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    s = species_params(OxygenParams(diffusion_coefficient=7.2e6, uptake_max=5.5385e7, michaelis_k=1.0,
+                                    boundary_value=38.0))
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=2000, check_every=20)
+    contact = ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0, margin=0.0, wall_rate=4.0)
+    lifecycle = LifecycleParams(division_rate=math.log(2.0) / 2.0, anoxic_death_rate=0.5, inhibition_threshold=8,
+                                hypoxia_threshold=5.0, death_threshold=1.0)
+    runs = []
+    try:
+        for threads in (1, 0):
+            orc.set_threads(threads)
+            sim = orc.OracleSim.from_numpy(pos, radii, capacity=3 * n, seed=7)
+            species = [orc.OracleSpecies(og, (0, 0, 0), s.boundary_value, s.diffusion, s.uptake_max, s.michaelis_k,
+                                         settings, production=s.production, name=s.name)]
+            sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
+            orc.metabolic_update(sim, species, {})
+            daughters = [orc.full_cell_step(sim, lifecycle, contact, 0.1, 0.1, species, {})[0] for _ in range(3)]
+            m = sim.count
+            runs.append((daughters, m, sim.position[:m].copy(), sim.cell_state[:m].copy(), sim.rng_state[:m].copy(),
+                         sim.neighbor_count[:m].copy(), species[0].values.copy()))
+    finally:
+        orc.set_threads(0)
+    one, many = runs
+    assert sum(one[0]) > 0  # the steps divide cells
+    assert one[0] == many[0] and one[1] == many[1]
+    for a, b in zip(one[2:], many[2:]):
+        np.testing.assert_array_equal(a, b)
