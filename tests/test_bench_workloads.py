@@ -74,3 +74,26 @@ def test_host_cpu_record():
     host = bench.host_cpu()
     assert host["cpu_count"] >= 1 and host["machine"]
     assert host["model"] is None or isinstance(host["model"], str)
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` on the 10k-cell workload: one JSON line with the GPU arm's metric,
+    unit and direction, a cpu_baseline describing the run and an e2e object with no copies."""
+    import json
+    import subprocess
+    import sys
+
+    out = subprocess.run([sys.executable, str(bench.ROOT / "bench.py"), "--impl", "reference", "--workload",
+                          "spheroid_10k_41", "--steps", "1", "--warmup", "0"], capture_output=True, text=True,
+                         timeout=600, check=True).stdout.strip().splitlines()
+    assert len(out) == 1
+    line = json.loads(out[0])
+    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True and line["config"]["workload"] == "spheroid_10k_41"
+    assert line["value"] > 0 and line["steps"] == 1
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    cpu = line["cpu_baseline"]
+    assert cpu["kind"] == "port" and cpu["value"] == line["value"] and cpu["cores"] >= 1 and cpu["sample"]
+    assert cpu["single_thread"]["cores"] == 1 and cpu["single_thread"]["value"] > 0
+    assert cpu["host"]["cpu_count"] >= 1
