@@ -124,3 +124,20 @@ def test_oxygen_can_be_disabled(tmp_path):
     assert result.summary["hypoxic_cells"] == 0
     assert np.isnan(result.summary["oxygen_cells_min_mmHg"])
     assert (tmp_path / "run" / "metrics.csv").exists()
+
+
+def test_experiment_in_a_tissue_region_from_a_mask_file(tmp_path):
+    # reference: simulation/experiment.py:141-145 (geometry.shape = mask, a NIfTI label image)
+    from tests.test_masks import _voxel_sphere, _write_single
+
+    mask, origin, _ = _voxel_sphere(n=30, voxel=20.0, radius=120.0)
+    _write_single(tmp_path / "lesion.nii.gz", np.where(mask, 2, 0).astype(np.int16), (0.02, 0.02, 0.02),
+                  compress=True)
+    data = _base(simulation__duration_h=1.0, cells__max_cells=6000)
+    data["geometry"] = {"enabled": True, "shape": "mask", "mask_file": str(tmp_path / "lesion.nii.gz"),
+                        "mask_label": 2, "mask_origin_um": [float(origin)] * 3, "seed_fill": True}
+    exp = Experiment(config_from_dict(data))
+    assert exp.region.name == "lesion.nii.gz" and exp.population.count > 500
+    result = exp.run()
+    assert result.status == "completed"
+    assert all(row["cells_outside_tissue"] == 0 for row in result.metrics)
