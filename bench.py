@@ -729,7 +729,8 @@ def run_reference_batched(args) -> dict:
                    "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
                    "boundary_mmHg": [sp["boundary"] for sp in specs]},
         "impl": "reference",
-        "cpu_baseline": {"value": round(value, 1), "unit": unit, "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": round(value, 1), "unit": unit, "cores": threads, "kind": "port", "sample": sample,
+                         "host": host_cpu()},
         "e2e": {"value": round(value, 1), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
 
