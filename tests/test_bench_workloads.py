@@ -97,3 +97,19 @@ def test_reference_arm_prints_the_contract_line():
     assert cpu["kind"] == "port" and cpu["value"] == line["value"] and cpu["cores"] >= 1 and cpu["sample"]
     assert cpu["single_thread"]["cores"] == 1 and cpu["single_thread"]["value"] > 0
     assert cpu["host"]["cpu_count"] >= 1
+
+
+@pytest.mark.parametrize("world", [2, 4, 8])
+def test_batched_sweep_shards_cover_every_instance_and_balance(world):
+    """The benchmark's batched sweep under torchrun: each rank batches its share of the 15 instances
+    (greedy longest-first on cells + nodes^3); the shares are disjoint, cover every instance, and the
+    busiest rank is within 5% of the mean load or holds a single instance that alone exceeds it."""
+    from warpbiocell_gb300.simulation.sweep import partition_runs
+
+    specs = bench.batch_specs(bench.WORKLOADS["batched_sweep_15"], seed=0)
+    costs = [float(s["cells"] + s["nodes"] ** 3) for s in specs]
+    shares = partition_runs(costs, world)
+    assert len(shares) == world and all(shares)
+    assert sorted(i for share in shares for i in share) == list(range(len(specs)))
+    loads = [sum(costs[i] for i in share) for share in shares]
+    assert max(loads) <= max(1.05 * sum(costs) / world, max(costs)) + 1e-9
