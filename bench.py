@@ -610,19 +610,20 @@ def run_reference(args) -> dict:
     sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
     orc.metabolic_update(sim, species, src)  # initial field solve, as the reference's Experiment.run
 
-    def step():
+    def step(timings=None):
         orc.full_cell_step(sim, P["lifecycle"], contact, stepping.dt_cells, stepping.dt_mechanics, species, src,
-                           network=onet)
+                           network=onet, timings=timings)
 
     for _ in range(args.warmup):
         step()
     cells = 0
+    stage_s: dict = {}
     t0 = time.perf_counter()
     done = 0
     budget_s = args.reference_budget_s
     for _ in range(args.steps):
         cells += sim.count
-        step()
+        step(stage_s)
         done += 1
         if time.perf_counter() - t0 > budget_s:
             break
@@ -649,6 +650,7 @@ def run_reference(args) -> dict:
         "config": {"workload": args.workload, **w, "grid_nodes": g.node_count},
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                         "stages_ms_per_step": {k: round(v * 1e3 / max(1, done), 3) for k, v in stage_s.items()},
                          "single_thread": single, "host": host_cpu()},
         "e2e": {"value": round(value, 1), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }

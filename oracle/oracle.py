@@ -16,6 +16,7 @@ expressions the reference passes to its kernels.
 from __future__ import annotations
 
 import ctypes
+import time
 from ctypes import c_double, c_float, c_int32, c_int64, c_void_p
 from dataclasses import dataclass, field
 
@@ -503,19 +504,32 @@ def metabolic_update(sim: OracleSim, species: list, production_source: dict) -> 
 
 
 def full_cell_step(sim: OracleSim, lifecycle, contact, dt_cells: float, dt_mechanics: float, species: list,
-                   production_source: dict, network: OracleNetwork | None = None, dim: int = 128):
-    """Mirror of simulation/simulator.py:58-81 with a MetabolicFields and an optional network."""
+                   production_source: dict, network: OracleNetwork | None = None, dim: int = 128,
+                   timings: dict | None = None):
+    """Mirror of simulation/simulator.py:58-81 with a MetabolicFields and an optional network.
+
+    ``timings``, when given, accumulates the seconds of each stage under "fields" (deposit, solves,
+    sampling), "network", "lifecycle" (decisions, scan, placement, inheritance) and "mechanics"."""
+    clock = time.perf_counter
+    t0 = clock()
     reports = metabolic_update(sim, species, production_source) if species else []
+    t1 = clock()
     if network is not None:
         network.step(sim, dt_cells)
+    t2 = clock()
     count_before = sim.count
     sim.decide_lifecycle(lifecycle, dt_cells)
     daughters = sim.commit_divisions(lifecycle)
     if network is not None and daughters:
         network.inherit(sim, count_before)
+    t3 = clock()
     substeps = max(1, int(round(dt_cells / dt_mechanics)))
     for _ in range(substeps):
         sim.contact_substep(contact.query_radius, dim, contact.query_radius, contact.rate, dt_mechanics)
+    if timings is not None:
+        t4 = clock()
+        for stage, dt in (("fields", t1 - t0), ("network", t2 - t1), ("lifecycle", t3 - t2), ("mechanics", t4 - t3)):
+            timings[stage] = timings.get(stage, 0.0) + dt
     return daughters, reports
 
 

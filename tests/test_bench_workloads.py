@@ -96,6 +96,9 @@ def test_reference_arm_prints_the_contract_line():
     cpu = line["cpu_baseline"]
     assert cpu["kind"] == "port" and cpu["value"] == line["value"] and cpu["cores"] >= 1 and cpu["sample"]
     assert cpu["single_thread"]["cores"] == 1 and cpu["single_thread"]["value"] > 0
+    stages = cpu["stages_ms_per_step"]
+    assert set(stages) == {"fields", "network", "lifecycle", "mechanics"}
+    assert sum(stages.values()) <= line["ms_per_step"] * 1.01 + 0.01
     assert cpu["host"]["cpu_count"] >= 1
 
 

@@ -277,7 +277,10 @@ def test_full_cell_steps_do_not_depend_on_the_thread_count():
                                          settings, production=s.production, name=s.name)]
             sim.contact_substep(contact.query_radius, 128, contact.query_radius, contact.rate, 0.0)
             orc.metabolic_update(sim, species, {})
-            daughters = [orc.full_cell_step(sim, lifecycle, contact, 0.1, 0.1, species, {})[0] for _ in range(3)]
+            timings = {} if threads == 0 else None  # stage timing must not change the results
+            daughters = [orc.full_cell_step(sim, lifecycle, contact, 0.1, 0.1, species, {}, timings=timings)[0]
+                         for _ in range(3)]
+            assert timings is None or set(timings) == {"fields", "network", "lifecycle", "mechanics"}
             m = sim.count
             runs.append((daughters, m, sim.position[:m].copy(), sim.cell_state[:m].copy(), sim.rng_state[:m].copy(),
                          sim.neighbor_count[:m].copy(), species[0].values.copy()))
