@@ -291,7 +291,9 @@ int wbc_division_scan(int32_t n, const int32_t* divide_flag, int32_t* division_o
  * the process exits. It accepts at most WBC_NOALLOC_SCAN_MAX_CELLS cells and returns
  * WBC_ERR_INVALID (with wbc_last_error explaining) beyond that. The first call on a device looks
  * up that array's device address (once per device, with the device current); make that first
- * call before any stream capture. Every call shares the array, which keeps the previous call's
+ * call before any stream capture. The cached address belongs to the device's current context:
+ * after cudaDeviceReset it is stale, so a process that resets a device must not call this entry
+ * point on that device again. Every call shares the array, which keeps the previous call's
  * partials (each call overwrites the entries it reads, so nothing needs clearing): calls that
  * overlap on the GPU, on any stream, race and must be serialised by the caller. Allocates nothing
  * and frees nothing. This entry point has no counterpart in the reference. */

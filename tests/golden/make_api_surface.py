@@ -15,11 +15,16 @@ from __future__ import annotations
 
 import ast
 import json
+import os
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# The reference project's checkout: the first argument, else $WBC_REFERENCE_ROOT.
+_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("WBC_REFERENCE_ROOT")
+if not _root:
+    sys.exit(f"usage: {Path(__file__).name} <reference checkout> (or set WBC_REFERENCE_ROOT)")
+REFERENCE = Path(_root)
 MODULES = ["device.py", "cells/state.py", "cells/mechanics.py", "cells/lifecycle.py", "cells/model.py",
            "cells/initialization.py",
            "spatial/neighbors.py", "fields/densities.py", "fields/diffusion.py", "fields/metabolism.py",

@@ -12,13 +12,18 @@ Output (committed): tests/golden/masks.npz. The tests never import the reference
 
 from __future__ import annotations
 
+import os
 import sys
 from pathlib import Path
 
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-REFERENCE = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+# The reference project's checkout: the first argument, else $WBC_REFERENCE_ROOT.
+_root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("WBC_REFERENCE_ROOT")
+if not _root:
+    sys.exit(f"usage: {Path(__file__).name} <reference checkout> (or set WBC_REFERENCE_ROOT)")
+REFERENCE = Path(_root)
 
 
 def _cases():

@@ -2,6 +2,7 @@
 tests/test_config.py, tests/test_sweep.py): host logic only, no device."""
 
 import math
+import os
 from pathlib import Path
 
 import numpy as np
@@ -245,11 +246,13 @@ def test_species_section_validation():
     assert params.glucose_threshold == 0.0 and params.necrosis_requires_glucose is False
 
 
-REFERENCE_CONFIGS = Path("/root/reference/configs")
+# The reference project's checkout, when one is on this machine (WBC_REFERENCE_ROOT names it).
+REFERENCE_CONFIGS = Path(os.environ.get("WBC_REFERENCE_ROOT", "")) / "configs" if os.environ.get("WBC_REFERENCE_ROOT") \
+    else None
 
 
-@pytest.mark.skipif(not REFERENCE_CONFIGS.is_dir(),
-                    reason="the reference's configuration files are not on this machine")
+@pytest.mark.skipif(REFERENCE_CONFIGS is None or not REFERENCE_CONFIGS.is_dir(),
+                    reason="WBC_REFERENCE_ROOT does not name a checkout of the reference with its configs")
 def test_reference_configuration_files_load_with_their_values():
     """Every shipped configuration of the reference loads through the YAML subset reader, with the
     values its files state (configs/*.yaml, configs/sweeps/oxygen_boundary.yaml)."""

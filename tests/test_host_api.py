@@ -105,11 +105,13 @@ def test_microc_programs_reproduce_reference_synchronous_steps(golden):
 
 
 def test_microc_reader_on_reference_file_if_present(golden):
+    import os
     from pathlib import Path
 
-    net_dir = Path("/root/reference/configs/networks")
-    if not (net_dir / "microc_jaya.bnd").exists():
-        pytest.skip("reference model files are not present on this machine")
+    root = os.environ.get("WBC_REFERENCE_ROOT")
+    net_dir = Path(root or ".") / "configs" / "networks"
+    if not root or not (net_dir / "microc_jaya.bnd").exists():
+        pytest.skip("WBC_REFERENCE_ROOT does not name a checkout of the reference with its model files")
     net = load_network(net_dir / "microc_jaya.bnd", net_dir / "microc_jaya.cfg")
     g = golden("network_microc")
     assert net.names == [str(x) for x in g["names"]]

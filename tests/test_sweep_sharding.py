@@ -159,3 +159,57 @@ def test_two_gloo_ranks_run_disjoint_shares_and_gather_the_summary(tmp_path, mon
         written = list(csv.DictReader(f))
     assert [r["label"] for r in written] == labels
     assert [int(float(r["final_cells"])) for r in written] == [int(row["final_cells"]) for row in single]
+
+
+def _is_failing(config) -> bool:
+    return config.cells.initial_count == 3000 and config.oxygen.grid.dx_um == 10.0 and config.simulation.seed == 0
+
+
+def _failing_experiment(config, run_dir, device):
+    # one run (3000 cells, 10 um spacing, seed 0) fails, as a run that ran out of device memory would
+    if _is_failing(config):
+        raise RuntimeError("simulated failure of one run")
+    return _fake_experiment(config, run_dir, device)
+
+
+def _failing_worker(rank, world, port, out_dir, ran_dir, queue):
+    import torch.distributed as dist
+    from datetime import timedelta
+
+    os.environ["WBC_TEST_RAN"] = os.path.join(ran_dir, f"rank{rank}.txt")
+    sw._run_experiment = _failing_experiment
+    # a short collective timeout: a rank left waiting in the gather would fail the test by time
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world,
+                            timeout=timedelta(seconds=60))
+    try:
+        sw.Sweep(_spec(), BASE).run(out_dir, batched=False)
+        queue.put((rank, "no error"))
+    except sw.SweepRankError as exc:
+        queue.put((rank, f"SweepRankError: {exc}"))
+    except Exception as exc:  # noqa: BLE001
+        queue.put((rank, f"{type(exc).__name__}: {exc}"))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_a_failing_run_on_one_rank_raises_on_every_rank_without_a_hang(tmp_path):
+    world = 2
+    spec = _spec()
+    sweep = sw.Sweep(spec, BASE)
+    parts = sw.partition_runs([sw.run_cost(c) for _, _, c in sweep.configs], world)
+    failing = [r for r in range(world) for i in parts[r] if _is_failing(sweep.configs[i][2])]
+    assert len(failing) == 1  # one rank's share holds the failing run; the other rank's runs all succeed
+    ctx = mp.get_context("spawn")
+    queue = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_failing_worker, args=(r, world, port, str(tmp_path / "sweep"), str(tmp_path), queue))
+             for r in range(world)]
+    for p in procs:
+        p.start()
+    got = dict(queue.get(timeout=50) for _ in range(world))  # well inside the 60 s collective timeout
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank in range(world):
+        assert got[rank].startswith("SweepRankError"), got[rank]
+        assert f"rank {failing[0]}" in got[rank] and "simulated failure of one run" in got[rank]

@@ -50,6 +50,33 @@ def test_no_alloc_scan_matches_workspace_scan_on_two_calls_in_a_row():
         assert int(got_total.item()) == int(ref_total.item()) == int(flags.sum().item())
 
 
+def test_no_alloc_scan_of_no_cells_writes_a_zero_total():
+    # n = 0 launches nothing and only sets the total, as the workspace scan does
+    empty = torch.zeros(0, dtype=torch.int32, device=DEV)
+    ref, ref_total = _scan_with_workspace(empty)
+    got, got_total = _scan_no_alloc(empty)
+    torch.cuda.synchronize()
+    assert got.numel() == ref.numel() == 0
+    assert int(got_total.item()) == int(ref_total.item()) == 0
+
+
+def test_no_alloc_scan_at_its_exact_limit():
+    # WBC_NOALLOC_SCAN_MAX_CELLS cells fill every tile partial, the total's entry included
+    n = 33_554_432
+    rng = np.random.default_rng(7)
+    flags = torch.zeros(n, dtype=torch.int32, device=DEV)
+    hits = torch.as_tensor(rng.choice(n, size=50_000, replace=False), device=DEV)
+    flags[hits] = 1
+    flags[-1] = 1  # the last cell divides: its offset is the total
+    ref, ref_total = _scan_with_workspace(flags)
+    got, got_total = _scan_no_alloc(flags)
+    torch.cuda.synchronize()
+    assert torch.equal(got, ref)
+    assert int(got_total.item()) == int(ref_total.item()) == int(flags.sum().item())
+    assert int(got[-1].item()) == int(got_total.item())
+    del flags, ref, got
+
+
 def test_no_alloc_scan_rejects_sizes_beyond_its_limit():
     lib = _lib.load()
     dummy = torch.zeros(1, dtype=torch.int32, device=DEV)

@@ -137,6 +137,11 @@ def run_cost(config) -> float:
     return float(steps) * float(config.cells.initial_count + nodes)
 
 
+class SweepRankError(RuntimeError):
+    """A sharded sweep in which at least one rank's runs raised; raised on every rank, after the
+    ranks have exchanged what happened, with each failing rank's runs and error."""
+
+
 def partition_runs(costs: list[float], world: int) -> list[list[int]]:
     """Run indices per rank: longest run first onto the least loaded rank (lowest rank on ties),
     each share in sweep order. Deterministic, so every rank computes the same partition."""
@@ -256,20 +261,38 @@ class Sweep:
         use_batch = batched and batchable([c for _, _, c in configs])
         mine = partition_runs([run_cost(c) for _, _, c in configs], world)[rank]
         done: list[tuple[int, dict]] = []
-        if mine:
-            if use_batch:
-                results = run_batched([configs[i][2] for i in mine], [out_dir / configs[i][0] for i in mine],
-                                      device=device, log=log)
-            else:
-                results = [_run_experiment(configs[i][2], out_dir / configs[i][0], device) for i in mine]
-            for i, result in zip(mine, results):
-                label, values, config = configs[i]
-                done.append((i, self._row(label, values, config, result, out_dir / label)))
-                if log:
-                    log(f"    [rank {rank}] {label}: {result.status}  cells={result.metrics[-1]['cells']}")
+        failure: dict | None = None
+        # Whatever happens to this rank's runs, it still takes part in the gather below: a rank
+        # that raised before it would leave every other rank blocked in the collective until the
+        # process group times out. Its error travels in the gathered data instead and every rank
+        # raises it after the gather.
+        try:
+            if mine:
+                if use_batch:
+                    results = run_batched([configs[i][2] for i in mine], [out_dir / configs[i][0] for i in mine],
+                                          device=device, log=log)
+                else:
+                    results = [_run_experiment(configs[i][2], out_dir / configs[i][0], device) for i in mine]
+                for i, result in zip(mine, results):
+                    label, values, config = configs[i]
+                    done.append((i, self._row(label, values, config, result, out_dir / label)))
+                    if log:
+                        log(f"    [rank {rank}] {label}: {result.status}  cells={result.metrics[-1]['cells']}")
+        except Exception as exc:  # noqa: BLE001 - re-raised on every rank after the gather
+            failure = {"rank": rank, "runs": [configs[i][0] for i in mine if i not in {j for j, _ in done}],
+                       "error": f"{type(exc).__name__}: {exc}"}
+            local_exc: Exception | None = exc
+        else:
+            local_exc = None
         gathered: list = [None] * world
-        dist.all_gather_object(gathered, done)
-        rows = [row for _, row in sorted((item for part in gathered for item in part), key=lambda t: t[0])]
+        dist.all_gather_object(gathered, {"rows": done, "failure": failure})
+        failures = [part["failure"] for part in gathered if part["failure"] is not None]
+        if failures:
+            what = "; ".join(f"rank {f['rank']} ({', '.join(f['runs']) or 'no run'}): {f['error']}" for f in failures)
+            if local_exc is not None:
+                raise SweepRankError(f"sweep failed on {len(failures)} of {world} ranks: {what}") from local_exc
+            raise SweepRankError(f"sweep failed on {len(failures)} of {world} ranks: {what}")
+        rows = [row for _, row in sorted((item for part in gathered for item in part["rows"]), key=lambda t: t[0])]
         if rank == 0:
             if self.sweep_path is not None:
                 shutil.copyfile(self.sweep_path, out_dir / "sweep.yaml")
