@@ -43,8 +43,29 @@ ROOT = Path(__file__).resolve().parent
 if str(ROOT) not in sys.path:
     sys.path.insert(0, str(ROOT))
 
-METRIC = "cell-steps/s @1M cells+161^3 O2 (coupled cell step)"
 UNIT = "cell-steps/s"
+
+
+def metric_for(workload: str) -> str:
+    """The metric label of a workload (the cell count and grid it is quoted on)."""
+    w = WORKLOADS[workload]
+    if w.get("batched"):
+        return "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)"
+    if w.get("adjoint"):
+        return "adjoint backward time / forward time (100k cells, 81^3 O2, K=64 contact steps)"
+    cells = w["cells"]
+    count = f"{cells // 1_000_000}M" if cells % 1_000_000 == 0 else f"{cells // 1000}k"
+    n = int(round(w["box_um"] / w["dx_um"])) + 1
+    fields = "O2 + glucose + lactate, 106-node networks" if w.get("metabolic") else "O2"
+    return f"cell-steps/s @{count} cells+{n}^3 {fields} (coupled cell step)"
+
+
+def workload_config(workload: str, grid_nodes: int | None = None) -> dict:
+    """The `config` object of both arms: the workload's name and defining sizes only."""
+    cfg = {"workload": workload, **WORKLOADS[workload]}
+    if grid_nodes is not None:
+        cfg["grid_nodes"] = grid_nodes
+    return cfg
 
 WORKLOADS = {
     "spheroid_1M_161": dict(cells=1_000_000, ball_um=1200.0, box_um=2400.0, dx_um=15.0, boundary=100.0),
@@ -69,10 +90,11 @@ WORKLOADS = {
                              cells_lo=2_000, cells_hi=200_000, nodes_lo=41, nodes_hi=121, box_over_radius=2.5),
 }
 
-# DRAM bytes per colour half-sweep of the resident SOR solver at 161^3: one `ncu --set full`
-# capture of k_sor_resident (the benchmark's initial solve, 780 sweeps = 1560 half-sweeps) read
-# and wrote 36.9 MB in total, tile load, coefficient copy and write-back included.
-SOR_DRAM_BYTES_PER_HALF_SWEEP = 23620.0
+# ncu figures of one warm k_sor_resident launch (one steady-state solve) of the 1M-cell / 161^3
+# workload, `profiles/k_sor_resident_spheroid_1M_161.md`: DRAM bytes read + written by the launch,
+# the sweeps it ran, its warp instructions per node update and its issue-active fraction.
+SOR_NCU = {"dram_bytes": 36.9e6, "sweeps": 780, "warp_inst_per_node_update": 11.99e9 / (780 * 4173281.0),
+           "issue_active": 0.788, "source": "profiles/k_sor_resident_spheroid_1M_161.md"}
 
 DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
 VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
@@ -497,19 +519,32 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
     peak_source = "measured" if "hbm_gbs" in peaks else "fallback"
     roofline = None
     if dominant == "sor":
-        # Unit: one colour half-sweep of the resident solver. Bytes: what a streaming half-sweep
-        # must move (field read, own-colour n_eff read, own-colour write: 8 B per node); duration:
-        # the solve time per step over its 2 x sweeps half-sweeps (residual checks included).
+        # Unit: one launch of the resident solver = one steady-state solve (all its sweeps and
+        # residual checks). Algorithmic bytes: the field read and written once and n_eff read once,
+        # 12 B per node (16 with a production term), whatever the sweep count; the solve then runs
+        # on chip, so HBM is not its binding roof: the issue rate is, reported beside it.
         s = stages["sor"]
-        half_sweeps = 2.0 * sum(r0["sweeps"]) / max(1, len(r0["sweeps"]))
-        unit_ms = s["ms"] / steps / half_sweeps
-        nbytes = 8.0 * nodes
-        achieved = nbytes / (unit_ms / 1e3) / 1e9
-        traffic = SOR_DRAM_BYTES_PER_HALF_SWEEP if r0.get("sor_path") == 2 else None
-        roofline = {"bound": "hbm", "kernel": "k_sor_resident (per colour half-sweep)", "achieved": round(achieved, 1),
-                    "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
-                    "peak_source": peak_source, "bytes_per_unit": nbytes, "unit_us": round(unit_ms * 1e3, 3),
-                    "node_updates_per_s": round(nodes * half_sweeps / 2.0 / (s["ms"] / steps / 1e3), 1)}
+        launch_ms = s["ms"] / max(1, s["calls"])
+        sweeps_per_launch = sum(r0["sweeps"]) / max(1, len(r0["sweeps"]))
+        nbytes = 12.0 * nodes
+        achieved = nbytes / (launch_ms / 1e3) / 1e9
+        traffic = None
+        if r0.get("sor_path") == 2 and args.workload == "spheroid_1M_161":
+            traffic = round(SOR_NCU["dram_bytes"], 0)
+        half_us = launch_ms * 1e3 / (2.0 * sweeps_per_launch)
+        updates_per_s = nodes * sweeps_per_launch / (launch_ms / 1e3)
+        roofline = {"bound": "hbm", "kernel": "k_sor_resident (one launch = one steady-state solve)",
+                    "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 6),
+                    "traffic": traffic, "peak_source": peak_source, "bytes_per_launch": nbytes,
+                    "launch_us": round(launch_ms * 1e3, 2), "sweeps_per_launch": round(sweeps_per_launch, 1),
+                    "issue_roof": {
+                        "what": "the solve is on chip and bound by instruction issue, not HBM",
+                        "node_updates_per_s": round(updates_per_s, 1),
+                        "half_sweep_us": round(half_us, 3),
+                        "warp_inst_per_node_update_ncu": round(SOR_NCU["warp_inst_per_node_update"], 3),
+                        "issue_active_ncu": SOR_NCU["issue_active"],
+                        "source": SOR_NCU["source"]},
+                    "streaming_equivalent_GBps": round(8.0 * nodes / (half_us / 1e6) / 1e9, 1)}
     elif dominant:
         s = stages[dominant]
         unit_ms = s["ms"] / max(1, s["calls"])
@@ -539,7 +574,7 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
                                    (v["ms"] / steps / 1e3) / 1e9, 1) if v["ms"] > 0 and k != "sor" else None}
                  for k, v in sorted(stages.items(), key=lambda kv: -kv[1]["ms"])}
     out = {
-        "metric": METRIC,
+        "metric": metric_for(args.workload),
         "value": round(value, 1),
         "unit": UNIT,
         "n_gpus": world,
@@ -551,11 +586,11 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
         "vs_baseline": None,
         "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
         "data": "synthetic (seeded uniform ball, clipped-normal radii)",
-        "config": {"workload": args.workload, **WORKLOADS[args.workload], "grid_nodes": nodes,
-                   "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT, "mechanics_substeps": 1,
-                   "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2: per-step working set (cells ~60 MB + int64 accumulator "
-                         f"{4 * 8 * nodes / 1e6:.0f} MB + fields) exceeds the 129 MB L2"},
+        "config": workload_config(args.workload, nodes),
+        "notes": {"sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT, "mechanics_substeps": 1,
+                  "parallelism": f"replicas x{world}",
+                  "l2": "inputs larger than L2: per-step working set (cells ~60 MB + int64 accumulator "
+                        f"{4 * 8 * nodes / 1e6:.0f} MB + fields) exceeds the 129 MB L2"},
         "gpu_launches": int(r0["launches"]),
         "e2e": {"value": round(e2e_value, 1), "unit": UNIT, "h2d_bytes_per_step": int(r0["h2d"]),
                 "d2h_bytes_per_step": int(r0["d2h"])},
@@ -643,11 +678,12 @@ def run_reference(args) -> dict:
     single = {"value": round(n1 / one_s, 1), "unit": UNIT, "cores": 1,
               "sample": f"the next full cell step ({n1} cells) on one thread; {one_s:.2f} s"}
     return {
-        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": done, "warmup": args.warmup,
+        "metric": metric_for(args.workload), "value": round(value, 1), "unit": UNIT, "n_gpus": 0, "steps": done,
+        "warmup": args.warmup,
         "ms_per_step": round(elapsed * 1e3 / max(1, done), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
         "data": "synthetic (seeded uniform ball, clipped-normal radii)",
-        "config": {"workload": args.workload, **w, "grid_nodes": g.node_count},
+        "config": workload_config(args.workload, g.node_count),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 1), "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
                          "stages_ms_per_step": {k: round(v * 1e3 / max(1, done), 3) for k, v in stage_s.items()},
@@ -722,14 +758,12 @@ def run_reference_batched(args) -> dict:
               f"run here: warp-lang is absent) on {threads} OpenMP threads")
     unit = "cell-steps/s"
     return {
-        "metric": "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)",
+        "metric": metric_for(args.workload),
         "value": round(value, 1), "unit": unit, "n_gpus": 0, "steps": done, "warmup": args.warmup,
         "ms_per_step": round(elapsed * 1e3 / max(1, done), 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
         "data": "synthetic (seeded uniform balls, clipped-normal radii)",
-        "config": {"workload": args.workload, "instances": len(specs),
-                   "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
-                   "boundary_mmHg": [sp["boundary"] for sp in specs]},
+        "config": batch_config(args.workload, specs),
         "impl": "reference",
         "cpu_baseline": {"value": round(value, 1), "unit": unit, "cores": threads, "kind": "port", "sample": sample,
                          "host": host_cpu()},
@@ -764,6 +798,12 @@ def batch_specs(w: dict, seed: int) -> list[dict]:
             specs.append(dict(cells=cells, ball=radius, nodes=nodes, dx=box / (nodes - 1), boundary=boundary,
                               seed=1000 * seed + 17 * len(specs) + s))
     return specs
+
+
+def batch_config(workload: str, specs: list[dict]) -> dict:
+    """The `config` object of both arms of the batched workload."""
+    return {"workload": workload, "instances": len(specs), "cells": [sp["cells"] for sp in specs],
+            "grid_nodes_per_side": [sp["nodes"] for sp in specs], "boundary_mmHg": [sp["boundary"] for sp in specs]}
 
 
 def build_member(spec: dict, P: dict, dev):
@@ -831,6 +871,9 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
         return cell_steps
 
     run_plain(args.warmup)
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    time.sleep(0.3)
     plain_cells, plain_ms = timed(lambda: run_plain(args.steps))
 
     # The same 15 runs as one batch: the first warm-up step outside the graph, then capture.
@@ -843,6 +886,7 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     if args.warmup > 1:
         batch.step(args.warmup - 1)
     _, batch_ms = timed(lambda: batch.step(args.steps))
+    clocks = sampler.stop()
     counts = batch.sync()
     identical = batch.status_codes() == [0] * len(specs)
     for m, p in zip(members, plain):
@@ -880,17 +924,16 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     plain_value = plain_cells / (plain_ms / 1e3)
     nodes = sum(sp["nodes"] ** 3 for sp in specs)
     return {
-        "metric": "cell-steps/s (15-spheroid batched sweep, one launch per stage, graph-captured step)",
+        "metric": metric_for(args.workload),
         "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(batch_ms / steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 fields/positions, int64 deposit, uint32 streams",
         "data": "synthetic (seeded uniform balls, clipped-normal radii)",
-        "config": {"workload": args.workload, "instances": len(specs),
-                   "cells": [sp["cells"] for sp in specs], "grid_nodes_per_side": [sp["nodes"] for sp in specs],
-                   "boundary_mmHg": [sp["boundary"] for sp in specs], "total_grid_nodes": nodes,
-                   "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT,
-                   "parallelism": "one GPU, instances batched" if world == 1 else
-                   f"{world} GPUs, instances sharded by rank and batched on each"},
+        "config": batch_config(args.workload, specs),
+        "notes": {"total_grid_nodes": nodes, "sor": "omega 1.8, tol 1e-6, check every 20, max 2000", "dt_h": DT,
+                  "parallelism": "one GPU, instances batched" if world == 1 else
+                  f"{world} GPUs, instances sharded by rank and batched on each"},
+        "clocks": clocks,
         "sequential": {"value": round(plain_value, 1), "ms_per_step": round(plain_ms / steps, 4),
                        "what": "the same runs through the plain per-run path (cell_step), one after another "
                                "(on each rank, its share)"},
@@ -950,8 +993,12 @@ def run_adjoint(args) -> dict:
         return out, e0.elapsed_time(e1)
 
     fwd_ms, bwd_ms = [], []
+    sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    sampler.start()
+    time.sleep(0.3)
     launches0 = _lib.launch_count()
-    for rep in range(max(1, args.warmup) + max(1, args.steps)):
+    reps = max(1, args.warmup) + max(1, args.steps)
+    for rep in range(reps):
         v = v0.clone().requires_grad_(True)
         scal = {k: torch.tensor(val, dtype=torch.float64, requires_grad=True) for k, val in theta.items()}
         (u, x), f_ms = timed(lambda: CoupledSteadyState.apply(v, scal["km"], scal["diffusion"], scal["boundary"],
@@ -962,60 +1009,95 @@ def run_adjoint(args) -> dict:
             fwd_ms.append(f_ms)
             bwd_ms.append(b_ms)
     launches = _lib.launch_count() - launches0
+    clocks = sampler.stop()
     grads = {k: float(t.grad) for k, t in scal.items()}
     grad_v = v.grad.double().cpu().numpy()
     result = {
-        "metric": "adjoint backward time / forward time (100k cells, 81^3 O2, K=64 contact steps)",
+        "metric": metric_for(args.workload),
         "value": round(float(np.median(bwd_ms)) / float(np.median(fwd_ms)), 3), "unit": "x forward",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 forward, fp32 adjoint with fp64 scalar sums",
         "data": "synthetic (seeded uniform ball, clipped-normal radii, log-normal Vmax)",
-        "config": {"workload": args.workload, **w},
+        "config": workload_config(args.workload),
         "forward_ms": round(float(np.median(fwd_ms)), 3), "backward_ms": round(float(np.median(bwd_ms)), 3),
         "forward_sweeps": model.last_forward_sweeps, "adjoint_sweeps": model.last_adjoint_sweeps,
         "adjoint_converged": model.last_adjoint_converged,
         "gpu_launches": int(launches),
+        "launches_per_forward_backward": round(launches / reps, 1),
         "gradients": {**grads, "vmax_norm": float(np.linalg.norm(grad_v))},
+        "clocks": clocks,
     }
     if not args.skip_cpu:
-        # Central differences of the FP64 re-run (oracle, double contact steps / exact deposit /
-        # double SOR to 1e-13) on the scalar parameters and one random Vmax direction.
-        sys.path.insert(0, str(ROOT))
-        from oracle import oracle as orc
-
-        orc.set_threads(os.cpu_count() or 1)
-        u64, rho64 = u_t.cpu().numpy(), rho_t.cpu().numpy()
-        og = orc.Geometry(geom.origin, geom.dx, geom.shape)
-
-        def loss64(vm, km, diffusion, boundary, stiffness):
-            field, p, _ = orc.adjoint_forward_f64(pos, radii, vm, og, w["steps"], DT, stiffness, 20.0, 20.0, 128,
-                                                  diffusion, km, boundary)
-            return float(((field - u64) ** 2).sum() + ((np.linalg.norm(p - p.mean(axis=0), axis=1) - rho64) ** 2).sum())
-
-        vm64 = vmax.astype(np.float64)
-        rel = 1e-4
-        errors = {}
-        t0 = time.perf_counter()
-        for name in ("km", "stiffness"):
-            h = rel * theta[name]
-            hi, lo = dict(theta), dict(theta)
-            hi[name] += h
-            lo[name] -= h
-            fd = (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * h)
-            errors[name] = abs(grads[name] - fd) / abs(fd)
-        d = np.where(rng.random(vmax.size) < 0.5, -1.0, 1.0)
-        fd = (loss64(vm64 * (1 + rel * d), **theta) - loss64(vm64 * (1 - rel * d), **theta)) / (2 * rel)
-        errors["vmax_direction"] = abs(float((grad_v * vm64 * d).sum()) - fd) / abs(fd)
-        # the stiffness derivative at two more step sizes (how well the difference itself settles)
-        for r in (1e-3, 1e-5):
-            hi, lo = dict(theta), dict(theta)
-            hi["stiffness"] *= 1 + r
-            lo["stiffness"] *= 1 - r
-            fd = (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * r * theta["stiffness"])
-            errors[f"stiffness_h{r:g}"] = abs(grads["stiffness"] - fd) / abs(fd)
-        result["fp64_central_difference_rel_error"] = {k: float(f"{e:.3g}") for k, e in errors.items()}
-        result["fp64_check_s"] = round(time.perf_counter() - t0, 1)
+        result.update(adjoint_fp64_checks(args, w, pos, radii, geom, vmax, theta, grads, grad_v, u_t, rho_t, rng))
     return result
+
+
+def adjoint_fp64_checks(args, w, pos, radii, geom, vmax, theta, grads, grad_v, u_t, rho_t, rng) -> dict:
+    """The GPU gradients against (a) the oracle's FP64 adjoint of the same model and (b) central
+    differences of the oracle's FP64 forward (double contact steps, exact deposit, double SOR to
+    1e-13), for all five: Km, D, boundary O2, stiffness and a random per-cell Vmax direction; for
+    the stiffness also at smaller steps, each with the count of contact-onset crossings (pairs in
+    contact at some step of one of the two trajectories but not the other) the difference spans."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle as orc
+
+    orc.set_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    u64, rho64 = u_t.cpu().numpy(), rho_t.cpu().numpy()
+    og = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    vm64 = vmax.astype(np.float64)
+    qr = 20.0
+
+    def forward64(vm, km, diffusion, boundary, stiffness):
+        return orc.adjoint_forward_f64(pos, radii, vm, og, w["steps"], DT, stiffness, qr, qr, 128, diffusion, km,
+                                       boundary)[:2]
+
+    def loss64(vm, **th):
+        field, p = forward64(vm, **th)
+        return float(((field - u64) ** 2).sum() + ((np.linalg.norm(p - p.mean(axis=0), axis=1) - rho64) ** 2).sum())
+
+    def loss_grads(field, p):
+        c = p - p.mean(axis=0)
+        rho = np.linalg.norm(c, axis=1)
+        gx = (2.0 * (rho - rho64))[:, None] * c / rho[:, None]
+        return 2.0 * (field - u64), gx - gx.mean(axis=0)
+
+    f64 = orc.adjoint_gradients_f64(pos, radii, vm64, og, w["steps"], DT, theta["stiffness"], 1.0, qr, qr, 128,
+                                    theta["diffusion"], theta["km"], theta["boundary"], loss_grads)
+    vs_adjoint = {k: abs(grads[k] - f64[k]) / abs(f64[k]) for k in ("km", "diffusion", "boundary", "stiffness")}
+    d = np.where(rng.random(vmax.size) < 0.5, -1.0, 1.0)
+    gpu_dir = float((grad_v * vm64 * d).sum())
+    f64_dir = float((f64["vmax"] * vm64 * d).sum())
+    vs_adjoint["vmax_direction"] = abs(gpu_dir - f64_dir) / abs(f64_dir)
+    rel = 1e-4
+    vs_fd = {}
+    fd_values = {}
+    for name in ("km", "diffusion", "boundary", "stiffness"):
+        h = rel * theta[name]
+        hi, lo = dict(theta), dict(theta)
+        hi[name] += h
+        lo[name] -= h
+        fd = (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * h)
+        fd_values[name] = fd
+        vs_fd[name] = abs(grads[name] - fd) / abs(fd)
+    fd = (loss64(vm64 * (1 + rel * d), **theta) - loss64(vm64 * (1 - rel * d), **theta)) / (2 * rel)
+    vs_fd["vmax_direction"] = abs(gpu_dir - fd) / abs(fd)
+    stiffness_steps = {}
+    for r in (1e-4, 1e-5, 1e-6):
+        hi, lo = dict(theta), dict(theta)
+        hi["stiffness"] *= 1 + r
+        lo["stiffness"] *= 1 - r
+        fd_r = fd_values["stiffness"] if r == rel else \
+            (loss64(vm64, **hi) - loss64(vm64, **lo)) / (2 * r * theta["stiffness"])
+        crossings = orc.contact_crossings_f64(pos, radii, w["steps"], DT, hi["stiffness"], lo["stiffness"], qr, qr,
+                                              128)
+        stiffness_steps[f"{r:g}"] = {"gpu_vs_fd": float(f"{abs(grads['stiffness'] - fd_r) / abs(fd_r):.3g}"),
+                                     "fp64_adjoint_vs_fd": float(f"{abs(f64['stiffness'] - fd_r) / abs(fd_r):.3g}"),
+                                     "contact_crossings": crossings}
+    return {"fp64_central_difference_rel_error": {k: float(f"{e:.3g}") for k, e in vs_fd.items()},
+            "fp64_adjoint_rel_error": {k: float(f"{e:.3g}") for k, e in vs_adjoint.items()},
+            "stiffness_by_step": stiffness_steps,
+            "fd_step": rel, "fp64_check_s": round(time.perf_counter() - t0, 1)}
 
 
 def main() -> None:
@@ -1030,6 +1112,8 @@ def main() -> None:
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--sor-tuning", default="",
                     help="halo_depth,tiles_i,tiles_j for the resident solver instead of the autotuner's pick")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline workload only: skip the batched-sweep and adjoint halves of the metric")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "gb300":
         print("note: fewer than 3 warm-up steps", file=sys.stderr)
@@ -1079,11 +1163,43 @@ def main() -> None:
     else:
         results = [result]
     if rank == 0:
-        print(json.dumps(report_gpu(args, results, world)))
+        line = report_gpu(args, results, world)
+        if world == 1 and args.workload == "spheroid_1M_161" and not args.no_extras:
+            line.update(metric_extras(args))
+        print(json.dumps(line))
     if world > 1:
         import torch.distributed as dist
 
         dist.destroy_process_group()
+
+
+def metric_extras(args) -> dict:
+    """The other two parts of the metric, measured on the same GPU after the headline steps: the
+    15-spheroid batched sweep against the same runs looped through the plain path, and the
+    adjoint's backward time over its forward time with its gradients checked against FP64."""
+    import copy
+
+    import torch
+
+    out = {}
+    b_args = copy.copy(args)
+    b_args.workload = "batched_sweep_15"
+    b = run_batched(b_args)
+    out["batched"] = {"workload": b_args.workload, "ratio_vs_sequential": b["speedup_vs_sequential"],
+                      "identical_outputs": b["identical_outputs"], "batched_ms_per_step": b["ms_per_step"],
+                      "sequential_ms_per_step": b["sequential"]["ms_per_step"], "value": b["value"],
+                      "unit": b["unit"], "steps": b["steps"], "warmup": b["warmup"],
+                      "launches_per_step": b["launches_per_step"], "config": b["config"], "clocks": b["clocks"]}
+    torch.cuda.empty_cache()
+    a_args = copy.copy(args)
+    a_args.workload = "adjoint_100k_81"
+    a = run_adjoint(a_args)
+    keep = ("value", "unit", "forward_ms", "backward_ms", "forward_sweeps", "adjoint_sweeps", "adjoint_converged",
+            "launches_per_forward_backward", "fp64_central_difference_rel_error", "fp64_adjoint_rel_error",
+            "stiffness_by_step", "fd_step", "clocks", "config")
+    out["adjoint"] = {"workload": a_args.workload, "what": "backward time / forward time", "steps": a["steps"],
+                      **{k: a[k] for k in keep if k in a}}
+    return out
 
 
 if __name__ == "__main__":

@@ -572,3 +572,65 @@ def contact_substep_region(pos: np.ndarray, radius: np.ndarray, cell_size: float
                                          f32(o[1]), f32(o[2]), f32(1.0 / region_geom.dx), P(s), P(g), f32(wall_rate),
                                          P(vel), P(nc))
     return vel, nc
+
+
+def adjoint_contact_f64(pos0: np.ndarray, radius: np.ndarray, steps: int, dt: float, rate: float, query_radius: float,
+                        cell_size: float, dim: int, grad_x: np.ndarray):
+    """FP64 reverse of ``steps`` contact steps from ``pos0``: (dL/dx_0, dL/drate) for dL/dx_K = grad_x."""
+    pos = np.ascontiguousarray(pos0, dtype=np.float64)
+    r = np.ascontiguousarray(radius, dtype=np.float64)
+    lam = np.ascontiguousarray(grad_x, dtype=np.float64).copy()
+    d_rate = np.zeros(1, dtype=np.float64)
+    lib().orc_adjoint_contact_f64.restype = None
+    lib().orc_adjoint_contact_f64(c_int32(pos.shape[0]), P(pos), P(r), f32(cell_size), c_int32(dim),
+                                  c_double(query_radius), c_double(rate), c_double(dt), c_int32(steps), P(lam),
+                                  P(d_rate))
+    return lam, float(d_rate[0])
+
+
+def contact_crossings_f64(pos0: np.ndarray, radius: np.ndarray, steps: int, dt: float, rate_a: float, rate_b: float,
+                          query_radius: float, cell_size: float, dim: int) -> int:
+    """Contact pairs present at a step of one FP64 trajectory (rate_a) and not of the other (rate_b)."""
+    pos = np.ascontiguousarray(pos0, dtype=np.float64)
+    r = np.ascontiguousarray(radius, dtype=np.float64)
+    lib().orc_contact_crossings_f64.restype = ctypes.c_int64
+    return int(lib().orc_contact_crossings_f64(c_int32(pos.shape[0]), P(pos), P(r), f32(cell_size), c_int32(dim),
+                                               c_double(query_radius), c_double(rate_a), c_double(rate_b),
+                                               c_double(dt), c_int32(steps)))
+
+
+def adjoint_field_f64(pos: np.ndarray, vmax: np.ndarray, geom: Geometry, diffusion: float, michaelis_k: float,
+                      u: np.ndarray, grad_u: np.ndarray, omega: float = 1.8, tolerance: float = 1e-12,
+                      max_sweeps: int = 200000):
+    """FP64 field half of the adjoint: ({"km", "diffusion", "boundary"}, dL/dVmax, the field's dL/dx, sweeps)."""
+    p = np.ascontiguousarray(pos, dtype=np.float64)
+    v = np.ascontiguousarray(vmax, dtype=np.float64)
+    uu = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+    gg = np.ascontiguousarray(grad_u, dtype=np.float64).reshape(-1)
+    nx, ny, nz = geom.shape
+    origin = np.ascontiguousarray(geom.origin, dtype=np.float64)
+    sums = np.zeros(3, dtype=np.float64)
+    grad_vmax = np.zeros(p.shape[0], dtype=np.float64)
+    grad_x = np.zeros_like(p)
+    lib().orc_adjoint_field_f64.restype = c_int32
+    sweeps = lib().orc_adjoint_field_f64(c_int32(nx), c_int32(ny), c_int32(nz), P(origin), c_double(geom.dx),
+                                         c_double(diffusion), c_double(michaelis_k), c_int32(p.shape[0]), P(p), P(v),
+                                         P(uu), P(gg), c_double(omega), c_double(tolerance), c_int32(max_sweeps),
+                                         P(sums), P(grad_vmax), P(grad_x))
+    return {"km": sums[0], "diffusion": sums[1], "boundary": sums[2]}, grad_vmax, grad_x, int(sweeps)
+
+
+def adjoint_gradients_f64(pos0: np.ndarray, radius: np.ndarray, vmax: np.ndarray, geom: Geometry, steps: int,
+                          dt: float, stiffness: float, damping: float, query_radius: float, cell_size: float, dim: int,
+                          diffusion: float, michaelis_k: float, boundary: float, loss_grads):
+    """The whole adjoint in FP64: forward (orc_adjoint_forward_f64), ``loss_grads(u, x_K) -> (dL/du,
+    dL/dx_K)`` in FP64, the field adjoint, then the contact steps in reverse. Returns the gradients
+    {"km", "diffusion", "boundary", "stiffness", "vmax"} of the same model the GPU adjoint differentiates."""
+    rate = stiffness / damping
+    field, pos, _ = adjoint_forward_f64(pos0, radius, vmax, geom, steps, dt, rate, query_radius, cell_size, dim,
+                                       diffusion, michaelis_k, boundary)
+    grad_u, grad_x = loss_grads(field, pos)
+    sums, grad_vmax, field_x, _ = adjoint_field_f64(pos, vmax, geom, diffusion, michaelis_k, field, grad_u)
+    _, d_rate = adjoint_contact_f64(pos0, radius, steps, dt, rate, query_radius, cell_size, dim,
+                                    np.asarray(grad_x, dtype=np.float64) + field_x)
+    return {**sums, "stiffness": d_rate / damping, "vmax": grad_vmax}

@@ -925,4 +925,258 @@ int32_t orc_adjoint_forward_f64(int32_t n, double* pos, const double* radius, co
     return sweeps;
 }
 
+// ---- FP64 reverse of the contact steps (checks of the GPU adjoint) --------------------------------------
+// The contact law of contact_substep, v_i = rate sum_j (R/d - 1) e_ij over the pairs with d < query
+// radius, R - d > 0 and d > 1e-6, in double, from the positions after `steps` FP64 steps; the reverse
+// sweep lambda_t = lambda_{t+1} + dt J(x_t)^T lambda_{t+1} with (J^T lambda)_i = rate sum_j A_ij
+// (lambda_i - lambda_j), A_ij = (R/d - 1) I - R e e^T / d^3, and dL/drate = dt sum_t lambda_{t+1} .
+// v(x_t) / rate. On entry `lambda` holds dL/dx_K; on return dL/dx_0. Pairs come from the buckets of
+// the float32 image of the positions, as orc_contact_substep_f64.
+void orc_adjoint_contact_f64(int32_t n, const double* pos0, const double* radius, float cell_size, int32_t dim,
+                             double query_radius, double rate, double dt, int32_t steps, double* lambda,
+                             double* d_rate) {
+    const size_t n3 = 3 * static_cast<size_t>(n);
+    std::vector<double> traj(n3 * static_cast<size_t>(steps > 0 ? steps : 1));
+    std::vector<double> pos(pos0, pos0 + n3), vel(n3);
+    std::vector<int32_t> nc(n);
+    for (int32_t t = 0; t < steps; ++t) {
+        std::copy(pos.begin(), pos.end(), traj.begin() + n3 * t);
+        orc_contact_substep_f64(n, pos.data(), radius, cell_size, dim, query_radius, rate, dt, vel.data(), nc.data());
+    }
+    std::vector<double> lam(lambda, lambda + n3), out(n3);
+    std::vector<float> bin(n3);
+    double total = 0.0;
+    for (int32_t t = steps - 1; t >= 0; --t) {
+        const double* x = traj.data() + n3 * t;
+        for (size_t q = 0; q < n3; ++q) bin[q] = static_cast<float>(x[q]);
+        Buckets bk;
+        bk.build(n, bin.data(), cell_size, dim);
+        double step_dot = 0.0;
+#pragma omp parallel for schedule(dynamic, 256) reduction(+ : step_dot)
+        for (int i = 0; i < n; ++i) {
+            const int cx = bk.coord(bin[3 * i]), cy = bk.coord(bin[3 * i + 1]), cz = bk.coord(bin[3 * i + 2]);
+            double g[3] = {0, 0, 0}, u[3] = {0, 0, 0};
+            for (int ox = -1; ox <= 1; ++ox)
+                for (int oy = -1; oy <= 1; ++oy)
+                    for (int oz = -1; oz <= 1; ++oz) {
+                        const int b = bk.bucket(cx + ox, cy + oy, cz + oz);
+                        for (int s = bk.start[b], e = s + bk.count[b]; s < e; ++s) {
+                            const int j = bk.ids[s];
+                            if (j == i) continue;
+                            const double e3[3] = {x[3 * i] - x[3 * j], x[3 * i + 1] - x[3 * j + 1],
+                                                  x[3 * i + 2] - x[3 * j + 2]};
+                            const double d = std::sqrt(e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2]);
+                            if (!(d < query_radius)) continue;
+                            const double R = radius[i] + radius[j];
+                            if (!(R - d > 0.0 && d > 1.0e-6)) continue;
+                            const double a = R / d - 1.0;
+                            const double l[3] = {lam[3 * i] - lam[3 * j], lam[3 * i + 1] - lam[3 * j + 1],
+                                                 lam[3 * i + 2] - lam[3 * j + 2]};
+                            const double proj = R / (d * d * d) * (e3[0] * l[0] + e3[1] * l[1] + e3[2] * l[2]);
+                            for (int c = 0; c < 3; ++c) {
+                                u[c] += a * e3[c];
+                                g[c] += a * l[c] - proj * e3[c];
+                            }
+                        }
+                    }
+            for (int c = 0; c < 3; ++c) out[3 * i + c] = lam[3 * i + c] + dt * rate * g[c];
+            step_dot += lam[3 * i] * u[0] + lam[3 * i + 1] * u[1] + lam[3 * i + 2] * u[2];
+        }
+        total += step_dot;
+        lam.swap(out);
+    }
+    std::copy(lam.begin(), lam.end(), lambda);
+    *d_rate = dt * total;
+}
+
+// Contact pairs (i < j with d < query radius, R - d > 0 and d > 1e-6) present at a step of one FP64
+// trajectory but not of the other, summed over the steps: trajectories from the same start with
+// contact rates rate_a and rate_b. Counts where a finite difference in the rate steps over the
+// force law's kink at contact onset.
+int64_t orc_contact_crossings_f64(int32_t n, const double* pos0, const double* radius, float cell_size, int32_t dim,
+                                  double query_radius, double rate_a, double rate_b, double dt, int32_t steps) {
+    const size_t n3 = 3 * static_cast<size_t>(n);
+    std::vector<double> pa(pos0, pos0 + n3), pb(pos0, pos0 + n3), vel(n3);
+    std::vector<int32_t> nc(n);
+    std::vector<float> ba(n3), bb(n3);
+    int64_t crossings = 0;
+    auto pairs_of = [&](const Buckets& bk, const std::vector<float>& bin, const std::vector<double>& x, int i,
+                        std::vector<int32_t>& out) {
+        out.clear();
+        const int cx = bk.coord(bin[3 * i]), cy = bk.coord(bin[3 * i + 1]), cz = bk.coord(bin[3 * i + 2]);
+        for (int ox = -1; ox <= 1; ++ox)
+            for (int oy = -1; oy <= 1; ++oy)
+                for (int oz = -1; oz <= 1; ++oz) {
+                    const int b = bk.bucket(cx + ox, cy + oy, cz + oz);
+                    for (int s = bk.start[b], e = s + bk.count[b]; s < e; ++s) {
+                        const int j = bk.ids[s];
+                        if (j <= i) continue;
+                        const double dx = x[3 * i] - x[3 * j], dy = x[3 * i + 1] - x[3 * j + 1],
+                                     dz = x[3 * i + 2] - x[3 * j + 2];
+                        const double d = std::sqrt(dx * dx + dy * dy + dz * dz);
+                        if (d < query_radius && radius[i] + radius[j] - d > 0.0 && d > 1.0e-6) out.push_back(j);
+                    }
+                }
+        std::sort(out.begin(), out.end());
+    };
+    for (int32_t t = 0; t <= steps; ++t) {
+        for (size_t q = 0; q < n3; ++q) {
+            ba[q] = static_cast<float>(pa[q]);
+            bb[q] = static_cast<float>(pb[q]);
+        }
+        Buckets ka, kb;
+        ka.build(n, ba.data(), cell_size, dim);
+        kb.build(n, bb.data(), cell_size, dim);
+        int64_t step_count = 0;
+#pragma omp parallel reduction(+ : step_count)
+        {
+            std::vector<int32_t> la, lb;
+#pragma omp for schedule(dynamic, 256)
+            for (int i = 0; i < n; ++i) {
+                pairs_of(ka, ba, pa, i, la);
+                pairs_of(kb, bb, pb, i, lb);
+                size_t x = 0, y = 0;
+                while (x < la.size() || y < lb.size()) {
+                    if (y == lb.size() || (x < la.size() && la[x] < lb[y])) {
+                        ++step_count;
+                        ++x;
+                    } else if (x == la.size() || lb[y] < la[x]) {
+                        ++step_count;
+                        ++y;
+                    } else {
+                        ++x;
+                        ++y;
+                    }
+                }
+            }
+        }
+        crossings += step_count;
+        if (t == steps) break;
+        orc_contact_substep_f64(n, pa.data(), radius, cell_size, dim, query_radius, rate_a, dt, vel.data(), nc.data());
+        orc_contact_substep_f64(n, pb.data(), radius, cell_size, dim, query_radius, rate_b, dt, vel.data(), nc.data());
+    }
+    return crossings;
+}
+
+// FP64 field half of the adjoint (Dirichlet faces on every side, the adjoint model's boundary): for
+// the steady field u of orc_adjoint_forward_f64 (cells at `pos`, capacities `vmax`) and dL/du = g,
+// solves (6 + h kappa_a) mu_a - sum_nb mu_nb = g_a (kappa_a = U_a K / (K + u_a)^2; mu = 0 on the faces
+// and where u_a = 0) by red-black SOR in double to a max residual below `tolerance` relative to
+// max(6 |mu|, |g|), then forms sums = {dL/dK, dL/dD, dL/dO_b}, dL/dVmax_i = -h inv_vol sum_a w_a(x_i)
+// phi_a (phi_a = mu_a u_a / (K + u_a)) and adds -h inv_vol Vmax_i grad_x sum_a w_a(x) phi_a to grad_x.
+// Returns the sweeps run.
+int32_t orc_adjoint_field_f64(int32_t nx, int32_t ny, int32_t nz, const double* origin, double dx, double diffusion,
+                              double michaelis_k, int32_t n, const double* pos, const double* vmax, const double* u,
+                              const double* g, double omega, double tolerance, int32_t max_sweeps, double* sums,
+                              double* grad_vmax, double* grad_x) {
+    const int64_t nodes = static_cast<int64_t>(nx) * ny * nz;
+    const double inv_dx = 1.0 / dx, inv_vol = inv_dx * inv_dx * inv_dx, h = dx * dx / diffusion;
+    auto cell_corner = [&](int c, int& i0, int& j0, int& k0, double& fx, double& fy, double& fz) {
+        const double ux = (pos[3 * c] - origin[0]) * inv_dx, uy = (pos[3 * c + 1] - origin[1]) * inv_dx,
+                     uz = (pos[3 * c + 2] - origin[2]) * inv_dx;
+        i0 = static_cast<int>(std::floor(ux));
+        j0 = static_cast<int>(std::floor(uy));
+        k0 = static_cast<int>(std::floor(uz));
+        if (i0 < 0 || j0 < 0 || k0 < 0 || i0 + 1 >= nx || j0 + 1 >= ny || k0 + 1 >= nz) return false;
+        fx = ux - i0;
+        fy = uy - j0;
+        fz = uz - k0;
+        return true;
+    };
+    std::vector<double> U(nodes, 0.0), kappa(nodes, -1.0), mu(nodes, 0.0), phi(nodes, 0.0);
+    for (int c = 0; c < n; ++c) {
+        int i0, j0, k0;
+        double fx, fy, fz;
+        if (!cell_corner(c, i0, j0, k0, fx, fy, fz)) continue;
+        for (int di = 0; di < 2; ++di)
+            for (int dj = 0; dj < 2; ++dj)
+                for (int dk = 0; dk < 2; ++dk)
+                    U[(static_cast<int64_t>(i0 + di) * ny + (j0 + dj)) * nz + (k0 + dk)] +=
+                        (di ? fx : 1.0 - fx) * (dj ? fy : 1.0 - fy) * (dk ? fz : 1.0 - fz) * vmax[c] * inv_vol;
+    }
+    auto interior = [&](int i, int j, int k) { return i > 0 && j > 0 && k > 0 && i < nx - 1 && j < ny - 1 && k < nz - 1; };
+    for (int i = 1; i < nx - 1; ++i)
+        for (int j = 1; j < ny - 1; ++j)
+            for (int k = 1; k < nz - 1; ++k) {
+                const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                if (u[a] > 0.0) kappa[a] = U[a] * michaelis_k / ((michaelis_k + u[a]) * (michaelis_k + u[a]));
+            }
+    const int64_t sx = static_cast<int64_t>(ny) * nz;
+    int32_t sweeps = 0;
+    while (sweeps < max_sweeps) {
+        for (int colour = 0; colour < 2; ++colour) {
+#pragma omp parallel for schedule(static)
+            for (int i = 1; i < nx - 1; ++i)
+                for (int j = 1; j < ny - 1; ++j)
+                    for (int k = 1 + ((colour + i + j + 1) & 1); k < nz - 1; k += 2) {
+                        const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                        if (!(kappa[a] >= 0.0)) continue;
+                        const double nb = mu[a - sx] + mu[a + sx] + mu[a - nz] + mu[a + nz] + mu[a - 1] + mu[a + 1];
+                        mu[a] = (1.0 - omega) * mu[a] + omega * (nb + g[a]) / (6.0 + h * kappa[a]);
+                    }
+        }
+        ++sweeps;
+        if (sweeps % 20 != 0) continue;
+        double res = 0.0, scale = 0.0;
+#pragma omp parallel for reduction(max : res, scale) schedule(static)
+        for (int i = 1; i < nx - 1; ++i)
+            for (int j = 1; j < ny - 1; ++j)
+                for (int k = 1; k < nz - 1; ++k) {
+                    const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                    if (!(kappa[a] >= 0.0)) continue;
+                    const double nb = mu[a - sx] + mu[a + sx] + mu[a - nz] + mu[a + nz] + mu[a - 1] + mu[a + 1];
+                    res = std::max(res, std::fabs(nb + g[a] - (6.0 + h * kappa[a]) * mu[a]));
+                    scale = std::max(scale, std::max(6.0 * std::fabs(mu[a]), std::fabs(g[a])));
+                }
+        if (res <= tolerance * scale) break;
+    }
+    double s_k = 0.0, s_d = 0.0, s_b = 0.0;
+    for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j)
+            for (int k = 0; k < nz; ++k) {
+                const int64_t a = (static_cast<int64_t>(i) * ny + j) * nz + k;
+                if (!interior(i, j, k)) {
+                    s_b += g[a];
+                    continue;
+                }
+                if (!(kappa[a] >= 0.0)) continue;
+                const double ua = u[a], m = mu[a], sk = michaelis_k + ua;
+                phi[a] = m * ua / sk;
+                s_k += m * h * U[a] * ua / (sk * sk);
+                s_d += m * h * U[a] * ua / (sk * diffusion);
+                const int faces = (i == 1) + (i == nx - 2) + (j == 1) + (j == ny - 2) + (k == 1) + (k == nz - 2);
+                s_b += m * faces;
+            }
+    sums[0] = s_k;
+    sums[1] = s_d;
+    sums[2] = s_b;
+    const double coef = -h * inv_vol;
+    for (int c = 0; c < n; ++c) {
+        int i0, j0, k0;
+        double fx, fy, fz;
+        if (!cell_corner(c, i0, j0, k0, fx, fy, fz)) {
+            grad_vmax[c] = 0.0;
+            continue;
+        }
+        double sv = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
+        for (int di = 0; di < 2; ++di)
+            for (int dj = 0; dj < 2; ++dj)
+                for (int dk = 0; dk < 2; ++dk) {
+                    const double wx = di ? fx : 1.0 - fx, wy = dj ? fy : 1.0 - fy, wz = dk ? fz : 1.0 - fz;
+                    const double dwx = di ? 1.0 : -1.0, dwy = dj ? 1.0 : -1.0, dwz = dk ? 1.0 : -1.0;
+                    const double ph = phi[(static_cast<int64_t>(i0 + di) * ny + (j0 + dj)) * nz + (k0 + dk)];
+                    sv += wx * wy * wz * ph;
+                    gx += dwx * wy * wz * ph;
+                    gy += wx * dwy * wz * ph;
+                    gz += wx * wy * dwz * ph;
+                }
+        grad_vmax[c] = coef * sv;
+        const double f = coef * vmax[c] * inv_dx;
+        grad_x[3 * c] += f * gx;
+        grad_x[3 * c + 1] += f * gy;
+        grad_x[3 * c + 2] += f * gz;
+    }
+    return sweeps;
+}
+
 }  // extern "C"

@@ -88,8 +88,11 @@ def test_reference_arm_prints_the_contract_line():
                          timeout=600, check=True).stdout.strip().splitlines()
     assert len(out) == 1
     line = json.loads(out[0])
-    assert line["impl"] == "reference" and line["metric"] == bench.METRIC and line["unit"] == bench.UNIT
-    assert line["higher_is_better"] is True and line["config"]["workload"] == "spheroid_10k_41"
+    assert line["impl"] == "reference" and line["metric"] == bench.metric_for("spheroid_10k_41")
+    assert line["metric"] == "cell-steps/s @10k cells+41^3 O2 (coupled cell step)" and line["unit"] == bench.UNIT
+    assert line["higher_is_better"] is True
+    # the GPU arm's config object for the same workload, key for key
+    assert line["config"] == bench.workload_config("spheroid_10k_41", 41 ** 3)
     assert line["value"] > 0 and line["steps"] == 1
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
@@ -116,3 +119,12 @@ def test_batched_sweep_shards_cover_every_instance_and_balance(world):
     assert sorted(i for share in shares for i in share) == list(range(len(specs)))
     loads = [sum(costs[i] for i in share) for share in shares]
     assert max(loads) <= max(1.05 * sum(costs) / world, max(costs)) + 1e-9
+
+
+def test_metric_labels_name_each_workload():
+    assert bench.metric_for("spheroid_1M_161") == "cell-steps/s @1M cells+161^3 O2 (coupled cell step)"
+    assert bench.metric_for("spheroid_100k_81") == "cell-steps/s @100k cells+81^3 O2 (coupled cell step)"
+    assert "106-node networks" in bench.metric_for("metabolic_network_100k_81")
+    assert "81^3" in bench.metric_for("metabolic_network_100k_81")
+    assert "batched" in bench.metric_for("batched_sweep_15")
+    assert "backward time" in bench.metric_for("adjoint_100k_81")

@@ -25,8 +25,8 @@
 // reference's sweep count, residual and stopping rule, with no host round trip. The field after
 // n sweeps is bit-identical to the oracle's and to the streaming kernels'.
 //
-// Every wait polls a bounded number of times (about a second); on timeout the CTA raises an
-// abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
+// Every wait is bounded in time (kWaitLimitNs of the GPU's global timer, 2 s); on timeout the CTA
+// raises an abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -79,7 +79,9 @@ struct SorArgs {
     float* pcopy;      // [2][nx][ny][M] production term of every updated node (production, source)
 };
 
-constexpr unsigned kBarrierPolls = 1u << 21;  // L2 round trips: about a second
+// Every device wait gives up after kWaitLimitNs nanoseconds of the GPU's global timer without
+// progress. The timer is read every 256 polls, so a wait ends within a few microseconds of the limit.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
 constexpr int kMaxLanesPerColumn = 8;         // M <= 256 (nz <= 511)
 
 __device__ __forceinline__ unsigned int load_acquire(const unsigned int* p) {
@@ -91,6 +93,30 @@ __device__ __forceinline__ unsigned int load_acquire(const unsigned int* p) {
 __device__ __forceinline__ void store_release(unsigned int* p, unsigned int v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The clock of one bounded wait. `claims` (batched solves only) is the work list's claim counter:
+// while fewer than `claims_needed` tiles have been claimed, some tile of this solve has no CTA yet
+// and is waiting behind earlier work, so the wait has not really started and its clock is held.
+struct WaitClock {
+    unsigned long long start = 0;
+    const unsigned int* claims = nullptr;
+    unsigned int claims_needed = 0;
+    // true once the wait has lasted longer than kWaitLimitNs
+    __device__ __forceinline__ bool expired() {
+        const unsigned long long now = global_ns();
+        if (start == 0 || (claims && load_acquire(claims) < claims_needed)) {
+            start = now;
+            return false;
+        }
+        return now - start > kWaitLimitNs;
+    }
+};
 
 // ---- halo exchange with tagged words (H = 1) ------------------------------------------------------------
 // Each exchanged entry is one 64-bit word {value bits, tag} written with a single relaxed store, so a
@@ -115,7 +141,8 @@ __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n 
 // elsewhere). A halo exchange only needs the neighbouring tiles; the residual needs all.
 // `me` is this CTA's tile among the `ntiles` tiles of its solve.
 __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch, int me,
-                                             int ntiles, const int* wait_for = nullptr, int n_wait = -1) {
+                                             int ntiles, const int* wait_for = nullptr, int n_wait = -1,
+                                             const unsigned int* claims = nullptr, unsigned int claims_needed = 0) {
     epoch += 1;
     __syncthreads();  // the CTA's writes happen before thread 0's release (bar.sync is cumulative)
     if (threadIdx.x == 0) store_release(flags + me, epoch);
@@ -124,13 +151,14 @@ __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flag
     for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
         const unsigned who = n_wait < 0 ? t : static_cast<unsigned>(wait_for[t]);
         unsigned polls = 0;
+        WaitClock clock{0ull, claims, claims_needed};
         while (static_cast<int>(load_acquire(flags + who) - epoch) < 0) {
             if ((++polls & 255u) == 0u) {
                 if (load_acquire(&ctl->abort) != 0u) {
                     aborted = 1;
                     break;
                 }
-                if (polls > kBarrierPolls) {
+                if (clock.expired()) {
                     atomicExch(&ctl->abort, 1u);
                     aborted = 1;
                     break;
@@ -436,8 +464,9 @@ __device__ __forceinline__ bool pull_tagged(const Sweep& w, const int2* list, in
             for (int r = 0; r < LANES; ++r)
                 if (lane + 32 * r < cnt[u]) {
                     unsigned polls = 0;
+                    WaitClock clock;
                     while (static_cast<unsigned int>(v[u][r] >> 32) != tag) {
-                        if ((++polls & 255u) == 0u && (polls > kBarrierPolls || load_acquire(&ctl->abort) != 0u)) {
+                        if ((++polls & 255u) == 0u && (load_acquire(&ctl->abort) != 0u || clock.expired())) {
                             fine = false;
                             break;
                         }
@@ -518,8 +547,10 @@ __device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list,
 constexpr int max_threads_for_lanes(int lanes) { return lanes > 3 ? 512 : 1024; }
 
 // One tile (`tile` of `ntiles`) of one solve, for the whole solve.
+// `claims` / `claims_needed`: see WaitClock (batched solves; null for a single solve).
 template <bool HAS_PROD, int LANES, int H>
-__device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles) {
+__device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles, const unsigned int* claims = nullptr,
+                                         unsigned int claims_needed = 0) {
     extern __shared__ __align__(128) float s[];
     __shared__ unsigned int s_red[32];
     __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
@@ -691,7 +722,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
     }
     // The ring columns' coefficients (and edge rows) are written by their owners: one global
     // barrier first.
-    bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles);
+    bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, nullptr, -1, claims, claims_needed);
     w.fast = s_outside_range == 0;  // read after the barrier's __syncthreads
 
     int sweeps = 0;
@@ -742,7 +773,8 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
                 copy_columns<LANES>(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
                 // A neighbour overwrites this buffer two exchanges later, i.e. only after this tile
                 // has signalled the next epoch, which comes after the pull below.
-                ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, s_neighbours, n_neighbours);
+                ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, s_neighbours, n_neighbours, claims,
+                                  claims_needed);
                 if (!ok) break;
                 copy_columns<LANES>(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
                 __syncthreads();
@@ -774,7 +806,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles)
             for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
             if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
         }
-        ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles);
+        ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, nullptr, -1, claims, claims_needed);
         if (!ok) break;
         residual = __uint_as_float(load_acquire(&a.ctl->res_bits[slot]));
         // The next chunk's slot was last read before this chunk's first barrier: safe to clear.
@@ -812,7 +844,7 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_residen
 
 // The solver's grid barrier alone, for the self-test of the bounded waits: `ntiles` tiles are
 // expected, gridDim.x of them run. With gridDim.x < ntiles the missing tiles never arrive, every
-// launched CTA gives up after its bounded polls, and the control block's status says so.
+// launched CTA gives up after its bounded wait, and the control block's status says so.
 __global__ void k_barrier_selftest(SorControl* ctl, unsigned int* flags, int ntiles, int rounds) {
     unsigned int epoch = 0;
     for (int r = 0; r < rounds; ++r) {
@@ -854,7 +886,8 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1)
         const int t = s_tile;
         if (t >= total) return;
         const int b = find_batch_item(tile_first, n, t);
-        sor_tile<HAS_PROD, LANES, 1>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b]);
+        sor_tile<HAS_PROD, LANES, 1>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
+                                     static_cast<unsigned int>(tile_first[b + 1]));
     }
 }
 
