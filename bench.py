@@ -349,8 +349,7 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     result = {
         "sor_path": _diffusion.last_solve.get("path"),
         "sor_tiles": _diffusion.last_solve.get("tiles"),
-        "sor_halo_depth": _diffusion.last_solve.get("halo_depth"),
-        "sor_tile_grid": [_diffusion.last_solve.get("tiles_i"), _diffusion.last_solve.get("tiles_j")],
+        "sor_strips": _diffusion.last_solve.get("strips"),
         "sor_autotune": [list(v) for v in _diffusion.autotune_cache.values()],
         "rank": rank,
         "elapsed_ms": elapsed_ms,
@@ -599,8 +598,7 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
         "stages": breakdown,
         "sor_sweeps_per_step": r0["sweeps"],
         "sor_solver": {"path": "shared-memory resident" if r0.get("sor_path") == 2 else "streaming",
-                       "ctas": r0.get("sor_tiles"), "halo_depth": r0.get("sor_halo_depth"),
-                       "tile_grid": r0.get("sor_tile_grid"),
+                       "ctas": r0.get("sor_tiles"), "strips": r0.get("sor_strips"),
                        "autotuned": r0.get("sor_autotune")},
         "initial_solve_sweeps": r0["initial_sweeps"],
         "clocks": r0["clocks"],
@@ -1111,7 +1109,7 @@ def main() -> None:
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline sample and parity check")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--sor-tuning", default="",
-                    help="halo_depth,tiles_i,tiles_j for the resident solver instead of the autotuner's pick")
+                    help="tiles,strips for the resident solver instead of the autotuner's pick")
     ap.add_argument("--no-extras", action="store_true",
                     help="headline workload only: skip the batched-sweep and adjoint halves of the metric")
     args = ap.parse_args()

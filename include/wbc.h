@@ -169,17 +169,16 @@ typedef struct wbc_sor_report {
     int32_t converged;           /* residual < tolerance                                             */
     int32_t path;                /* 2 = shared-memory resident solver, 1 = streaming colour launches */
     int32_t tiles;               /* CTAs of the resident solver (0 for the streaming path)           */
-    int32_t halo_depth;          /* half-sweeps between halo exchanges (resident path)               */
-    int32_t tiles_i, tiles_j;    /* tile grid of the resident solver                                 */
+    int32_t strips;              /* strips along j the tiles are cut from (resident path)             */
 } wbc_sor_report;
 
-/* Optional choices for the resident solver (NULL or zeros = automatic). halo_depth H in {1, 2, 4}:
- * each tile keeps a halo of H columns and performs H colour half-sweeps between exchanges with
- * its neighbours (the halo columns are updated redundantly, with identical results). tiles_i x
- * tiles_j fixes the tile grid (at most one tile per SM). Every choice gives the same field bits. */
+/* Optional choices for the resident solver (NULL or zeros = automatic). The (i, j) plane of
+ * columns is cut into `strips` strips along j, and each strip's columns, row by row, into equal
+ * runs, one per tile: `tiles` tiles (CTAs, at most one per SM; 0 = every SM). Every choice gives
+ * the same field bits. */
 typedef struct wbc_sor_tuning {
-    int32_t halo_depth;
-    int32_t tiles_i, tiles_j;
+    int32_t tiles;
+    int32_t strips;
 } wbc_sor_tuning;
 
 /* Scratch bytes wbc_sor_solve needs for this grid (control block, halo exchange buffers, the
@@ -190,25 +189,27 @@ size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p);
  * stopping rule of fields/diffusion.py:79-123 (kernels/field_kernels.py:185-243). path 0 = auto:
  * one persistent cooperative launch with the field tile resident in shared memory when the grid
  * fits on chip, otherwise streaming colour launches with a host check per chunk; 1 = streaming;
- * 2 = resident only. Synchronises `stream` and fills the host-side `report`. The field after the
- * solve is bit-identical on both paths and for every `tuning` (may be NULL). Returns
- * WBC_ERR_TIMEOUT if a grid barrier timed out. */
+ * 2 = resident only. Synchronises `stream` and fills the host-side `report`; when residual_out is
+ * non-NULL the final residual is also written there (device float, the reference's
+ * residual_buffer). The field after the solve is bit-identical on both paths and for every
+ * `tuning` (may be NULL). Returns WBC_ERR_TIMEOUT if a device wait timed out. */
 int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
                   const int32_t* fixed, const float* density, const float* production, const float* source,
-                  float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
-                  const wbc_sor_tuning* tuning, void* stream);
+                  float* field, float* residual_out, wbc_sor_report* report, void* workspace,
+                  size_t workspace_bytes, int32_t path, const wbc_sor_tuning* tuning, void* stream);
 /* Self-test of the solver's bounded device waits (no counterpart in the reference): runs the grid
  * barrier of the resident solver `rounds` times on `ctas` expected CTAs, of which `ctas - missing`
  * are launched (cooperatively, one small CTA each; ctas <= the SM count). With missing = 0 the
  * barriers complete and WBC_OK is returned; with missing > 0 the missing CTAs never arrive, every
- * launched CTA stops polling after its bound (about a second), and WBC_ERR_TIMEOUT is returned with
+ * launched CTA stops waiting after its time limit (2 s), and WBC_ERR_TIMEOUT is returned with
  * the device context intact. `workspace` (at least the control block and barrier flags of
  * wbc_sor_solve_workspace_bytes, 16-byte aligned) is cleared first. Synchronises `stream`. */
 int wbc_sor_wait_selftest(int32_t ctas, int32_t missing, int32_t rounds, void* workspace, size_t workspace_bytes,
                           void* stream);
 /* Times the resident solver on a copy of `field` (into `scratch_field`, nx*ny*nz floats) for
- * 2 * check_every sweeps under each candidate tuning (halo depths 1, 2, 4; per depth the tile grid
- * with the fewest columns per tile, its transpose and the squarest grid) and returns the fastest in
+ * 2 * check_every sweeps under each candidate tuning (one tile per SM; the strip count whose
+ * largest tile and bounding box are smallest, and the strip counts one and two either side of it)
+ * and returns the fastest in
  * *best (zeros if the grid does not fit on chip) and its time per sweep in *best_us_per_sweep (may
  * be NULL). `field` is not modified; synchronises `stream`. The choice changes speed only: every
  * tuning gives the same field bits. */
@@ -233,7 +234,7 @@ typedef struct wbc_sor_batch_item {
 } wbc_sor_batch_item;
 
 typedef struct wbc_sor_batch {    /* filled by wbc_sor_batch_prepare                                */
-    int32_t items, total_tiles, ctas, threads, lanes, has_prod;
+    int32_t items, total_tiles, ctas, threads, zclamp, has_prod;
     int64_t smem_bytes;
     void* device_plan;
 } wbc_sor_batch;

@@ -622,13 +622,14 @@ def adjoint_field_f64(pos: np.ndarray, vmax: np.ndarray, geom: Geometry, diffusi
 
 def adjoint_gradients_f64(pos0: np.ndarray, radius: np.ndarray, vmax: np.ndarray, geom: Geometry, steps: int,
                           dt: float, stiffness: float, damping: float, query_radius: float, cell_size: float, dim: int,
-                          diffusion: float, michaelis_k: float, boundary: float, loss_grads):
+                          diffusion: float, michaelis_k: float, boundary: float, loss_grads,
+                          tolerance: float = 1e-13):
     """The whole adjoint in FP64: forward (orc_adjoint_forward_f64), ``loss_grads(u, x_K) -> (dL/du,
     dL/dx_K)`` in FP64, the field adjoint, then the contact steps in reverse. Returns the gradients
     {"km", "diffusion", "boundary", "stiffness", "vmax"} of the same model the GPU adjoint differentiates."""
     rate = stiffness / damping
     field, pos, _ = adjoint_forward_f64(pos0, radius, vmax, geom, steps, dt, rate, query_radius, cell_size, dim,
-                                       diffusion, michaelis_k, boundary)
+                                       diffusion, michaelis_k, boundary, tolerance=tolerance)
     grad_u, grad_x = loss_grads(field, pos)
     sums, grad_vmax, field_x, _ = adjoint_field_f64(pos, vmax, geom, diffusion, michaelis_k, field, grad_u)
     _, d_rate = adjoint_contact_f64(pos0, radius, steps, dt, rate, query_radius, cell_size, dim,

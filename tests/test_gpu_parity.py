@@ -492,10 +492,10 @@ def test_resident_solver_bitwise_equals_streaming_and_oracle(shape, boundary, ex
     ((33, 27, 31), (Boundary.NEUMANN, Boundary.DIRICHLET, Boundary.NEUMANN)),
     ((41, 41, 41), (Boundary.NEUMANN,) * 3),
 ])
-def test_resident_halo_depths_and_tilings_bitwise(shape, boundary):
-    """Every halo depth (half-sweeps per exchange) and tile grid gives the streaming path's bits,
-    including tile grids whose last tile is narrower than the halo and a chunk of 2 * 7 half-sweeps
-    that is not a multiple of the depth."""
+def test_resident_tilings_bitwise(shape, boundary):
+    """Every partition of the columns (tile count, strip count) gives the streaming path's bits:
+    one strip, strips of one or two columns, tiles of a partial row, staircase tiles, and a chunk
+    of 2 * 7 half-sweeps."""
     geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
     rng = np.random.default_rng(7 + sum(shape))
     start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
@@ -505,12 +505,15 @@ def test_resident_halo_depths_and_tilings_bitwise(shape, boundary):
     source = rng.uniform(0.0, 5.0, shape).astype(np.float32)
     settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=63, check_every=7)
     a, ra, _ = _solve_with_path(1, geom, boundary, start, density, pins, production, source, settings)
-    for tuning in [(1, 0, 0), (2, 0, 0), (4, 0, 0), (2, 5, 3), (4, 4, 6), (1, 9, 2), (2, 2, 2)]:
+    ny = shape[1]
+    for tuning in [(0, 0), (0, 1), (0, 3), (17, 2), (40, 5), (7, 7), (2, 1), (3, 1), (60, ny), (100, ny // 2)]:
         b, rb, ib = _solve_with_path(2, geom, boundary, start, density, pins, production, source, settings,
                                      tuning=tuning)
-        assert ib["path"] == 2 and ib["halo_depth"] == tuning[0], (tuning, ib)
-        if tuning[1]:  # the tile grid actually needed for tiles of ceil(n / requested) columns
-            assert ib["tiles_i"] <= tuning[1] and ib["tiles_j"] <= tuning[2], (tuning, ib)
+        assert ib["path"] == 2, (tuning, ib)
+        if tuning[0]:
+            assert ib["tiles"] == tuning[0], (tuning, ib)
+        if tuning[1]:
+            assert ib["strips"] == tuning[1], (tuning, ib)
         assert (ra.sweeps, ra.converged, ra.residual) == (rb.sweeps, rb.converged, rb.residual), tuning
         np.testing.assert_array_equal(a, b, err_msg=str(tuning))
 
@@ -520,7 +523,7 @@ def test_resident_halo_depths_and_tilings_bitwise(shape, boundary):
     ((19, 22, 263), (Boundary.DIRICHLET,) * 3),
 ])
 def test_resident_long_columns_bitwise(shape, boundary):
-    """Columns of more than 128 entries per parity (16-warp CTAs) at every halo depth."""
+    """Columns of more than 128 entries per colour under several partitions."""
     geom = GridGeometry(origin=(0.0, 0.0, 0.0), dx=10.0, shape=shape)
     rng = np.random.default_rng(3 + sum(shape))
     start = rng.uniform(5.0, 30.0, shape).astype(np.float32)
@@ -528,10 +531,10 @@ def test_resident_long_columns_bitwise(shape, boundary):
     production = rng.uniform(0.0, 40.0, shape).astype(np.float32)
     settings = SolverSettings(omega=1.8, tolerance=1e-6, max_sweeps=40, check_every=10)
     a, ra, _ = _solve_with_path(1, geom, boundary, start, density, production=production, settings=settings)
-    for tuning in [(1, 0, 0), (2, 0, 0), (4, 0, 0)]:
+    for tuning in [(0, 0), (8, 2), (30, 3), (60, 5)]:
         b, rb, ib = _solve_with_path(2, geom, boundary, start, density, production=production, settings=settings,
                                      tuning=tuning)
-        assert ib["path"] == 2 and ib["halo_depth"] == tuning[0]
+        assert ib["path"] == 2
         assert (ra.sweeps, ra.residual) == (rb.sweeps, rb.residual), tuning
         np.testing.assert_array_equal(a, b, err_msg=str(tuning))
 
@@ -551,9 +554,9 @@ def test_autotuned_solve_bitwise_equals_streaming():
     diffusion.autotune_cache.clear()
     b, rb, ib = _solve_with_path(0, geom, MIXED, start, density, settings=settings, tuning=None)
     assert len(diffusion.autotune_cache) == 1
-    (depth, ti, tj, us), = diffusion.autotune_cache.values()
-    assert depth in (1, 2, 4) and us > 0.0
-    assert (ib["path"], ib["halo_depth"], ib["tiles_i"], ib["tiles_j"]) == (2, depth, ti, tj)
+    (tiles, strips, us), = diffusion.autotune_cache.values()
+    assert tiles >= 1 and strips >= 1 and us > 0.0
+    assert (ib["path"], ib["tiles"], ib["strips"]) == (2, tiles, strips)
     assert (ra.sweeps, ra.converged, ra.residual) == (rb.sweeps, rb.converged, rb.residual)
     np.testing.assert_array_equal(a, b)
 

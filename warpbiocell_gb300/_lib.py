@@ -90,17 +90,14 @@ class SorReportC(ctypes.Structure):
         ("converged", c_int32),
         ("path", c_int32),
         ("tiles", c_int32),
-        ("halo_depth", c_int32),
-        ("tiles_i", c_int32),
-        ("tiles_j", c_int32),
+        ("strips", c_int32),
     ]
 
 
 class SorTuningC(ctypes.Structure):
     _fields_ = [
-        ("halo_depth", c_int32),
-        ("tiles_i", c_int32),
-        ("tiles_j", c_int32),
+        ("tiles", c_int32),
+        ("strips", c_int32),
     ]
 
 
@@ -185,7 +182,7 @@ class SorBatchC(ctypes.Structure):
         ("total_tiles", c_int32),
         ("ctas", c_int32),
         ("threads", c_int32),
-        ("lanes", c_int32),
+        ("zclamp", c_int32),
         ("has_prod", c_int32),
         ("smem_bytes", c_int64),
         ("device_plan", c_void_p),
@@ -235,8 +232,8 @@ SIGNATURES: dict[str, list] = {
     "wbc_ftcs_step": [POINTER(SorParamsC), _F, _P, _P, _P, _P, _P, _P, _P],
     "wbc_sor_solve_workspace_bytes": [POINTER(SorParamsC)],
     "wbc_sor_wait_selftest": [_I, _I, _I, _P, c_size_t, _P],
-    "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, POINTER(SorReportC), _P,
-                      c_size_t, _I, POINTER(SorTuningC), _P],
+    "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, _P, POINTER(SorReportC),
+                      _P, c_size_t, _I, POINTER(SorTuningC), _P],
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
                          POINTER(c_float), _P],
     "wbc_sor_batch_plan_bytes": [_I],

@@ -404,9 +404,7 @@ int wbc_adjoint_field_solve(const wbc_sor_params* p, const float* u, const float
     report->converged = residual < tolerance ? 1 : 0;
     report->path = 1;
     report->tiles = 0;
-    report->halo_depth = 0;
-    report->tiles_i = 0;
-    report->tiles_j = 0;
+    report->strips = 0;
     return check_launch("wbc_adjoint_field_solve", launches + 1);
 }
 

@@ -1,29 +1,38 @@
 // Red-black SOR solve to convergence in one persistent, cooperative launch with the field held
 // in shared memory (kernels/field_kernels.py:185-243 iterated as fields/diffusion.py:79-123).
 //
-// Decomposition: the (i, j) plane is cut into tx x ty tiles of ti x tj columns; each CTA (one
-// per SM) owns one tile with the full z extent. Shared memory holds the tile plus a halo of all
-// columns within L1 distance H of it, split by k parity (E[col][m] = f(k = 2m),
-// O[col][m] = f(k = 2m + 1)): within a column all nodes of one colour share a k parity, so a warp
-// that owns a column updates its colour with 32 consecutive words per access and no bank
-// conflicts, and the k-neighbours of entry m are entries m - 1 + kp and m + kp of the other
-// parity (clamped at the ends, which is exactly the reference's mirror rule). At the start each
-// CTA writes the uptake coefficients density * uptake_max of its columns, split the same way, to
-// an L2-resident scratch copy (a negative value marks the nodes that are never updated:
-// Dirichlet faces and pinned nodes).
+// Decomposition: the (i, j) plane of columns is cut into `strips` strips along j, and each strip's
+// columns, taken row by row, into consecutive runs of equal length: one run per CTA (one CTA per
+// SM), so every CTA owns the same number of columns to within one. A tile is thus a block of
+// strip rows whose first and last rows may be partial (a staircase). Shared memory holds the
+// tile's bounding box plus a one-column halo, split by colour: plane c holds the nodes with
+// (i + j + k) % 2 == c, entry m of a column being its node k = 2m + ((c + i + j) & 1). All six
+// neighbours of a node of colour c lie in plane 1 - c: the lateral ones at the same entry of the
+// neighbouring columns, the k-neighbours at entries m - 1 + kp and m + kp (kp = the k parity of
+// the node), clamped at the column ends when the z faces are Neumann (the reference's mirror
+// rule). Dirichlet faces, pinned nodes and the padding entry of odd-length colour columns carry
+// no uptake coefficient and are never written.
 //
-// Temporal blocking: between two halo exchanges a tile performs H colour half-sweeps; the p-th
-// updates the columns within distance H - 1 - p of the tile (the ring columns redundantly, with
-// the same inputs and the same float expression as their owner, hence the same bits), so each
-// half-sweep still reads only values that are current. Columns outside the domain (on a Neumann
-// face) are refreshed by copying their mirror column after every half-sweep. After the H
-// half-sweeps the columns within H of the tile edge are published to a double-buffered,
-// parity-split exchange buffer in L2, the tile waits for its neighbouring tiles' epoch flags
-// (release / acquire; 4 neighbours for H = 1, 8 for H > 1), and pulls its halo. Every
-// `check_every` sweeps the max-norm residual is reduced (warp shuffles, one atomicMax per CTA,
-// the only global barrier) and all CTAs stop together once it is below the tolerance: the
-// reference's sweep count, residual and stopping rule, with no host round trip. The field after
-// n sweeps is bit-identical to the oracle's and to the streaming kernels'.
+// Work: the tile's columns form runs of consecutive columns in a box row, and within one colour
+// plane the entries of a run are contiguous; each run is cut into groups of 96 entries (three
+// lane-chunks of 32) that may span several columns, and a warp relaxes one group at a time with one
+// descriptor for its three lane-chunks, so no lane idles except at the end of a run (at 161 z
+// levels a column holds 81 entries per colour: 32-entry slots per column would leave 16% of the
+// lanes idle). At the start each CTA builds its group lists, loads its box, and writes the uptake
+// coefficients density * uptake_max of its columns, split the same way, to an L2-resident copy
+// (-1 marks nodes that are never updated), together with the production term when there is one.
+//
+// Halo exchange: the tile's edge columns (those with an in-domain neighbour owned by another
+// tile) are relaxed first, and each new value is stored to an exchange buffer in L2 as one
+// 64-bit word {value, half-sweep tag} with a relaxed store; the inner columns follow; then the
+// halo columns are read from their owners' tagged words, re-reading any word whose tag is not yet
+// this half-sweep's. No flag, fence or barrier is needed between neighbouring tiles: a neighbour
+// rewrites a word two half-sweeps later, which needs this tile's words of the half-sweep in
+// between, written after this read. Every `check_every` sweeps the max-norm residual is reduced
+// (warp shuffles, one atomicMax per CTA, the only global barrier) and all CTAs stop together once
+// it is below the tolerance: the reference's sweep count, residual and stopping rule, with no host
+// round trip. The field after n sweeps is bit-identical to the oracle's and to the streaming
+// kernels'.
 //
 // Every wait is bounded in time (kWaitLimitNs of the GPU's global timer, 2 s); on timeout the CTA
 // raises an abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
@@ -46,19 +55,19 @@ struct __align__(128) SorControl {
     int pad[25];
 };
 static_assert(sizeof(SorControl) == 128, "SorControl is one 128-byte line");
-constexpr int kMaxCtas = 1024;  // barrier flags that follow the control block
+constexpr int kMaxCtas = 1024;     // barrier flags that follow the control block
+constexpr int kSorThreads = 1024;  // threads per CTA of the resident solver
+constexpr int kMaxEntries = 1023;  // entries per colour column (nz <= 2045): 10 bits of a chunk word
+constexpr int kPlaneSlack = 64;    // floats past the largest box: lanes beyond a run's end read there
 
+// Shared-memory layout of one tile, sized for the largest tile of the solve.
 struct SorTiling {
-    int tx, ty;  // CTAs along i and j
-    int ti, tj;  // tile extent (columns) along i and j
-    int M;       // column stride per parity: (nz + 1) / 2 entries rounded up to 4 (16-byte rows)
-    int lanes;   // 32-entry chunks per parity column
-    int threads;
-    int H;       // halo depth = half-sweeps between exchanges
-    int nbox;    // columns of the bounding box (ti + 2H) * (tj + 2H)
-    size_t planes_bytes;
-    size_t table_offset;  // byte offset of the column table (2 int4 per box column)
-    size_t smem;
+    int tiles, strips;  // CTAs; strips along j
+    int M;              // entries per colour column: (nz + 1) / 2
+    int max_box;        // columns of the largest bounding box (halo included)
+    int relax_cap, pull_cap, mirror_cap, run_cap;
+    size_t plane_floats;  // floats per colour plane
+    size_t relax_off, masks_off, pull_off, mirror_off, run_off, kind_off, smem;
 };
 
 struct SorArgs {
@@ -69,20 +78,20 @@ struct SorArgs {
     const float* production;
     const float* source;
     float* field;
-    float* xchg;   // [2 buffers][2 parities][nx][ny][M] halo exchange
-    float* coeff;  // [2][nx][ny][M] density * uptake_max, -1 where not updated
+    unsigned long long* xchg;  // [2 colours][nx][ny][M] tagged halo words
+    float* coeff;              // [2][nx][ny][M] density * uptake_max, -1 where not updated
+    float* pcopy;              // [2][nx][ny][M] production term of every updated node
     SorControl* ctl;
     unsigned int* flags;  // [tiles] barrier epochs
+    float* residual_out;  // optional device float: the final residual
     int check_every;
     int max_sweeps;
     double tolerance;  // compared in double, as the reference compares float(residual) < tolerance
-    float* pcopy;      // [2][nx][ny][M] production term of every updated node (production, source)
 };
 
 // Every device wait gives up after kWaitLimitNs nanoseconds of the GPU's global timer without
 // progress. The timer is read every 256 polls, so a wait ends within a few microseconds of the limit.
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;  // 2 s
-constexpr int kMaxLanesPerColumn = 8;         // M <= 256 (nz <= 511)
 
 __device__ __forceinline__ unsigned int load_acquire(const unsigned int* p) {
     unsigned int v;
@@ -118,11 +127,9 @@ struct WaitClock {
     }
 };
 
-// ---- halo exchange with tagged words (H = 1) ------------------------------------------------------------
+// ---- halo exchange with tagged words --------------------------------------------------------------
 // Each exchanged entry is one 64-bit word {value bits, tag} written with a single relaxed store, so a
-// reader that sees the tag of the half-sweep it needs also sees that half-sweep's value: no flag,
-// fence or barrier between neighbouring tiles. The buffer has the layout of the coefficient copy
-// ([parity][nx][ny][M]) in 8-byte words.
+// reader that sees the tag of the half-sweep it needs also sees that half-sweep's value.
 __device__ __forceinline__ void store_tagged(unsigned long long* p, float v, unsigned int tag) {
     const unsigned long long word = (static_cast<unsigned long long>(tag) << 32) | __float_as_uint(v);
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(word) : "memory");
@@ -134,25 +141,21 @@ __device__ __forceinline__ unsigned long long load_tagged(const unsigned long lo
     return word;
 }
 
-__device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n - 1 ? n - 2 : i); }
+__host__ __device__ __forceinline__ int mirror(int i, int n) { return i < 0 ? 1 : (i > n - 1 ? n - 2 : i); }
 
-// Signals this CTA's arrival at the next epoch, then waits for the CTAs listed in `wait_for`
-// (n_wait of them) or, with n_wait < 0, for every CTA. Returns false when aborted (timeout here or
-// elsewhere). A halo exchange only needs the neighbouring tiles; the residual needs all.
-// `me` is this CTA's tile among the `ntiles` tiles of its solve.
+// Signals this CTA's arrival at the next epoch, then waits for every CTA of the solve. Returns
+// false when aborted (timeout here or elsewhere). `me` is this CTA's tile among `ntiles`.
 __device__ __forceinline__ bool grid_barrier(SorControl* ctl, unsigned int* flags, unsigned int& epoch, int me,
-                                             int ntiles, const int* wait_for = nullptr, int n_wait = -1,
-                                             const unsigned int* claims = nullptr, unsigned int claims_needed = 0) {
+                                             int ntiles, const unsigned int* claims = nullptr,
+                                             unsigned int claims_needed = 0) {
     epoch += 1;
     __syncthreads();  // the CTA's writes happen before thread 0's release (bar.sync is cumulative)
     if (threadIdx.x == 0) store_release(flags + me, epoch);
     int aborted = 0;
-    const unsigned n = n_wait < 0 ? static_cast<unsigned>(ntiles) : static_cast<unsigned>(n_wait);
-    for (unsigned t = threadIdx.x; t < n; t += blockDim.x) {
-        const unsigned who = n_wait < 0 ? t : static_cast<unsigned>(wait_for[t]);
+    for (int t = threadIdx.x; t < ntiles; t += blockDim.x) {
         unsigned polls = 0;
         WaitClock clock{0ull, claims, claims_needed};
-        while (static_cast<int>(load_acquire(flags + who) - epoch) < 0) {
+        while (static_cast<int>(load_acquire(flags + t) - epoch) < 0) {
             if ((++polls & 255u) == 0u) {
                 if (load_acquire(&ctl->abort) != 0u) {
                     aborted = 1;
@@ -176,30 +179,51 @@ __device__ __forceinline__ float prod_term(const SorArgs& a, int64_t idx) {
     return prod * div_rn(v, a.p.source_k + v);
 }
 
-// Column lists in shared memory, after the two parity planes. A column is an int2:
-// x = index in the bounding box, y = (gi << 16) | gj with gi, gj its (mirrored) global position.
-struct Lists {
-    int2* upd;       // in-domain columns within distance H - 1, by distance (owned first)
-    int* upd_end;    // upd_end[d]: columns within distance d (d = 0 .. H - 1)
-    int2* pull;      // in-domain columns at distance 1 .. H
-    int2* publish;   // owned columns within H of the tile edge
-    int2* inner;     // owned columns farther than H from the tile edge
-    int2* mir;       // outside the domain: x = box index, y = box index of the mirror column
-    int n_pull, n_publish, n_inner, n_mir;
+// ---- the partition ------------------------------------------------------------------------------------
+// Strip s covers columns j in [strip_start(s), strip_start(s + 1)); its tiles are the runs
+// tiles_before(s) ... tiles_before(s + 1) - 1 of its columns in (i, j) order, cut evenly.
+struct TileRect {
+    int ia, ib;  // first and last row
+    int ja, jb;  // the first row starts at column ja, the last row ends before column jb
+    int j0, j1;  // the strip's columns
 };
 
-// Loop invariants of a colour half-sweep.
-struct Sweep {
-    float* s;
-    const int4* tab;
-    const float* coeff;
-    float* xchg;  // exchange buffer, laid out like the coefficient scratch copy
-    int ncm, M, si, nx, ny, nz, cnt_even, cnt_odd;
-    int64_t sx;
-    float K, h, omega, one_minus_omega;
-    bool zclamp;  // Neumann z faces: the k-neighbours of the end nodes are mirrored
-    bool fast;    // K, h and every coefficient of this tile pass the fixed range tests below
-};
+__host__ __device__ __forceinline__ int strip_start(int s, int strips, int ny) {
+    return static_cast<int>(static_cast<int64_t>(s) * ny / strips);
+}
+
+__host__ __device__ __forceinline__ int tiles_before(int s, int strips, int ny, int tiles) {
+    const int64_t j = strip_start(s, strips, ny);
+    return static_cast<int>((2 * static_cast<int64_t>(tiles) * j + ny) / (2 * static_cast<int64_t>(ny)));
+}
+
+__host__ __device__ __forceinline__ TileRect tile_rect(int t, int tiles, int strips, int nx, int ny) {
+    int s = 0;
+    while (s + 1 < strips && tiles_before(s + 1, strips, ny, tiles) <= t) ++s;
+    TileRect r;
+    r.j0 = strip_start(s, strips, ny);
+    r.j1 = strip_start(s + 1, strips, ny);
+    const int w = r.j1 - r.j0;
+    const int t0 = tiles_before(s, strips, ny, tiles);
+    const int tn = tiles_before(s + 1, strips, ny, tiles) - t0;
+    const int64_t cols = static_cast<int64_t>(nx) * w;
+    const int64_t q0 = (t - t0) * cols / tn, q1 = (t - t0 + 1) * cols / tn;
+    r.ia = static_cast<int>(q0 / w);
+    r.ja = r.j0 + static_cast<int>(q0 % w);
+    r.ib = static_cast<int>((q1 - 1) / w);
+    r.jb = r.j0 + static_cast<int>((q1 - 1) % w) + 1;
+    return r;
+}
+
+__host__ __device__ __forceinline__ bool owns(const TileRect& r, int i, int j) {
+    if (i < r.ia || i > r.ib || j < r.j0 || j >= r.j1) return false;
+    if (i == r.ia && j < r.ja) return false;
+    if (i == r.ib && j >= r.jb) return false;
+    return true;
+}
+
+// Column kinds of the bounding box.
+enum : unsigned char { kNone = 0, kInner = 1, kEdge = 2, kPull = 3, kMirror = 4 };
 
 // Operand ranges of the update's two divisions, cu = u / (K + o) and gs = a2 / (6 + h cu), for the
 // fast correctly rounded quotient (div_fast_range: both operands within [2^-60, 2^60], numerator
@@ -229,30 +253,6 @@ __device__ __forceinline__ bool numerator_in_range(float a2) {
     return b == 0u || b - 0x21800000u <= 0x5d800000u - 0x21800000u;  // +0 or [2^-60, 2^60]
 }
 
-// Per (box column, colour) entry of the column table in shared memory:
-// x = offset of entry 0 of the parity the colour updates, y = the same for the other parity,
-// z = offset of the column's coefficient row (that parity) in the scratch copy,
-// w = kp | cnt << 1 | last << 11 (kp: the parity updated, cnt: its entries, last: the other
-// parity's last entry).
-__device__ __forceinline__ int4 column_entry(const Sweep& w, int box, int gi, int gj, int colour) {
-    const int kp = (colour + gi + gj) & 1;
-    const int cnt = kp ? w.cnt_odd : w.cnt_even;
-    const int last = (kp ? w.cnt_even : w.cnt_odd) - 1;
-    return make_int4(kp * w.ncm + box * w.M, (kp ^ 1) * w.ncm + box * w.M, ((kp * w.nx + gi) * w.ny + gj) * w.M,
-                     kp | (cnt << 1) | (last << 11));
-}
-
-template <int LANES>
-__device__ __forceinline__ void load_column(const Sweep& w, const int2* list, int q, int colour, int lane, int2& c,
-                                            int4& e, float (&du)[LANES]) {
-    c = list[q];
-    e = w.tab[2 * c.x + colour];
-    const int cnt = (e.w >> 1) & 1023;
-    const float* crow = w.coeff + e.z + lane;
-#pragma unroll
-    for (int r = 0; r < LANES; ++r) du[r] = lane + 32 * r < cnt ? crow[32 * r] : -1.0f;
-}
-
 // The update's quotient with IEEE divisions, for operands outside the fast quotient's range. Out
 // of line, so the rarely taken branch to it stays a branch instead of predicated code in every
 // node's path.
@@ -269,544 +269,459 @@ __device__ __noinline__ float residual_exact(float u, float b1, float nb, float 
     return __fdiv_rn(fabsf(res), den);
 }
 
-// Entries m = lane + 32 r of one parity column: `po` points at entry `lane`, the four lateral
-// neighbours are po -+ si (i) and po -+ M (j). The k-neighbours of entry m are entries m + kp - 1
-// and m + kp of the other parity: with Dirichlet z faces every updated node has both inside the
-// column (pv points at entry lane + kp - 1), with Neumann z faces they are clamped to the column
-// ends (the mirror rule k = -1 -> 1, k = nz -> nz - 2). Every lane computes; only nodes with a
-// coefficient (not a Dirichlet face, a pinned node or past the column end) are written, and the
-// IEEE division replaces the fast one only where the range tests above do not hold.
-template <bool HAS_PROD, bool ZCLAMP, int LANES>
-__device__ __forceinline__ void relax_nodes(const SorArgs& a, const Sweep& w, float* po, const float* pv, int lane,
-                                            int kp, int last, const float* prow, unsigned long long* xrow, int cnt,
-                                            unsigned int tag, const float (&du)[LANES]) {
-    const float* pim = po - w.si;
-    const float* pip = po + w.si;
-    const float* pjm = po - w.M;
-    const float* pjp = po + w.M;
-#pragma unroll
-    for (int r = 0; r < LANES; ++r) {
-        const int off = 32 * r;
-        const bool active = du[r] >= 0.0f;
-        const float o = po[off];
-        const float b1 = w.K + o;
-        float cc = div_rn_fast_nonneg_zero(du[r], b1);
-        float prod = 0.0f;
-        if (HAS_PROD) {
-            if (active) prod = prow[off];
-        }
-        float vlo, vhi;
-        if (ZCLAMP) {
-            const int m = lane + off;
-            vlo = pv[max(m + kp - 1, 0)];
-            vhi = pv[min(m + kp, last)];
-        } else {
-            vlo = pv[off];
-            vhi = pv[off + 1];
-        }
-        const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
-        // Without production h * 0 = +0 and nb + 0 = nb except for nb = -0, which the range test
-        // sends to the exact branch below.
-        float a2 = HAS_PROD ? nb + w.h * prod : nb;
-        float b2 = 6.0f + w.h * cc;
-        float gs = div_rn_fast_nonneg_zero(a2, b2);
-        if (active && !(w.fast && old_value_in_range(o) && numerator_in_range(a2))) gs = gs_exact(du[r], b1, nb, prod, w.h);
-        const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
-        if (active) po[off] = v;
-        // An edge column publishes every entry (unchanged ones too) with this half-sweep's tag.
-        if (xrow && lane + off < cnt) store_tagged(xrow + off, active ? v : o, tag);
+// Loop invariants of the solve on one tile.
+struct Sweep {
+    float* s;  // plane 0; plane 1 follows `plane` floats later
+    const int4* relax;  // groups
+    const uint4* masks;
+    const int4* pull;
+    const int2* mir;
+    int n_relax, n_pull, n_mir;
+    int64_t plane;   // floats per shared-memory plane
+    int64_t gplane;  // entries per colour plane of the global copies: nx * ny * M
+    int M, si;       // entries per colour column; box row stride in floats
+    float K, h, omega, one_minus_omega;
+    bool fast;  // K, h and every coefficient of this tile pass the fixed range tests above
+};
+
+// Relaxed entries are listed in groups of up to kGroup consecutive entries of one run (one
+// descriptor per group, so the per-group bookkeeping is shared by its kGroup / 32 lane-chunks).
+// A group (int4): x = its first entry in a shared-memory plane, y = its first entry in colour
+// plane 0 of the global copies, z = edge | (m of its first entry) << 8, w = valid entries; beside
+// it a uint4 of lane masks, bit l of word r: (i + j) & 1 of the column of entry 32 r + l.
+// A pull chunk (int4): x, y as above for 32 entries, z = valid lanes.
+constexpr int kGroup = 96;
+constexpr int kSub = kGroup / 32;
+static_assert(kGroup % 32 == 0 && kSub <= 4, "a group's lane masks fit one uint4");
+__device__ __forceinline__ bool group_edge(const int4& d) { return d.z & 1; }
+
+// With Neumann z faces: the entry m of lane `lane` and the last entry of the other colour's
+// column (which holds k parity 1 - kp: (nz + 1) / 2 entries for even k, nz / 2 for odd k).
+__device__ __forceinline__ void lane_entry(const Sweep& w, const int4& d, int entry, int kp, int nz, int& m,
+                                           int& last) {
+    m = ((d.z >> 8) + entry) % w.M;
+    last = (kp ? (nz + 1) / 2 : nz / 2) - 1;
+}
+
+// The six neighbours in the other colour's plane; pv points at the node's own entry there.
+template <bool ZCLAMP>
+__device__ __forceinline__ float neighbour_sum(const Sweep& w, const float* pv, int kp, int m, int last) {
+    float vlo, vhi;
+    if (ZCLAMP) {
+        vlo = pv[max(m + kp - 1, 0) - m];
+        vhi = pv[min(m + kp, last) - m];
+    } else {
+        vlo = pv[kp - 1];
+        vhi = pv[kp];
     }
+    return pv[-w.si] + pv[w.si] + pv[-w.M] + pv[w.M] + vlo + vhi;
 }
 
-// One colour of one column: the reference's update (field_kernels.py:185-212) with the
-// Michaelis-Menten uptake linearised at the old value, over-relaxed and clamped at zero.
-template <bool HAS_PROD, int LANES>
-__device__ __forceinline__ void relax_column(const SorArgs& a, const Sweep& w, int2 c, int4 e, int lane,
-                                             unsigned int tag, const float (&du)[LANES]) {
-    const int kp = e.w & 1;
-    const int last = e.w >> 11;
-    float* po = w.s + e.x + lane;
-    const float* oth = w.s + e.y;
-    const float* prow = HAS_PROD ? a.pcopy + e.z + lane : nullptr;
-    unsigned long long* xrow = tag ? reinterpret_cast<unsigned long long*>(w.xchg) + e.z + lane : nullptr;
-    const int cnt = (e.w >> 1) & 1023;
-    if (w.zclamp)
-        relax_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, prow, xrow, cnt, tag, du);
-    else
-        relax_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, prow, xrow, cnt, tag,
-                                            du);
+// One lane-chunk (32 entries from `off` of group d) of colour `colour`: the reference's update
+// (field_kernels.py:185-212) with the Michaelis-Menten uptake linearised at the old value,
+// over-relaxed and clamped at zero. `own` and `oth` point at this lane's entry 0 of the two
+// colour planes. Every lane computes; only nodes with a coefficient are written, and the IEEE
+// division replaces the fast one only where the range tests above do not hold. An edge group also
+// stores every valid entry (unchanged ones too) to the exchange buffer with this half-sweep's tag.
+template <bool HAS_PROD, bool ZCLAMP>
+__device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, float* po, const float* pv,
+                                            unsigned long long* xp, const int4& d, int off, unsigned mask, float du,
+                                            float prod, int colour, int lane, unsigned int tag) {
+    const int kp = ((mask >> lane) & 1) ^ colour;
+    int m = 0, last = 0;
+    if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
+    const bool active = du >= 0.0f;
+    const float o = *po;
+    const float b1 = w.K + o;
+    const float cc = div_rn_fast_nonneg_zero(du, b1);
+    const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
+    // Without production h * 0 = +0 and nb + 0 = nb except for nb = -0, which the range test
+    // sends to the exact branch below.
+    const float a2 = HAS_PROD ? nb + w.h * prod : nb;
+    const float b2 = 6.0f + w.h * cc;
+    float gs = div_rn_fast_nonneg_zero(a2, b2);
+    if (active && !(w.fast && old_value_in_range(o) && numerator_in_range(a2))) gs = gs_exact(du, b1, nb, prod, w.h);
+    const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
+    if (active) *po = v;
+    if (group_edge(d) && off + lane < d.w) store_tagged(xp, active ? v : o, tag);
 }
 
-// The columns list[0 .. end) for one colour, a warp per column; the next column's table entry and
-// coefficients are loaded before the current column is relaxed. A nonzero `tag` also publishes
-// the columns to the exchange buffer.
-template <bool HAS_PROD, int LANES>
-__device__ __forceinline__ void relax_columns(const SorArgs& a, const Sweep& w, const int2* list, int end, int colour,
-                                              int warp, int nwarps, int lane, unsigned int tag = 0u) {
+// The groups of one colour, a warp per group, edge groups first; the next group's coefficients
+// (and production terms), which live in L2, are loaded before the current group is relaxed.
+template <bool HAS_PROD, bool ZCLAMP>
+__device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, int colour, int warp, int nwarps,
+                                             int lane, unsigned int tag) {
     int q = warp;
-    if (q >= end) return;
-    int2 c;
-    int4 e;
-    float du[LANES];
-    load_column<LANES>(w, list, q, colour, lane, c, e, du);
+    if (q >= w.n_relax) return;
+    const float* coeff = a.coeff + colour * w.gplane + lane;
+    const float* pc = HAS_PROD ? a.pcopy + colour * w.gplane + lane : nullptr;
+    float* own = w.s + colour * w.plane + lane;
+    const float* oth = w.s + (colour ^ 1) * w.plane + lane;
+    unsigned long long* xrow = a.xchg + colour * w.gplane + lane;
+    int4 d = w.relax[q];
+    float du[kSub], pr[kSub];
+#pragma unroll
+    for (int r = 0; r < kSub; ++r) {
+        du[r] = lane + 32 * r < d.w ? coeff[d.y + 32 * r] : -1.0f;
+        pr[r] = HAS_PROD && du[r] >= 0.0f ? pc[d.y + 32 * r] : 0.0f;
+    }
     while (true) {
         const int qn = q + nwarps;
-        const bool more = qn < end;
-        int2 cn = c;
-        int4 en = e;
-        float dn[LANES];
-        if (more) load_column<LANES>(w, list, qn, colour, lane, cn, en, dn);
-        relax_column<HAS_PROD, LANES>(a, w, c, e, lane, tag, du);
-        if (!more) break;
-        c = cn;
-        e = en;
+        const bool more = qn < w.n_relax;
+        int4 dn = d;
+        float dun[kSub], prn[kSub];
+        if (more) dn = w.relax[qn];
 #pragma unroll
-        for (int r = 0; r < LANES; ++r) du[r] = dn[r];
+        for (int r = 0; r < kSub; ++r) {
+            dun[r] = more && lane + 32 * r < dn.w ? coeff[dn.y + 32 * r] : -1.0f;
+            prn[r] = HAS_PROD && dun[r] >= 0.0f ? pc[dn.y + 32 * r] : 0.0f;
+        }
+        const uint4 mk = w.masks[q];
+        const unsigned mw[4] = {mk.x, mk.y, mk.z, mk.w};
+        float* po = own + d.x;
+        const float* pv = oth + d.x;
+        unsigned long long* xp = xrow + d.y;
+#pragma unroll
+        for (int r = 0; r < kSub; ++r)
+            if (r == 0 || d.w > 32 * r)
+                relax_lanes<HAS_PROD, ZCLAMP>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r], du[r],
+                                              pr[r], colour, lane, tag);
+        if (!more) break;
+        d = dn;
+#pragma unroll
+        for (int r = 0; r < kSub; ++r) {
+            du[r] = dun[r];
+            pr[r] = prn[r];
+        }
         q = qn;
     }
 }
 
-// Max-norm residual |r| / max(6 u, reference) of the nodes relax_nodes would update, with
+// Max-norm residual |r| / max(6 u, reference) of the group's nodes of colour `colour`, with
 // r = nb + h prod - (6 + h c) u (field_kernels.py:215-243), as float bits (all values are >= 0).
-template <bool HAS_PROD, bool ZCLAMP, int LANES>
-__device__ __forceinline__ unsigned int residual_nodes(const SorArgs& a, const Sweep& w, const float* po,
-                                                       const float* pv, int lane, int kp, int last, const float* prow,
-                                                       const float (&du)[LANES]) {
-    const float* pim = po - w.si;
-    const float* pip = po + w.si;
-    const float* pjm = po - w.M;
-    const float* pjp = po + w.M;
+template <bool HAS_PROD, bool ZCLAMP>
+__device__ __forceinline__ unsigned int residual_group(const SorArgs& a, const Sweep& w, int q, int colour,
+                                                       int lane) {
+    const int4 d = w.relax[q];
+    const uint4 mk = w.masks[q];
+    const unsigned mw[4] = {mk.x, mk.y, mk.z, mk.w};
     unsigned int bits = 0u;
 #pragma unroll
-    for (int r = 0; r < LANES; ++r) {
+    for (int r = 0; r < kSub; ++r) {
         const int off = 32 * r;
-        const bool active = du[r] >= 0.0f;
-        const float o = po[off];
+        if (off >= d.w) break;
+        const float du = off + lane < d.w ? a.coeff[colour * w.gplane + d.y + off + lane] : -1.0f;
+        const bool active = du >= 0.0f;
+        const float prod = HAS_PROD && active ? a.pcopy[colour * w.gplane + d.y + off + lane] : 0.0f;
+        const int kp = ((mw[r] >> lane) & 1) ^ colour;
+        const float* po = w.s + colour * w.plane + d.x + off + lane;
+        const float* pv = w.s + (colour ^ 1) * w.plane + d.x + off + lane;
+        int m = 0, last = 0;
+        if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
+        const float o = *po;
         const float b1 = w.K + o;
-        float cc = div_rn_fast(du[r], b1);
-        float prod = 0.0f;
-        if (HAS_PROD) {
-            if (active) prod = prow[off];
-        }
-        float vlo, vhi;
-        if (ZCLAMP) {
-            const int m = lane + off;
-            vlo = pv[max(m + kp - 1, 0)];
-            vhi = pv[min(m + kp, last)];
-        } else {
-            vlo = pv[off];
-            vhi = pv[off + 1];
-        }
-        const float nb = pim[off] + pip[off] + pjm[off] + pjp[off] + vlo + vhi;
-        float res = nb + w.h * prod - (6.0f + w.h * cc) * o;
+        const float cc = div_rn_fast(du, b1);
+        const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
+        const float res = nb + w.h * prod - (6.0f + w.h * cc) * o;
         const float den = fmaxf(6.0f * o, a.p.reference);
         float val = div_rn_fast(fabsf(res), den);
-        if (active && !(div_fast_range(du[r], b1) && div_fast_range(fabsf(res), den)))
-            val = residual_exact(du[r], b1, nb, prod, w.h, o, den);
+        if (active && !(div_fast_range(du, b1) && div_fast_range(fabsf(res), den)))
+            val = residual_exact(du, b1, nb, prod, w.h, o, den);
         if (active) bits = max(bits, __float_as_uint(val));
     }
     return bits;
 }
 
-// Residual bits of one column's `colour` nodes.
-template <bool HAS_PROD, int LANES>
-__device__ __forceinline__ unsigned int residual_column(const SorArgs& a, const Sweep& w, const int2* list, int q,
-                                                        int colour, int lane) {
-    int2 c;
-    int4 e;
-    float du[LANES];
-    load_column<LANES>(w, list, q, colour, lane, c, e, du);
-    const int kp = e.w & 1;
-    const int last = e.w >> 11;
-    const float* po = w.s + e.x + lane;
-    const float* oth = w.s + e.y;
-    const float* prow = HAS_PROD ? a.pcopy + e.z + lane : nullptr;
-    if (w.zclamp) return residual_nodes<HAS_PROD, true, LANES>(a, w, po, oth, lane, kp, last, prow, du);
-    return residual_nodes<HAS_PROD, false, LANES>(a, w, po, oth + kp - 1 + lane, lane, kp, last, prow, du);
-}
-
-// Reads the parity `colour` updated in each listed halo column once every entry carries `tag`
-// (two columns per warp at a time, all of their words in flight before any is checked) and stores
-// the values in shared memory. Returns false when a wait timed out or another CTA aborted.
-template <int LANES>
-__device__ __forceinline__ bool pull_tagged(const Sweep& w, const int2* list, int n, int colour, unsigned int tag,
-                                            const SorControl* ctl, int warp, int nwarps, int lane) {
-    const unsigned long long* ll = reinterpret_cast<const unsigned long long*>(w.xchg);
+// Reads colour `colour` of the halo columns once every entry carries `tag` and stores the values
+// in shared memory; each warp has the words of up to kBatch chunks in flight before it checks
+// any (their descriptors are re-read from shared memory, so only the words occupy registers).
+// Returns false when a wait timed out or another CTA aborted.
+__device__ __forceinline__ bool pull_halo(const SorArgs& a, const Sweep& w, int colour, unsigned int tag, int warp,
+                                          int nwarps, int lane) {
+    constexpr int kBatch = 5;
+    const unsigned long long* src = a.xchg + colour * w.gplane + lane;
+    float* dst = w.s + colour * w.plane + lane;
     bool fine = true;
-    for (int q0 = warp; q0 < n; q0 += 2 * nwarps) {
-        const unsigned long long* src[2];
-        float* dst[2];
-        int cnt[2];
+    for (int q0 = warp; q0 < w.n_pull; q0 += kBatch * nwarps) {
+        unsigned long long v[kBatch];
 #pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int q = q0 + u * nwarps;
-            cnt[u] = 0;
-            src[u] = nullptr;
-            dst[u] = nullptr;
-            if (q < n) {
-                const int2 c = list[q];
-                const int gi = c.y >> 16, gj = c.y & 0xffff;
-                const int par = (colour + gi + gj) & 1;
-                cnt[u] = par ? w.cnt_odd : w.cnt_even;
-                src[u] = ll + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
-                dst[u] = w.s + par * w.ncm + c.x * w.M + lane;
+        for (int b = 0; b < kBatch; ++b) {
+            const int q = q0 + b * nwarps;
+            v[b] = 0ull;
+            if (q < w.n_pull) {
+                const int4 d = w.pull[q];
+                if (lane < d.z) v[b] = load_tagged(src + d.y);
             }
         }
-        unsigned long long v[2][LANES];
 #pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-            for (int r = 0; r < LANES; ++r)
-                if (lane + 32 * r < cnt[u]) v[u][r] = load_tagged(src[u] + 32 * r);
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-            for (int r = 0; r < LANES; ++r)
-                if (lane + 32 * r < cnt[u]) {
-                    unsigned polls = 0;
-                    WaitClock clock;
-                    while (static_cast<unsigned int>(v[u][r] >> 32) != tag) {
-                        if ((++polls & 255u) == 0u && (load_acquire(&ctl->abort) != 0u || clock.expired())) {
-                            fine = false;
-                            break;
-                        }
-                        v[u][r] = load_tagged(src[u] + 32 * r);
+        for (int b = 0; b < kBatch; ++b) {
+            const int q = q0 + b * nwarps;
+            if (q >= w.n_pull) break;
+            const int4 d = w.pull[q];
+            if (lane < d.z) {
+                unsigned polls = 0;
+                WaitClock clock;
+                while (static_cast<unsigned int>(v[b] >> 32) != tag) {
+                    if ((++polls & 255u) == 0u && (load_acquire(&a.ctl->abort) != 0u || clock.expired())) {
+                        fine = false;
+                        break;
                     }
-                    dst[u][32 * r] = __uint_as_float(static_cast<unsigned int>(v[u][r]));
+                    v[b] = load_tagged(src + d.y);
                 }
+                dst[d.x] = __uint_as_float(static_cast<unsigned int>(v[b]));
+            }
+        }
     }
     return fine;
 }
 
-// Copies one parity (the one colour `colour` updates in each column) or both parities of the
-// listed columns between the exchange buffer and shared memory. A warp moves two column parities
-// at a time and loads all of their entries before storing any, so two whole columns are in flight.
-template <int LANES>
-__device__ __forceinline__ void copy_columns(const Sweep& w, const int2* list, int n, float* xb, int colour,
-                                             bool both, bool to_xchg, int warp, int nwarps, int lane) {
-    const int per = both ? 2 : 1;
-    const int items = n * per;
-    for (int t0 = warp; t0 < items; t0 += 2 * nwarps) {
-        float* src[2];
-        float* dst[2];
-        int cnt[2];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-            const int t = t0 + u * nwarps;
-            cnt[u] = 0;
-            src[u] = dst[u] = nullptr;
-            if (t < items) {
-                const int2 c = list[both ? (t >> 1) : t];
-                const int gi = c.y >> 16, gj = c.y & 0xffff;
-                const int par = both ? (t & 1) : ((colour + gi + gj) & 1);
-                cnt[u] = par ? w.cnt_odd : w.cnt_even;
-                float* x = xb + ((static_cast<int64_t>(par) * w.nx + gi) * w.ny + gj) * w.M + lane;
-                float* sm = w.s + par * w.ncm + c.x * w.M + lane;
-                src[u] = to_xchg ? sm : x;
-                dst[u] = to_xchg ? x : sm;
+// Refreshes colour `colour` of the ghost columns outside a Neumann face from their mirror columns.
+__device__ __forceinline__ void mirror_columns(const Sweep& w, int colour, int warp, int nwarps, int lane) {
+    for (int q = warp; q < w.n_mir; q += nwarps) {
+        const int2 c = w.mir[q];
+        float* dst = w.s + colour * w.plane + static_cast<int64_t>(c.x) * w.M;
+        const float* src = w.s + colour * w.plane + static_cast<int64_t>(c.y) * w.M;
+        for (int m = lane; m < w.M; m += 32) dst[m] = src[m];
+    }
+}
+
+// Builds the tile's column kinds, runs and chunk lists in shared memory and fills the list fields
+// of `w`.
+__device__ __forceinline__ void build_lists(const SorArgs& a, const TileRect& r, Sweep& w, int warp, int nwarps,
+                                            int lane) {
+    const int nx = a.p.nx, ny = a.p.ny, M = a.t.M;
+    const int bw = r.j1 - r.j0 + 2;
+    const int rows = r.ib - r.ia + 3;
+    const int nbox = rows * bw;
+    char* base = reinterpret_cast<char*>(w.s);
+    unsigned char* kind = reinterpret_cast<unsigned char*>(base + a.t.kind_off);
+    int4* runs = reinterpret_cast<int4*>(base + a.t.run_off);
+    int4* relax = reinterpret_cast<int4*>(base + a.t.relax_off);
+    uint4* masks = reinterpret_cast<uint4*>(base + a.t.masks_off);
+    int4* pull = reinterpret_cast<int4*>(base + a.t.pull_off);
+    int2* mir = reinterpret_cast<int2*>(base + a.t.mirror_off);
+    __shared__ int s_counts[5];  // runs, edge groups, inner groups, pull chunks, mirror columns
+    // pass 1: the kind of every box column
+    for (int e = threadIdx.x; e < nbox; e += blockDim.x) {
+        const int i = r.ia - 1 + e / bw, j = r.j0 - 1 + e % bw;
+        unsigned char k = kNone;
+        if (owns(r, i, j)) {
+            k = kInner;
+            const int ni[4] = {i - 1, i + 1, i, i};
+            const int nj[4] = {j, j, j - 1, j + 1};
+            for (int q = 0; q < 4; ++q)
+                if (ni[q] >= 0 && ni[q] < nx && nj[q] >= 0 && nj[q] < ny && !owns(r, ni[q], nj[q])) k = kEdge;
+        } else if (owns(r, i - 1, j) || owns(r, i + 1, j) || owns(r, i, j - 1) || owns(r, i, j + 1)) {
+            const bool out_i = i < 0 || i >= nx, out_j = j < 0 || j >= ny;
+            if (!out_i && !out_j) {
+                k = kPull;
+            } else if (out_i != out_j && (out_i ? a.p.bc_x != 0 : a.p.bc_y != 0)) {
+                // Only the columns just outside a Neumann face are read (by the face column); across
+                // a Dirichlet face nothing reads them.
+                k = kMirror;
             }
         }
-        float v[2][LANES];
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-            for (int r = 0; r < LANES; ++r)
-                if (lane + 32 * r < cnt[u]) v[u][r] = to_xchg ? src[u][32 * r] : __ldcg(src[u] + 32 * r);
-#pragma unroll
-        for (int u = 0; u < 2; ++u)
-#pragma unroll
-            for (int r = 0; r < LANES; ++r)
-                if (lane + 32 * r < cnt[u]) {
-                    if (to_xchg)
-                        __stcg(dst[u] + 32 * r, v[u][r]);
-                    else
-                        dst[u][32 * r] = v[u][r];
-                }
+        kind[e] = k;
     }
-}
-
-// Refreshes the outside-the-domain columns from their mirror images: the parity that colour
-// `colour` updates in the mirror column, or both.
-__device__ __forceinline__ void mirror_columns(const Sweep& w, const int2* list, int n, int bw, int gi0, int gj0,
-                                               int colour, bool both, int warp, int nwarps, int lane) {
-    for (int q = warp; q < n; q += nwarps) {
-        const int2 c = list[q];
-        const int mi = c.y / bw, mj = c.y - (c.y / bw) * bw;
-        const int kp_colour = (colour + gi0 + mi + gj0 + mj) & 1;
-        for (int par = 0; par < 2; ++par) {
-            if (!both && par != kp_colour) continue;
-            const int cnt = par ? w.cnt_odd : w.cnt_even;
-            float* dst = w.s + par * w.ncm + c.x * w.M;
-            const float* src = w.s + par * w.ncm + c.y * w.M;
-            for (int m = lane; m < cnt; m += 32) dst[m] = src[m];
+    __syncthreads();
+    // pass 2 (one thread): runs of one kind along each box row with their first group (pull chunk);
+    // edge groups are numbered first, inner groups after every edge group.
+    if (threadIdx.x == 0) {
+        int n_runs = 0, n_edge = 0, n_inner = 0, n_pull = 0, n_mir = 0;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int row = 0; row < rows; ++row) {
+                int c = 0;
+                while (c < bw) {
+                    const unsigned char k = kind[row * bw + c];
+                    if (k == kMirror) {
+                        if (pass == 0) {
+                            const int i = r.ia - 1 + row, j = r.j0 - 1 + c;
+                            const int mi = mirror(i, nx) - (r.ia - 1), mj = mirror(j, ny) - (r.j0 - 1);
+                            mir[n_mir++] = make_int2(row * bw + c, mi * bw + mj);
+                        }
+                        c += 1;
+                        continue;
+                    }
+                    int len = 1;
+                    while (c + len < bw && kind[row * bw + c + len] == k) ++len;
+                    const int chunks = k == kPull ? (len * M + 31) / 32 : (len * M + kGroup - 1) / kGroup;
+                    if (pass == 0 ? (k == kEdge || k == kPull) : k == kInner) {
+                        int first;
+                        if (k == kEdge) {
+                            first = n_edge;
+                            n_edge += chunks;
+                        } else if (k == kInner) {
+                            first = n_edge + n_inner;
+                            n_inner += chunks;
+                        } else {
+                            first = n_pull;
+                            n_pull += chunks;
+                        }
+                        runs[n_runs++] = make_int4(row * bw + c, k | (len << 4), first, row);
+                    }
+                    c += len;
+                }
+            }
+        }
+        s_counts[0] = n_runs;
+        s_counts[1] = n_edge;
+        s_counts[2] = n_inner;
+        s_counts[3] = n_pull;
+        s_counts[4] = n_mir;
+    }
+    __syncthreads();
+    const int n_runs = s_counts[0];
+    // pass 3a: the pull chunks of each halo run, a warp per run
+    for (int q = warp; q < n_runs; q += nwarps) {
+        const int4 run = runs[q];
+        if ((run.y & 15) != kPull) continue;
+        const int len = run.y >> 4, box = run.x, row = run.w;
+        const int i = r.ia - 1 + row, j = r.j0 - 1 + box % bw;
+        const int total = len * M;
+        for (int c = lane; 32 * c < total; c += 32)
+            pull[run.z + c] = make_int4(box * M + 32 * c, (i * ny + j) * M + 32 * c, min(32, total - 32 * c), 0);
+    }
+    // pass 3b: the groups of each owned run, a warp per run
+    for (int q = warp; q < n_runs; q += nwarps) {
+        const int4 run = runs[q];
+        const int k = run.y & 15;
+        if (k != kEdge && k != kInner) continue;
+        const int len = run.y >> 4, box = run.x, row = run.w;
+        const int i = r.ia - 1 + row, j = r.j0 - 1 + box % bw;
+        const int total = len * M;
+        for (int c = 0; kGroup * c < total; ++c) {
+            const int first = kGroup * c, end = min(first + kGroup, total);
+            unsigned mw[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+            for (int rr = 0; rr < kSub; ++rr) {
+                const int f = first + 32 * rr + lane;
+                mw[rr] = __ballot_sync(0xffffffffu, f < end && ((i + j + f / M) & 1));
+            }
+            if (lane == 0) {
+                relax[run.z + c] = make_int4(box * M + first, (i * ny + j) * M + first,
+                                             (k == kEdge ? 1 : 0) | ((first % M) << 8), end - first);
+                masks[run.z + c] = make_uint4(mw[0], mw[1], mw[2], mw[3]);
+            }
         }
     }
+    __syncthreads();
+    w.relax = relax;
+    w.masks = masks;
+    w.pull = pull;
+    w.mir = mir;
+    w.n_relax = s_counts[1] + s_counts[2];
+    w.n_pull = s_counts[3];
+    w.n_mir = s_counts[4];
+    w.si = bw * M;
 }
 
-// Columns longer than 3 x 32 entries per parity run 16 warps per CTA (128 registers a thread).
-constexpr int max_threads_for_lanes(int lanes) { return lanes > 3 ? 512 : 1024; }
-
-// One tile (`tile` of `ntiles`) of one solve, for the whole solve.
-// `claims` / `claims_needed`: see WaitClock (batched solves; null for a single solve).
-template <bool HAS_PROD, int LANES, int H>
+// One tile (`tile` of `ntiles`) of one solve, for the whole solve. `claims` / `claims_needed`:
+// see WaitClock (batched solves; null for a single solve).
+template <bool HAS_PROD, bool ZCLAMP>
 __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles, const unsigned int* claims = nullptr,
                                          unsigned int claims_needed = 0) {
     extern __shared__ __align__(128) float s[];
     __shared__ unsigned int s_red[32];
-    __shared__ int s_counts[8 + 4];  // per distance class, then pull / publish / inner / mirror counters
+    __shared__ int s_outside_range;
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int bx = tile / a.t.ty;
-    const int by = tile - bx * a.t.ty;
-    const int i0 = bx * a.t.ti, j0 = by * a.t.tj;
-    const int ai = min(a.t.ti, nx - i0), aj = min(a.t.tj, ny - j0);
-    const int bw = a.t.tj + 2 * H;  // bounding-box row length
-    const int nbox = a.t.nbox;
+    const TileRect r = tile_rect(tile, ntiles, a.t.strips, nx, ny);
     Sweep w;
     w.s = s;
-    w.coeff = a.coeff;
+    w.plane = static_cast<int64_t>(a.t.plane_floats);
+    w.gplane = static_cast<int64_t>(nx) * ny * M;
     w.M = M;
-    w.ncm = nbox * M;  // floats per parity plane
-    w.si = bw * M;
-    w.nx = nx;
-    w.ny = ny;
-    w.nz = nz;
-    w.cnt_even = (nz + 1) / 2;
-    w.cnt_odd = nz / 2;
-    w.sx = static_cast<int64_t>(ny) * nz;
     w.K = a.p.michaelis_k;
     w.h = a.p.dx2_over_D;
     w.omega = a.p.omega;
     w.one_minus_omega = 1.0f - a.p.omega;
-    w.zclamp = a.p.bc_z != 0;
-    w.tab = reinterpret_cast<const int4*>(reinterpret_cast<char*>(s) + a.t.table_offset);
-    w.xchg = a.xchg;
-    __shared__ int s_neighbours[8];
-    __shared__ int s_n_neighbours;
-    if (threadIdx.x == 0) {
-        int n = 0;
-        for (int di = -1; di <= 1; ++di)
-            for (int dj = -1; dj <= 1; ++dj) {
-                if ((di == 0 && dj == 0) || (H == 1 && di != 0 && dj != 0)) continue;
-                const int nbx = bx + di, nby = by + dj;
-                if (nbx >= 0 && nbx < a.t.tx && nby >= 0 && nby < a.t.ty) s_neighbours[n++] = nbx * a.t.ty + nby;
-            }
-        s_n_neighbours = n;
-    }
-
-    // ---- column lists ---------------------------------------------------------------------------------
-    Lists L;
-    {
-        int2* base = reinterpret_cast<int2*>(reinterpret_cast<char*>(s) + a.t.planes_bytes);
-        L.upd = base;
-        L.pull = base + nbox;
-        L.publish = base + 2 * nbox;
-        L.inner = base + 3 * nbox;
-        L.mir = base + 4 * nbox;
-        L.upd_end = reinterpret_cast<int*>(base + 5 * nbox);
-    }
-    __shared__ int s_outside_range;
-    if (threadIdx.x < 12) s_counts[threadIdx.x] = 0;
     if (threadIdx.x == 0) s_outside_range = solve_constants_in_range(w.K, w.h) ? 0 : 1;
-    __syncthreads();
-    const int box_rows = ai + 2 * H, box_cols = aj + 2 * H;
-    auto dist_of = [&](int li, int lj) {
-        const int di = li < 0 ? -li : (li >= ai ? li - ai + 1 : 0);
-        const int dj = lj < 0 ? -lj : (lj >= aj ? lj - aj + 1 : 0);
-        return di + dj;
-    };
-    // pass 1: count in-domain columns per distance class
-    for (int e = threadIdx.x; e < box_rows * box_cols; e += blockDim.x) {
-        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
-        const int d = dist_of(li, lj);
-        const int gi = i0 + li, gj = j0 + lj;
-        if (d < H && gi >= 0 && gi < nx && gj >= 0 && gj < ny) atomicAdd(&s_counts[d], 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int run = 0;
-        for (int d = 0; d < H; ++d) {
-            const int c = s_counts[d];
-            s_counts[d] = run;  // start of class d
-            run += c;
-            L.upd_end[d] = run;
-        }
-    }
-    __syncthreads();
-    // pass 2: fill the lists
-    for (int e = threadIdx.x; e < box_rows * box_cols; e += blockDim.x) {
-        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
-        const int d = dist_of(li, lj);
-        if (d > H) continue;
-        const int gi = i0 + li, gj = j0 + lj;
-        const int box = (li + H) * bw + (lj + H);
-        const bool inside = gi >= 0 && gi < nx && gj >= 0 && gj < ny;
-        if (inside) {
-            const int2 c = make_int2(box, (gi << 16) | gj);
-            if (d < H) {
-                L.upd[atomicAdd(&s_counts[d], 1)] = c;
-                int4* tab = const_cast<int4*>(w.tab);
-                tab[2 * box] = column_entry(w, box, gi, gj, 0);
-                tab[2 * box + 1] = column_entry(w, box, gi, gj, 1);
-            }
-            if (d >= 1) L.pull[atomicAdd(&s_counts[8], 1)] = c;
-            if (d == 0) {
-                if (li < H || li >= ai - H || lj < H || lj >= aj - H)
-                    L.publish[atomicAdd(&s_counts[9], 1)] = c;
-                else
-                    L.inner[atomicAdd(&s_counts[10], 1)] = c;
-            }
-        } else {
-            // Only the columns just outside a Neumann face are read (by the face column, which is
-            // updated); across a Dirichlet face, at a corner or farther out nothing reads them.
-            const bool out_i = gi < 0 || gi >= nx, out_j = gj < 0 || gj >= ny;
-            const bool read = out_i != out_j && (out_i ? (a.p.bc_x != 0 && (gi == -1 || gi == nx))
-                                                       : (a.p.bc_y != 0 && (gj == -1 || gj == ny)));
-            if (read) {
-                const int mi = mirror(gi, nx) - i0 + H, mj = mirror(gj, ny) - j0 + H;
-                L.mir[atomicAdd(&s_counts[11], 1)] = make_int2(box, mi * bw + mj);
-            }
-        }
-    }
-    __syncthreads();
-    L.n_pull = s_counts[8];
-    L.n_publish = s_counts[9];
-    L.n_inner = s_counts[10];
-    L.n_mir = s_counts[11];
-    const int n_neighbours = s_n_neighbours;
-    const int gi0 = i0 - H, gj0 = j0 - H;  // global position of box row / column 0
+    build_lists(a, r, w, warp, nwarps, lane);
+    const int bw = r.j1 - r.j0 + 2;
+    const int rows = r.ib - r.ia + 3;
+    const unsigned char* kind = reinterpret_cast<const unsigned char*>(reinterpret_cast<char*>(s) + a.t.kind_off);
+    const int64_t sx = static_cast<int64_t>(ny) * nz;
 
-    // ---- tile + halo into shared memory; owned coefficients into the scratch copy -------------------
-    for (int e = warp; e < box_rows * box_cols; e += nwarps) {
-        const int li = e / box_cols - H, lj = e - (e / box_cols) * box_cols - H;
-        if (dist_of(li, lj) > H) continue;
-        const int gi = mirror(i0 + li, nx), gj = mirror(j0 + lj, ny);
-        const int box = (li + H) * bw + (lj + H);
-        const bool owned = li >= 0 && li < ai && lj >= 0 && lj < aj;
-        const int64_t base = gi * w.sx + static_cast<int64_t>(gj) * nz;
-        for (int k = lane; k < nz; k += 32) {
-            const int64_t idx = base + k;
-            s[(k & 1) * w.ncm + box * M + (k >> 1)] = a.field[idx];
-            if (owned) {
-                const wbc_sor_params& p = a.p;
-                const bool face = (p.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
-                                  (p.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
-                                  (p.bc_z == 0 && (k == 0 || k == nz - 1));
-                float v = -1.0f;
-                if (!face && !(a.fixed && a.fixed[idx] != 0)) v = a.density[idx] * p.uptake_max;
-                const int64_t at = ((static_cast<int64_t>(k & 1) * nx + gi) * ny + gj) * M + (k >> 1);
-                a.coeff[at] = v;
+    // ---- box into shared memory; owned coefficients (and production terms) into the copies -----------
+    for (int e = warp; e < rows * bw; e += nwarps) {
+        const unsigned char k = kind[e];
+        if (k == kNone) continue;
+        const int i = r.ia - 1 + e / bw, j = r.j0 - 1 + e % bw;
+        const int gi = mirror(i, nx), gj = mirror(j, ny);
+        const int p = (i + j) & 1;  // a ghost column has the parity of its mirror column
+        const int64_t base = gi * sx + static_cast<int64_t>(gj) * nz;
+        for (int kk = lane; kk < 2 * M; kk += 32) {
+            const int c = (p + kk) & 1;  // colour of node kk
+            const float v = kk < nz ? a.field[base + kk] : 0.0f;
+            s[c * w.plane + static_cast<int64_t>(e) * M + (kk >> 1)] = v;
+            if (k == kInner || k == kEdge) {
+                const wbc_sor_params& pp = a.p;
+                float u = -1.0f;
+                if (kk < nz) {
+                    const int64_t idx = base + kk;
+                    const bool face = (pp.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
+                                      (pp.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
+                                      (pp.bc_z == 0 && (kk == 0 || kk == nz - 1));
+                    if (!face && !(a.fixed && a.fixed[idx] != 0)) u = a.density[idx] * pp.uptake_max;
+                    if (!coefficient_in_range(u, w.K, w.h)) s_outside_range = 1;
+                }
+                const int64_t at = c * w.gplane + (static_cast<int64_t>(gi) * ny + gj) * M + (kk >> 1);
+                a.coeff[at] = u;
                 // The production term is fixed for the solve: computed once here (only where a node
                 // is updated, as the update itself would) instead of in every sweep.
-                if (HAS_PROD) a.pcopy[at] = v >= 0.0f ? prod_term(a, idx) : 0.0f;
-                if (!coefficient_in_range(v, w.K, w.h)) s_outside_range = 1;
+                if (HAS_PROD) a.pcopy[at] = u >= 0.0f ? prod_term(a, base + kk) : 0.0f;
+                // The edge columns start with tag 0 (half-sweeps are tagged from 1), so words a
+                // previous solve left in the buffer are never taken for this solve's.
+                if (k == kEdge) store_tagged(a.xchg + at, v, 0u);
             }
         }
     }
     unsigned int epoch = 0;
-    if (H == 1) {
-        // The edge rows start with tag 0 (half-sweeps are tagged from 1), so words a previous solve
-        // left in the buffer are never taken for this solve's.
-        __syncthreads();
-        unsigned long long* ll = reinterpret_cast<unsigned long long*>(a.xchg);
-        for (int q = warp; q < L.n_publish; q += nwarps) {
-            const int2 c = L.publish[q];
-            const int gi = c.y >> 16, gj = c.y & 0xffff;
-            for (int par = 0; par < 2; ++par) {
-                const int cnt = par ? w.cnt_odd : w.cnt_even;
-                for (int m = lane; m < cnt; m += 32)
-                    store_tagged(ll + ((static_cast<int64_t>(par) * nx + gi) * ny + gj) * M + m,
-                                 s[par * w.ncm + c.x * M + m], 0u);
-            }
-        }
-    }
-    // The ring columns' coefficients (and edge rows) are written by their owners: one global
-    // barrier first.
-    bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, nullptr, -1, claims, claims_needed);
+    // The halo columns' coefficients and edge words are written by their owners: one barrier first.
+    bool ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, claims, claims_needed);
     w.fast = s_outside_range == 0;  // read after the barrier's __syncthreads
 
     int sweeps = 0;
     float residual = __int_as_float(0x7f800000);
     bool converged = false;
     int chunk_index = 0;
-    unsigned int interval = 0;
     while (ok && sweeps < a.max_sweeps) {
         const int chunk = min(a.check_every, a.max_sweeps - sweeps);
-        int half_left = 2 * chunk;
-        int colour = 0;
-        while (ok && half_left > 0) {
-            if constexpr (H == 1) {
-                // Edge columns first, each new value also stored to the exchange buffer tagged
-                // with this half-sweep; then the inner columns; then the halo is read from the
-                // neighbours' tagged words. A neighbour rewrites a word two half-sweeps later, which
-                // needs this tile's words of the half-sweep in between, written after this pull.
-                const unsigned int tag = static_cast<unsigned int>(2 * sweeps + (2 * chunk - half_left) + 1);
-                relax_columns<HAS_PROD, LANES>(a, w, L.publish, L.n_publish, colour, warp, nwarps, lane, tag);
-                relax_columns<HAS_PROD, LANES>(a, w, L.inner, L.n_inner, colour, warp, nwarps, lane);
-                const bool fine = pull_tagged<LANES>(w, L.pull, L.n_pull, colour, tag, a.ctl, warp, nwarps, lane);
-                if (__syncthreads_or(!fine)) {
-                    if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
-                    ok = false;
-                    break;
-                }
-                if (L.n_mir > 0) {
-                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
-                    __syncthreads();
-                }
-                colour ^= 1;
-                half_left -= 1;
-            } else {
-                // H half-sweeps over shrinking regions (the halo columns relaxed redundantly), then
-                // one exchange of both parities through a double buffer.
-                const int nph = min(H, half_left);
-                for (int ph = 0; ph < nph; ++ph) {
-                    relax_columns<HAS_PROD, LANES>(a, w, L.upd, L.upd_end[nph - 1 - ph], colour, warp, nwarps, lane);
-                    __syncthreads();
-                    if (L.n_mir > 0) {
-                        mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, colour, false, warp, nwarps, lane);
-                        __syncthreads();
-                    }
-                    colour ^= 1;
-                }
-                half_left -= nph;
-                float* xb = a.xchg + static_cast<int64_t>(interval & 1u) * 2 * nx * ny * M;
-                copy_columns<LANES>(w, L.publish, L.n_publish, xb, 0, true, true, warp, nwarps, lane);
-                // A neighbour overwrites this buffer two exchanges later, i.e. only after this tile
-                // has signalled the next epoch, which comes after the pull below.
-                ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, s_neighbours, n_neighbours, claims,
-                                  claims_needed);
-                if (!ok) break;
-                copy_columns<LANES>(w, L.pull, L.n_pull, xb, 0, true, false, warp, nwarps, lane);
+        for (int half = 0; half < 2 * chunk; ++half) {
+            const int colour = half & 1;
+            const unsigned int tag = static_cast<unsigned int>(2 * sweeps + half + 1);
+            relax_colour<HAS_PROD, ZCLAMP>(a, w, colour, warp, nwarps, lane, tag);
+            const bool fine = pull_halo(a, w, colour, tag, warp, nwarps, lane);
+            if (__syncthreads_or(!fine)) {
+                if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
+                ok = false;
+                break;
+            }
+            if (w.n_mir > 0) {
+                mirror_columns(w, colour, warp, nwarps, lane);
                 __syncthreads();
-                if (L.n_mir > 0) {
-                    mirror_columns(w, L.mir, L.n_mir, bw, gi0, gj0, 0, true, warp, nwarps, lane);
-                    __syncthreads();
-                }
-                ++interval;
             }
         }
         if (!ok) break;
         sweeps += chunk;
-        __syncthreads();  // the halo warp may be ahead of the relaxing warps
         // Max-norm residual of the current field over every updated node (both colours).
         unsigned int bits = 0u;
-        const int n_owned = L.upd_end[0];
-        for (int q = warp; q < n_owned; q += nwarps) {
-            bits = max(bits, residual_column<HAS_PROD, LANES>(a, w, L.upd, q, 0, lane));
-            bits = max(bits, residual_column<HAS_PROD, LANES>(a, w, L.upd, q, 1, lane));
+        for (int q = warp; q < w.n_relax; q += nwarps) {
+            bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 0, lane));
+            bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 1, lane));
         }
 #pragma unroll
-        for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
+        for (int dd = 16; dd > 0; dd >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
         if (lane == 0) s_red[warp] = bits;
         __syncthreads();
         const int slot = chunk_index & 1;
         if (warp == 0) {
             bits = lane < nwarps ? s_red[lane] : 0u;
 #pragma unroll
-            for (int d = 16; d > 0; d >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, d));
+            for (int dd = 16; dd > 0; dd >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
             if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
         }
-        ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, nullptr, -1, claims, claims_needed);
+        ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, claims, claims_needed);
         if (!ok) break;
         residual = __uint_as_float(load_acquire(&a.ctl->res_bits[slot]));
         // The next chunk's slot was last read before this chunk's first barrier: safe to clear.
@@ -822,24 +737,27 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
         return;
     }
     // Owned columns back to the field.
-    const int n_owned = L.upd_end[0];
-    for (int q = warp; q < n_owned; q += nwarps) {
-        const int2 c = L.upd[q];
-        const int gi = c.y >> 16, gj = c.y & 0xffff;
-        float* out = a.field + gi * w.sx + static_cast<int64_t>(gj) * nz;
-        for (int k = lane; k < nz; k += 32) out[k] = s[(k & 1) * w.ncm + c.x * M + (k >> 1)];
+    for (int e = warp; e < rows * bw; e += nwarps) {
+        const unsigned char k = kind[e];
+        if (k != kInner && k != kEdge) continue;
+        const int i = r.ia - 1 + e / bw, j = r.j0 - 1 + e % bw;
+        const int p = (i + j) & 1;
+        float* out = a.field + i * sx + static_cast<int64_t>(j) * nz;
+        for (int kk = lane; kk < nz; kk += 32)
+            out[kk] = s[((p + kk) & 1) * w.plane + static_cast<int64_t>(e) * M + (kk >> 1)];
     }
     if (tile == 0 && threadIdx.x == 0) {
         a.ctl->sweeps = sweeps;
         a.ctl->residual = residual;
         a.ctl->converged = converged ? 1 : 0;
         a.ctl->status = 0;
+        if (a.residual_out) *a.residual_out = residual;
     }
 }
 
-template <bool HAS_PROD, int LANES, int H>
-__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1) k_sor_resident(SorArgs a) {
-    sor_tile<HAS_PROD, LANES, H>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
+template <bool HAS_PROD, bool ZCLAMP>
+__global__ void __launch_bounds__(kSorThreads, 1) k_sor_resident(SorArgs a) {
+    sor_tile<HAS_PROD, ZCLAMP>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
 }
 
 // The solver's grid barrier alone, for the self-test of the bounded waits: `ntiles` tiles are
@@ -873,8 +791,8 @@ __device__ __forceinline__ int find_batch_item(const int32_t* first, int n, int 
     return lo;
 }
 
-template <bool HAS_PROD, int LANES>
-__global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1)
+template <bool HAS_PROD, bool ZCLAMP>
+__global__ void __launch_bounds__(kSorThreads, 1)
     k_sor_batched(const SorArgs* __restrict__ args, const int32_t* __restrict__ tile_first, int n,
                   unsigned int* __restrict__ next_tile) {
     __shared__ int s_tile;
@@ -886,8 +804,8 @@ __global__ void __launch_bounds__(max_threads_for_lanes(LANES), 1)
         const int t = s_tile;
         if (t >= total) return;
         const int b = find_batch_item(tile_first, n, t);
-        sor_tile<HAS_PROD, LANES, 1>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
-                                     static_cast<unsigned int>(tile_first[b + 1]));
+        sor_tile<HAS_PROD, ZCLAMP>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
+                                   static_cast<unsigned int>(tile_first[b + 1]));
     }
 }
 
@@ -907,29 +825,9 @@ __global__ void k_sor_batch_reset(const SorArgs* __restrict__ args, const int32_
 // ---- host side -------------------------------------------------------------------------------------------
 using KernelFn = void (*)(SorArgs);
 
-template <bool P, int Hd>
-static KernelFn kernel_for_lanes(int lanes) {
-    switch (lanes) {
-        case 1: return k_sor_resident<P, 1, Hd>;
-        case 2: return k_sor_resident<P, 2, Hd>;
-        case 3: return k_sor_resident<P, 3, Hd>;
-        case 4: return k_sor_resident<P, 4, Hd>;
-        case 5: return k_sor_resident<P, 5, Hd>;
-        case 6: return k_sor_resident<P, 6, Hd>;
-        case 7: return k_sor_resident<P, 7, Hd>;
-        default: return k_sor_resident<P, 8, Hd>;
-    }
-}
-
-static KernelFn kernel_for(bool has_prod, int lanes, int H) {
-    if (has_prod) {
-        if (H == 1) return kernel_for_lanes<true, 1>(lanes);
-        if (H == 2) return kernel_for_lanes<true, 2>(lanes);
-        return kernel_for_lanes<true, 4>(lanes);
-    }
-    if (H == 1) return kernel_for_lanes<false, 1>(lanes);
-    if (H == 2) return kernel_for_lanes<false, 2>(lanes);
-    return kernel_for_lanes<false, 4>(lanes);
+static KernelFn kernel_for(bool has_prod, bool zclamp) {
+    if (has_prod) return zclamp ? k_sor_resident<true, true> : k_sor_resident<true, false>;
+    return zclamp ? k_sor_resident<false, true> : k_sor_resident<false, false>;
 }
 
 struct DeviceInfo {
@@ -955,104 +853,116 @@ static DeviceInfo device_info() {
     return d;
 }
 
-static bool tiling_for(const wbc_sor_params& p, int tx, int ty, int H, size_t smem_limit, SorTiling* out) {
-    const int entries = (p.nz + 1) / 2;
-    const int M = (entries + 3) & ~3;
-    const int lanes = (entries + 31) / 32;
-    const int ti = (p.nx + tx - 1) / tx, tj = (p.ny + ty - 1) / ty;
-    if (ti < H || tj < H || ti < 2 || tj < 2) return false;
-    const int ex = (p.nx + ti - 1) / ti, ey = (p.ny + tj - 1) / tj;
-    const int nbox = (ti + 2 * H) * (tj + 2 * H);
-    const size_t planes = ((2ull * nbox * M * sizeof(float)) + 15) & ~15ull;
-    const size_t lists = 5ull * nbox * sizeof(int2) + 16 * sizeof(int);
-    const size_t table = (planes + lists + 15) & ~15ull;
-    const size_t smem = table + 2ull * nbox * sizeof(int4);
-    if (smem > smem_limit) return false;
-    if (2ll * p.nx * p.ny * M >= (1ll << 31)) return false;  // coefficient offsets are 32-bit
-    const int warps = std::min(max_threads_for_lanes(lanes) / 32, std::max(1, ti * tj));
-    *out = SorTiling{ex, ey, ti, tj, M, lanes, 32 * warps, H, nbox, planes, table, smem};
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// The shared-memory layout for `tiles` tiles cut from `strips` strips; false if that partition is
+// not valid for the grid (an empty strip or tile) or the largest tile does not fit in smem_limit.
+// `score` (may be NULL): the largest tile's columns, then its bounding box, for choosing among
+// partitions.
+static bool tiling_for(const wbc_sor_params& p, int tiles, int strips, size_t smem_limit, SorTiling* out,
+                       long* score = nullptr) {
+    if (tiles < 1 || tiles > kMaxCtas || strips < 1 || strips > p.ny || strips > tiles) return false;
+    const int M = (p.nz + 1) / 2;
+    if (M > kMaxEntries || p.nx > 32767 || p.ny > 32767) return false;
+    if (static_cast<int64_t>(p.nx) * p.ny * M >= (1ll << 31) - 64) return false;  // 32-bit chunk offsets
+    for (int s = 0; s < strips; ++s) {
+        const int w = strip_start(s + 1, strips, p.ny) - strip_start(s, strips, p.ny);
+        const int tn = tiles_before(s + 1, strips, p.ny, tiles) - tiles_before(s, strips, p.ny, tiles);
+        if (w < 1 || tn < 1 || static_cast<int64_t>(tn) > static_cast<int64_t>(p.nx) * w) return false;
+    }
+    int max_box = 0, max_rows = 0, max_owned = 0, max_perimeter = 0;
+    for (int t = 0; t < tiles; ++t) {
+        const TileRect r = tile_rect(t, tiles, strips, p.nx, p.ny);
+        const int rows = r.ib - r.ia + 3, bw = r.j1 - r.j0 + 2;
+        const int owned = (r.ib - r.ia + 1) * (r.j1 - r.j0) - (r.ja - r.j0) - (r.j1 - r.jb);
+        max_box = std::max(max_box, rows * bw);
+        max_rows = std::max(max_rows, rows);
+        max_owned = std::max(max_owned, owned);
+        max_perimeter = std::max(max_perimeter, 2 * (rows + bw));
+    }
+    SorTiling t{};
+    t.tiles = tiles;
+    t.strips = strips;
+    t.M = M;
+    t.max_box = max_box;
+    // Groups: a run of len owned columns has ceil(len M / kGroup); every row of a tile has at most
+    // five runs of owned columns (edge / inner / edge, and the staircase). Pull chunks: the halo
+    // columns lie on the bounding box's perimeter, ceil(len M / 32) per run.
+    t.relax_cap = (max_owned * M + kGroup - 1) / kGroup + 6 * max_rows + 8;
+    t.pull_cap = (max_perimeter * M + 31) / 32 + max_perimeter + 8;
+    t.mirror_cap = max_perimeter + 8;
+    t.run_cap = max_box + 8;
+    t.plane_floats = align_up(static_cast<size_t>(max_box) * M + kPlaneSlack, 32);
+    t.relax_off = align_up(2 * t.plane_floats * sizeof(float), 16);
+    t.masks_off = align_up(t.relax_off + static_cast<size_t>(t.relax_cap) * sizeof(int4), 16);
+    t.pull_off = align_up(t.masks_off + static_cast<size_t>(t.relax_cap) * sizeof(uint4), 16);
+    t.run_off = align_up(t.pull_off + static_cast<size_t>(t.pull_cap) * sizeof(int4), 16);
+    t.mirror_off = align_up(t.run_off + static_cast<size_t>(t.run_cap) * sizeof(int4), 16);
+    t.kind_off = align_up(t.mirror_off + static_cast<size_t>(t.mirror_cap) * sizeof(int2), 16);
+    t.smem = align_up(t.kind_off + static_cast<size_t>(max_box), 16);
+    if (t.smem > smem_limit) return false;
+    *out = t;
+    if (score) *score = static_cast<long>(max_owned) * 100000 + max_box;
     return true;
 }
 
-// tx x ty tiles, at most one CTA per SM (and within the barrier flags), minimising the columns of
-// the largest tile, then the halo perimeter.
-static bool choose_tiling(const wbc_sor_params& p, int sms, size_t smem_limit, int H, int want_tx, int want_ty,
-                          SorTiling* out) {
-    const int entries = (p.nz + 1) / 2;
-    if (entries > 32 * kMaxLanesPerColumn || p.nx > 32767 || p.ny > 32767) return false;
-    const int max_ctas = std::min(sms, kMaxCtas);
-    if (want_tx > 0 && want_ty > 0) return want_tx * want_ty <= max_ctas && tiling_for(p, want_tx, want_ty, H, smem_limit, out);
+// `tiles` tiles (at most one CTA per SM and within the barrier flags); the strip count with the
+// smallest largest tile, then the smallest bounding box, unless `want_strips` fixes it.
+static bool choose_tiling(const wbc_sor_params& p, int tiles, size_t smem_limit, int want_strips, SorTiling* out) {
+    tiles = std::min({tiles, kMaxCtas, p.nx * p.ny});
+    if (tiles < 1) return false;
+    if (want_strips > 0) return tiling_for(p, tiles, want_strips, smem_limit, out);
     bool found = false;
-    long best_score = 0;
-    for (int tx = 1; tx <= std::min(p.nx, max_ctas); ++tx) {
-        const int ty_max = std::min(p.ny, max_ctas / tx);
-        for (int ty = 1; ty <= ty_max; ++ty) {
-            SorTiling t{};
-            if (!tiling_for(p, tx, ty, H, smem_limit, &t)) continue;
-            const long score = static_cast<long>(t.ti) * t.tj * 1000 + (t.ti + t.tj);
-            if (!found || score < best_score) {
-                found = true;
-                best_score = score;
-                *out = t;
-            }
+    long best = 0;
+    for (int strips = 1; strips <= std::min(p.ny, tiles); ++strips) {
+        SorTiling t{};
+        long score = 0;
+        if (!tiling_for(p, tiles, strips, smem_limit, &t, &score)) continue;
+        if (!found || score < best) {
+            found = true;
+            best = score;
+            *out = t;
         }
     }
     return found;
 }
 
-static size_t plane_bytes(const wbc_sor_params& p) {
-    return 2ull * p.nx * p.ny * ((((p.nz + 1) / 2) + 3) & ~3) * sizeof(float);
+static size_t plane_bytes(const wbc_sor_params& p, size_t element) {
+    return 2ull * p.nx * p.ny * ((p.nz + 1) / 2) * element;
 }
 
-static size_t header_bytes() { return sizeof(SorControl) + kMaxCtas * sizeof(unsigned int); }
+static size_t header_bytes() { return align_up(sizeof(SorControl) + kMaxCtas * sizeof(unsigned int), 256); }
 
-// [control block + barrier flags][exchange: 2 planes][coefficient copy][production copy]
-size_t sor_workspace_bytes(const wbc_sor_params& p) { return header_bytes() + 4 * plane_bytes(p) + 256; }
+// [control block + barrier flags][tagged exchange words][coefficient copy][production copy]
+size_t sor_workspace_bytes(const wbc_sor_params& p) {
+    return header_bytes() + align_up(plane_bytes(p, 8), 256) + 2 * align_up(plane_bytes(p, 4), 256) + 256;
+}
+
+static void place_workspace(const wbc_sor_params& p, void* workspace, SorArgs* a) {
+    char* base = static_cast<char*>(workspace);
+    a->ctl = reinterpret_cast<SorControl*>(base);
+    a->flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
+    size_t off = header_bytes();
+    a->xchg = reinterpret_cast<unsigned long long*>(base + off);
+    off += align_up(plane_bytes(p, 8), 256);
+    a->coeff = reinterpret_cast<float*>(base + off);
+    off += align_up(plane_bytes(p, 4), 256);
+    a->pcopy = reinterpret_cast<float*>(base + off);
+}
 
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
-                       float* field, wbc_sor_report* report, void* workspace, const wbc_sor_tuning* tuning,
-                       cudaStream_t stream, bool* feasible) {
+                       float* field, float* residual_out, wbc_sor_report* report, void* workspace,
+                       const wbc_sor_tuning* tuning, cudaStream_t stream, bool* feasible) {
     const DeviceInfo dev = device_info();
-    const size_t reserve = 1024;  // static shared memory of the kernel
-    const size_t limit = static_cast<size_t>(dev.smem_optin) - reserve;
+    const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;  // static shared memory of the kernel
     SorTiling t{};
-    int H = tuning && tuning->halo_depth > 0 ? tuning->halo_depth : 0;
-    const int want_tx = tuning ? tuning->tiles_i : 0, want_ty = tuning ? tuning->tiles_j : 0;
-    if (H != 0 && H != 1 && H != 2 && H != 4) {
-        set_error_msg("wbc_sor_solve: halo_depth must be 1, 2 or 4");
-        return WBC_ERR_INVALID;
-    }
-    *feasible = false;
-    if (dev.sms > 0) {
-        if (H != 0) {
-            *feasible = choose_tiling(p, dev.sms, limit, H, want_tx, want_ty, &t);
-        } else {
-            // Default: a one-column halo, exchanged while the inner columns are relaxed, when
-            // the tiles have inner columns to hide it behind; otherwise the deepest halo that fits
-            // (fewer exchanges for small grids, where the exchange latency dominates).
-            SorTiling t1{};
-            const bool f1 = choose_tiling(p, dev.sms, limit, 1, want_tx, want_ty, &t1);
-            if (f1 && std::min(t1.ti, t1.tj) >= 4) {
-                t = t1;
-                *feasible = true;
-            } else {
-                for (int depth : {4, 2}) {
-                    if (choose_tiling(p, dev.sms, limit, depth, want_tx, want_ty, &t)) {
-                        *feasible = true;
-                        break;
-                    }
-                }
-                if (!*feasible && f1) {
-                    t = t1;
-                    *feasible = true;
-                }
-            }
-        }
-    }
+    const int want_tiles = tuning && tuning->tiles > 0 ? tuning->tiles : dev.sms;
+    const int want_strips = tuning ? tuning->strips : 0;
+    *feasible = dev.sms > 0 && want_tiles <= dev.sms && choose_tiling(p, want_tiles, limit, want_strips, &t);
     if (!*feasible) return WBC_OK;
     const bool has_prod = production != nullptr || p.has_source;
-    KernelFn fn = kernel_for(has_prod, t.lanes, t.H);
+    KernelFn fn = kernel_for(has_prod, p.bc_z != 0);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem));
     if (err != cudaSuccess) {
@@ -1060,27 +970,32 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
         return WBC_ERR_CUDA;
     }
     int per_sm = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.threads, t.smem);
-    if (err != cudaSuccess || per_sm < 1 || t.tx * t.ty > per_sm * dev.sms) {
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSorThreads, t.smem);
+    if (err != cudaSuccess || per_sm < 1 || t.tiles > per_sm * dev.sms) {
         cudaGetLastError();
         *feasible = false;
         return WBC_OK;
     }
-    char* base = reinterpret_cast<char*>(workspace);
-    auto* ctl = reinterpret_cast<SorControl*>(base);
-    auto* flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
-    float* xchg = reinterpret_cast<float*>(base + header_bytes());
-    float* coeff = reinterpret_cast<float*>(base + header_bytes() + 2 * plane_bytes(p));
-    err = cudaMemsetAsync(base, 0, header_bytes(), stream);
+    SorArgs args{};
+    args.p = p;
+    args.t = t;
+    args.fixed = fixed;
+    args.density = density;
+    args.production = production;
+    args.source = source;
+    args.field = field;
+    args.residual_out = residual_out;
+    args.check_every = check_every;
+    args.max_sweeps = max_sweeps;
+    args.tolerance = tolerance;
+    place_workspace(p, workspace, &args);
+    err = cudaMemsetAsync(workspace, 0, header_bytes(), stream);
     if (err != cudaSuccess) {
         set_error("wbc_sor_solve: cudaMemsetAsync", err);
         return WBC_ERR_CUDA;
     }
-    SorArgs args{p,    t,     fixed, density, production, source,      field,
-                 xchg, coeff, ctl,   flags,   check_every, max_sweeps, tolerance};
-    args.pcopy = reinterpret_cast<float*>(base + header_bytes() + 3 * plane_bytes(p));
     void* params[] = {&args};
-    err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(t.tx * t.ty), dim3(t.threads), params,
+    err = cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(fn), dim3(t.tiles), dim3(kSorThreads), params,
                                       t.smem, stream);
     if (err != cudaSuccess) {
         set_error("wbc_sor_solve: cudaLaunchCooperativeKernel", err);
@@ -1089,71 +1004,45 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     int rc = check_launch("wbc_sor_solve", 1);
     if (rc != WBC_OK) return rc;
     SorControl host{};
-    err = cudaMemcpyAsync(&host, ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, stream);
+    err = cudaMemcpyAsync(&host, args.ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
     if (err != cudaSuccess) {
         set_error("wbc_sor_solve: reading the report", err);
         return WBC_ERR_CUDA;
     }
     if (host.status != 0) {
-        set_error_msg("wbc_sor_solve: grid barrier timed out");
+        set_error_msg("wbc_sor_solve: a device wait timed out");
         return WBC_ERR_TIMEOUT;
     }
     report->sweeps = host.sweeps;
     report->residual = host.residual;
     report->converged = host.converged;
     report->path = 2;
-    report->tiles = t.tx * t.ty;
-    report->halo_depth = t.H;
-    report->tiles_i = t.tx;
-    report->tiles_j = t.ty;
+    report->tiles = t.tiles;
+    report->strips = t.strips;
     return WBC_OK;
 }
 
-// Candidate tunings for the autotuner: per halo depth, the tile grid with the fewest columns per
-// tile, its transpose, and the squarest grid within the SM count.
+// Candidate tunings for the autotuner: every SM, and the strip counts around the one with the
+// smallest largest tile and bounding box.
 static std::vector<wbc_sor_tuning> tuning_candidates(const wbc_sor_params& p, int sms, size_t limit) {
     std::vector<wbc_sor_tuning> out;
-    auto add = [&](int H, int want_tx, int want_ty) {
+    SorTiling best{};
+    if (!choose_tiling(p, sms, limit, 0, &best)) return out;
+    for (int strips : {best.strips, best.strips - 1, best.strips + 1, best.strips - 2, best.strips + 2}) {
         SorTiling t{};
-        if (!choose_tiling(p, sms, limit, H, want_tx, want_ty, &t)) return;
-        for (const wbc_sor_tuning& c : out)
-            if (c.halo_depth == H && c.tiles_i == t.tx && c.tiles_j == t.ty) return;
-        out.push_back(wbc_sor_tuning{H, t.tx, t.ty});
-    };
-    int q = 1;
-    while ((q + 1) * (q + 1) <= std::min(sms, kMaxCtas)) ++q;
-    for (int H : {1, 2, 4}) {
-        SorTiling t{};
-        if (!choose_tiling(p, sms, limit, H, 0, 0, &t)) continue;
-        add(H, t.tx, t.ty);
-        add(H, t.ty, t.tx);
-        add(H, q, q);
+        if (strips >= 1 && tiling_for(p, best.tiles, strips, limit, &t))
+            out.push_back(wbc_sor_tuning{t.tiles, t.strips});
     }
     return out;
 }
 
-}  // namespace wbc
-
-using namespace wbc;
-
 // ---- batched solves: host side -------------------------------------------------------------------------
-namespace wbc {
-
 using BatchedFn = void (*)(const SorArgs*, const int32_t*, int, unsigned int*);
 
-template <bool P>
-static BatchedFn batched_for_lanes(int lanes) {
-    switch (lanes) {
-        case 1: return k_sor_batched<P, 1>;
-        case 2: return k_sor_batched<P, 2>;
-        case 3: return k_sor_batched<P, 3>;
-        case 4: return k_sor_batched<P, 4>;
-        case 5: return k_sor_batched<P, 5>;
-        case 6: return k_sor_batched<P, 6>;
-        case 7: return k_sor_batched<P, 7>;
-        default: return k_sor_batched<P, 8>;
-    }
+static BatchedFn batched_for(bool has_prod, bool zclamp) {
+    if (has_prod) return zclamp ? k_sor_batched<true, true> : k_sor_batched<true, false>;
+    return zclamp ? k_sor_batched<false, true> : k_sor_batched<false, false>;
 }
 
 struct SorBatchLayout {
@@ -1173,6 +1062,8 @@ static SorBatchLayout sor_batch_layout(int n) {
 
 }  // namespace wbc
 
+using namespace wbc;
+
 extern "C" {
 
 size_t wbc_sor_batch_plan_bytes(int32_t n) { return n > 0 ? sor_batch_layout(n).bytes : 0; }
@@ -1191,10 +1082,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     const int G = std::min(dev.sms, kMaxCtas);
     const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;
     // Expected work per item: the caller's weight (e.g. nodes x sweeps of the previous solve), or
-    // its node count. Items go on the work list heaviest first, each with CTAs in proportion to
-    // its work (three times its share of the GPU: the grids rarely all fit in shared memory at
-    // once, and smaller tiles shorten the heaviest solves, which bound the launch), raised until
-    // its tiles fit in shared memory.
+    // its node count.
     std::vector<double> work(n);
     double total_work = 0.0;
     for (int b = 0; b < n; ++b) {
@@ -1215,8 +1103,9 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     // can be tiled with floor(G x its share of the wave's work) CTAs in shared memory and the
     // wave's tiles fit on the GPU at once; then a new wave starts. A wave's items start together
     // and, their CTAs being proportional to their work, end together, so the next wave's tiles are
-    // claimed when a whole wave of CTAs frees up. If some item cannot be tiled that way, the
-    // proportional plan below is used instead.
+    // claimed when a whole wave of CTAs frees up. If some item cannot be tiled that way, each item
+    // gets CTAs in proportion to three times its share of all the work instead, raised until its
+    // tiles fit in shared memory.
     std::vector<SorTiling> tiling(n);
     bool waves = true;
     {
@@ -1228,8 +1117,8 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
                 const int b = order[k];
                 const int share = std::max(1, static_cast<int>(G * work[b] / w));
                 SorTiling t{};
-                if (!choose_tiling(items[b].params, share, limit, 1, 0, 0, &t)) return false;
-                tiles += t.tx * t.ty;
+                if (!choose_tiling(items[b].params, share, limit, 0, &t)) return false;
+                tiles += t.tiles;
                 if (commit) tiling[k] = t;
             }
             return tiles <= G;
@@ -1248,8 +1137,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     }
     std::vector<SorArgs> args(n);
     std::vector<int32_t> first(n + 1, 0);
-    int lanes = 1, threads = 32;
-    bool has_prod = false;
+    bool has_prod = false, zclamp = false;
     size_t smem = 0;
     for (int k = 0; k < n; ++k) {
         const int b = order[k];
@@ -1259,13 +1147,12 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
         if (!waves) {
             int share = std::min(G, std::max(1, static_cast<int>(3.0 * G * work[b] / total_work + 0.5)));
             bool fits = false;
-            for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 1, 0, 0, &t);
+            for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 0, &t);
             if (!fits) {
                 set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
                 return WBC_ERR_INVALID;
             }
         }
-        char* base = static_cast<char*>(it.workspace);
         SorArgs& a = args[k];
         a.p = p;
         a.t = t;
@@ -1274,26 +1161,21 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
         a.production = it.production;
         a.source = it.source;
         a.field = it.field;
-        a.xchg = reinterpret_cast<float*>(base + header_bytes());
-        a.coeff = reinterpret_cast<float*>(base + header_bytes() + 2 * plane_bytes(p));
-        a.pcopy = reinterpret_cast<float*>(base + header_bytes() + 3 * plane_bytes(p));
-        a.ctl = reinterpret_cast<SorControl*>(base);
-        a.flags = reinterpret_cast<unsigned int*>(base + sizeof(SorControl));
+        a.residual_out = nullptr;
         a.check_every = check_every;
         a.max_sweeps = max_sweeps;
         a.tolerance = tolerance;
-        first[k + 1] = first[k] + t.tx * t.ty;
-        lanes = std::max(lanes, t.lanes);
-        threads = std::max(threads, t.threads);
+        place_workspace(p, it.workspace, &a);
+        first[k + 1] = first[k] + t.tiles;
         smem = std::max(smem, t.smem);
         has_prod = has_prod || it.production != nullptr || p.has_source;
+        zclamp = zclamp || p.bc_z != 0;
     }
-    threads = std::min(threads, max_threads_for_lanes(lanes));
-    BatchedFn fn = has_prod ? batched_for_lanes<true>(lanes) : batched_for_lanes<false>(lanes);
+    BatchedFn fn = batched_for(has_prod, zclamp);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     int per_sm = 0;
-    if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    if (err == cudaSuccess) err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kSorThreads, smem);
     if (err != cudaSuccess || per_sm < 1) {
         cudaGetLastError();
         set_error_msg("wbc_sor_batch_prepare: the batched solver does not fit on an SM");
@@ -1314,8 +1196,8 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     out->items = n;
     out->total_tiles = first[n];
     out->ctas = ctas;
-    out->threads = threads;
-    out->lanes = lanes;
+    out->threads = kSorThreads;
+    out->zclamp = zclamp ? 1 : 0;
     out->has_prod = has_prod ? 1 : 0;
     out->smem_bytes = static_cast<int64_t>(smem);
     out->device_plan = plan;
@@ -1331,10 +1213,10 @@ int wbc_sor_batch_solve(const wbc_sor_batch* b, void* stream) {
     unsigned int* next = reinterpret_cast<unsigned int*>(base + L.next);
     cudaStream_t s = as_stream(stream);
     k_sor_batch_reset<<<std::min(b->items, 1024), 128, 0, s>>>(args, first, b->items, next);
-    BatchedFn fn = b->has_prod ? batched_for_lanes<true>(b->lanes) : batched_for_lanes<false>(b->lanes);
+    BatchedFn fn = batched_for(b->has_prod != 0, b->zclamp != 0);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(b->ctas);
-    cfg.blockDim = dim3(b->threads);
+    cfg.blockDim = dim3(kSorThreads);
     cfg.dynamicSmemBytes = static_cast<size_t>(b->smem_bytes);
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -1380,18 +1262,12 @@ int wbc_sor_batch_reports(const wbc_sor_batch* b, wbc_sor_report* reports, void*
         r.converged = ctl[k].converged;
         r.path = 2;
         r.tiles = first[k + 1] - first[k];
-        r.halo_depth = 1;
-        r.tiles_i = args[k].t.tx;
-        r.tiles_j = args[k].t.ty;
+        r.strips = args[k].t.strips;
         if (ctl[k].status != 0) rc = WBC_ERR_TIMEOUT;
     }
     if (rc != WBC_OK) set_error_msg("wbc_sor_batch_reports: a solve timed out");
     return rc;
 }
-
-}  // extern "C"
-
-extern "C" {
 
 size_t wbc_sor_solve_workspace_bytes(const wbc_sor_params* p) {
     if (!p) return 0;
@@ -1410,7 +1286,7 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
         set_error_msg("wbc_sor_autotune: the workspace must be 16-byte aligned");
         return WBC_ERR_INVALID;
     }
-    *best = wbc_sor_tuning{0, 0, 0};
+    *best = wbc_sor_tuning{0, 0};
     if (best_us_per_sweep) *best_us_per_sweep = 0.0f;
     const DeviceInfo dev = device_info();
     if (dev.sms <= 0) return WBC_OK;
@@ -1443,7 +1319,7 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
             bool feasible = false;
             // A negative tolerance never converges: every candidate runs the same sweeps.
             rc = sor_solve_resident(*p, check_every, sweeps, -1.0, fixed, density, production, source, scratch_field,
-                                    &r, workspace, &cands[c], s, &feasible);
+                                    nullptr, &r, workspace, &cands[c], s, &feasible);
             if (rc != WBC_OK) break;
             err = cudaEventRecord(e1, s);
             if (err == cudaSuccess) err = cudaEventSynchronize(e1);
@@ -1506,8 +1382,8 @@ int wbc_sor_wait_selftest(int32_t ctas, int32_t missing, int32_t rounds, void* w
 
 int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
                   const int32_t* fixed, const float* density, const float* production, const float* source,
-                  float* field, wbc_sor_report* report, void* workspace, size_t workspace_bytes, int32_t path,
-                  const wbc_sor_tuning* tuning, void* stream) {
+                  float* field, float* residual_out, wbc_sor_report* report, void* workspace,
+                  size_t workspace_bytes, int32_t path, const wbc_sor_tuning* tuning, void* stream) {
     if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || check_every < 1 || max_sweeps < 1 || !density || !field ||
         !report || !workspace || (p->has_source && !source) || path < 0 || path > 2)
         return WBC_ERR_INVALID;
@@ -1520,7 +1396,7 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
     bool feasible = false;
     if (path != 1) {
         int rc = sor_solve_resident(*p, check_every, max_sweeps, tolerance, fixed, density, production, source, field,
-                                    report, workspace, tuning, s, &feasible);
+                                    residual_out, report, workspace, tuning, s, &feasible);
         if (rc != WBC_OK || feasible) return rc;
         if (path == 2) {
             set_error_msg("wbc_sor_solve: the grid does not fit the shared-memory resident solver");
@@ -1544,14 +1420,19 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
         }
         if (static_cast<double>(residual) < tolerance) break;
     }
+    if (residual_out) {
+        cudaError_t err = cudaMemcpyAsync(residual_out, residual_dev, sizeof(float), cudaMemcpyDeviceToDevice, s);
+        if (err != cudaSuccess) {
+            set_error("wbc_sor_solve: writing the residual", err);
+            return WBC_ERR_CUDA;
+        }
+    }
     report->sweeps = sweeps;
     report->residual = residual;
     report->converged = static_cast<double>(residual) < tolerance ? 1 : 0;
     report->path = 1;
     report->tiles = 0;
-    report->halo_depth = 0;
-    report->tiles_i = 0;
-    report->tiles_j = 0;
+    report->strips = 0;
     return WBC_OK;
 }
 

@@ -104,6 +104,8 @@ def solve_steady_state(
     ``production`` [conc/h] is an optional zero-order source per node, scaled by
     ``S/(source_k + S)`` of the ``source`` field when one is given.
     """
+    if residual_buffer.dtype != torch.float32 or residual_buffer.device != field.device or residual_buffer.numel() < 1:
+        raise ValueError("residual_buffer must be a float32 tensor of at least one element on the field's device")
     prod, has_source, src, source_k = _source_args(field, production, source, source_k)
     params = sor_params(field, kinetics, settings.omega, has_source, source_k)
     workspace = _workspace(field, params)
@@ -114,27 +116,26 @@ def solve_steady_state(
         tuning = _autotuned(field, params, settings, density, prod, src, workspace)
     else:
         tuning = None
+    # The library writes the final residual into residual_buffer[0] itself (no extra kernel).
     with profiling.stage("sor"):
         _lib.call("wbc_sor_solve", ctypes.byref(params), int(settings.check_every), int(settings.max_sweeps),
                   float(settings.tolerance), _lib.ptr(field.fixed_or_none()), _lib.ptr(density), _lib.ptr(prod),
-                  _lib.ptr(src), _lib.ptr(field.values), ctypes.byref(report), _lib.ptr(workspace),
-                  workspace.numel(), int(solver_path), ctypes.byref(tuning) if tuning is not None else None,
-                  _lib.stream(field.device))
-    residual_buffer.fill_(float(report.residual))
-    last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles, halo_depth=report.halo_depth,
-                      tiles_i=report.tiles_i, tiles_j=report.tiles_j)
+                  _lib.ptr(src), _lib.ptr(field.values), _lib.ptr(residual_buffer), ctypes.byref(report),
+                  _lib.ptr(workspace), workspace.numel(), int(solver_path),
+                  ctypes.byref(tuning) if tuning is not None else None, _lib.stream(field.device))
+    last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles, strips=report.strips)
     return SolveReport(sweeps=int(report.sweeps), residual=float(report.residual), converged=bool(report.converged))
 
 
 # 0: the shared-memory resident solver when the grid fits on chip, else streaming colour launches;
 # 1: streaming colour launches only; 2: resident only (an error if the grid does not fit).
 solver_path = 0
-# (halo_depth, tiles_i, tiles_j) for the resident solver: None = measured by the autotuner on the
+# (tiles, strips) for the resident solver: None = measured by the autotuner on the
 # first solve of each grid configuration; zeros = the library's built-in choice.
-solver_tuning: tuple[int, int, int] | None = None
+solver_tuning: tuple[int, int] | None = None
 # sweeps / path / CTA count of the most recent solve (for benchmarks and tests)
 last_solve: dict = {}
-# autotuner results: key -> (halo_depth, tiles_i, tiles_j, us_per_sweep)
+# autotuner results: key -> (tiles, strips, us_per_sweep)
 autotune_cache: dict = {}
 
 
@@ -154,9 +155,9 @@ def _autotuned(field: ScalarField, params: _lib.SorParamsC, settings: SolverSett
                   _lib.ptr(density), _lib.ptr(prod), _lib.ptr(src), _lib.ptr(field.values), _lib.ptr(scratch),
                   _lib.ptr(workspace), workspace.numel(), ctypes.byref(best), ctypes.byref(us),
                   _lib.stream(field.device))
-        hit = (int(best.halo_depth), int(best.tiles_i), int(best.tiles_j), float(us.value))
+        hit = (int(best.tiles), int(best.strips), float(us.value))
         autotune_cache[key] = hit
-    return _lib.SorTuningC(*hit[:3])
+    return _lib.SorTuningC(*hit[:2])
 
 
 def _workspace(field: ScalarField, params: _lib.SorParamsC) -> torch.Tensor:
