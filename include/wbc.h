@@ -197,6 +197,17 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
                   const int32_t* fixed, const float* density, const float* production, const float* source,
                   float* field, float* residual_out, wbc_sor_report* report, void* workspace,
                   size_t workspace_bytes, int32_t path, const wbc_sor_tuning* tuning, void* stream);
+/* The linear system d_a x_a - sum_nb x_nb = b_a (d_a > 0; nodes with d_a <= 0 and Dirichlet faces
+ * keep their values in x) by red-black SOR with relaxation p->omega in the same resident
+ * launch as wbc_sor_solve, from x's current values, checking every `check_every` sweeps whether
+ * max_a |b_a + sum_nb x_nb - d_a x_a| < tolerance * max_a max(6 |x_a|, |b_a|). Only nx, ny, nz,
+ * the boundary flags and omega of `p` are read. Used by the hand-written adjoint (the transposed
+ * linearised field operator) and by its Newton correction of the forward steady state; no
+ * counterpart in the reference. Synchronises `stream`; WBC_ERR_INVALID if the grid does not fit
+ * the resident solver. */
+int wbc_sor_linear_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
+                         const float* diag, const float* rhs, float* x, wbc_sor_report* report, void* workspace,
+                         size_t workspace_bytes, void* stream);
 /* Self-test of the solver's bounded device waits (no counterpart in the reference): runs the grid
  * barrier of the resident solver `rounds` times on `ctas` expected CTAs, of which `ctas - missing`
  * are launched (cooperatively, one small CTA each; ctas <= the SM count). With missing = 0 the
@@ -384,6 +395,51 @@ int wbc_adjoint_contact(const wbc_neighbor_grid* grid, int32_t n, float query_ra
 int wbc_adjoint_field_solve(const wbc_sor_params* p, const float* u, const float* U, const float* grad_u, float* mu,
                             float* kappa, int32_t check_every, int32_t max_sweeps, float tolerance, float* phi,
                             double* sums, uint32_t* residual_bits, wbc_sor_report* report, void* stream);
+/* `steps` contact steps (each wbc_grid_build + wbc_contact_substep, same bits) in one cooperative
+ * launch whose phases are separated by bounded grid barriers; `grid` supplies dim, cell_size and
+ * the per-cell scratch (cell_bucket, cell_rank, scatter), the workspace
+ * (wbc_contact_steps_workspace_bytes(dim, capacity, slots), 256-byte aligned) holds the grids.
+ * checkpoints (NULL or float[steps / every + 1][n][3]) receives x_t before step t for t % every
+ * == 0. history = 1 builds step t's grid into workspace slot t (steps <= slots) for
+ * wbc_adjoint_steps; last_build_only = 1 builds the last step's grid without moving the cells.
+ * position_lo (NULL or float[n][3], with checkpoints_lo beside checkpoints) makes the positions
+ * compensated, position + position_lo: pair differences include the low parts and the Euler step
+ * is an exact two-sum, so the trajectory keeps about 48 bits (forces stay in float).
+ * sync_status = 1 synchronises `stream` and returns WBC_ERR_TIMEOUT if a barrier timed out. The
+ * adjoint model's forward steps and its checkpoint-segment recomputation; no counterpart in the
+ * reference. */
+size_t wbc_contact_steps_workspace_bytes(int32_t dim, int64_t capacity, int32_t slots);
+int wbc_contact_steps(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                      int32_t steps, float* position, float* position_lo, const float* radius, float* velocity,
+                      int32_t* neighbor_count, float* checkpoints, float* checkpoints_lo, int32_t checkpoint_every,
+                      int32_t slots, int32_t history, int32_t last_build_only, void* workspace,
+                      size_t workspace_bytes, int32_t sync_status, void* stream);
+/* The reverse of `steps` contact steps whose grids wbc_contact_steps left in history slots
+ * 0 .. steps - 1 of `workspace`, in one cooperative launch: lambda (dL/dx after the steps on
+ * entry, dL/dx before them on return; lambda_tmp is scratch of the same size) goes through
+ * lambda_t = lambda_{t+1} + dt J(x_t)^T lambda_{t+1}, and rate_dot[0] (device double, not cleared)
+ * accumulates sum_t sum_i lambda_{t+1,i} . v_i(x_t) / rate. compensated = 1 when the grids were
+ * built from compensated positions. */
+int wbc_adjoint_steps(const wbc_neighbor_grid* grid, int32_t n, float query_radius, float rate, float dt,
+                      int32_t steps, int32_t compensated, float* lambda, float* lambda_tmp, double* rate_dot,
+                      int32_t slots, void* workspace, size_t workspace_bytes, int32_t sync_status, void* stream);
+/* Mixed-precision refinement (the fp32 solves stop near a relative residual of 1e-6): the Newton
+ * step of the steady field at u (FP64): diag = 6 + h U K / (K + u)^2 and rhs = sum_nb u -
+ * (6 + h U / (K + u)) u in FP64 (diag = -1 at faces and at nodes held at the zero clamp), to be
+ * solved by wbc_sor_linear_solve and added by wbc_adjoint_newton_apply (u += d, clamped at 0). */
+int wbc_adjoint_newton_prepare(const wbc_sor_params* p, const double* u, const float* U, float* diag, float* rhs,
+                               void* stream);
+int wbc_adjoint_newton_apply(int64_t nodes, const float* delta, double* u, void* stream);
+/* out[i] = (double) in[i]. */
+int wbc_widen(int64_t n, const float* in, double* out, void* stream);
+/* r = b - (diag x - sum_nb x) in FP64 where diag > 0, 0 elsewhere (the adjoint's refinement step). */
+int wbc_adjoint_linear_residual(const wbc_sor_params* p, const float* diag, const float* b, const float* x, float* r,
+                                void* stream);
+/* The field's gradient sums from the refined field u (FP64) and adjoint mu0 + dmu: sums = {dL/dK,
+ * D dL/dD, dL/dO_b} (cleared first) and phi = mu u / (K + u) for wbc_adjoint_cells. */
+int wbc_adjoint_field_grads(const wbc_sor_params* p, const double* u, const float* U, const float* mu0,
+                            const float* dmu, const float* diag, const float* grad_u, float* phi, double* sums,
+                            void* stream);
 /* Per cell: grad_vmax = coef sum_a w_a phi_a, grad_x += coef vmax grad_x(sum_a w_a phi_a). */
 int wbc_adjoint_cells(const wbc_grid_geometry* geom, int32_t n, const float* position, const float* vmax,
                       const float* phi, float coef, float* grad_vmax, float* grad_x, void* stream);

@@ -22,7 +22,7 @@ CSRC = PACKAGE_DIR / "csrc"
 LIB_DIR = PACKAGE_DIR / "_lib"
 LIB_NAME = "libwbc_gb300.so"
 SOURCES = ("wbc_runtime.cu", "wbc_mechanics.cu", "wbc_fields.cu", "wbc_cells.cu", "wbc_network.cu", "wbc_sor.cu",
-           "wbc_batch.cu", "wbc_adjoint.cu")
+           "wbc_batch.cu", "wbc_adjoint.cu", "wbc_steps.cu")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 

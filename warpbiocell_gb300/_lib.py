@@ -254,6 +254,17 @@ SIGNATURES: dict[str, list] = {
     "wbc_adjoint_field_solve": [POINTER(SorParamsC), _P, _P, _P, _P, _P, _I, _I, _F, _P, _P, _P,
                                 POINTER(SorReportC), _P],
     "wbc_adjoint_cells": [POINTER(GridGeometryC), _I, _P, _P, _P, _F, _P, _P, _P],
+    "wbc_contact_steps_workspace_bytes": [_I, c_int64, _I],
+    "wbc_contact_steps": [POINTER(NeighborGridC), _I, _F, _F, _F, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P,
+                          c_size_t, _I, _P],
+    "wbc_adjoint_steps": [POINTER(NeighborGridC), _I, _F, _F, _F, _I, _I, _P, _P, _P, _I, _P, c_size_t, _I, _P],
+    "wbc_sor_linear_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, POINTER(SorReportC), _P,
+                             c_size_t, _P],
+    "wbc_adjoint_newton_prepare": [POINTER(SorParamsC), _P, _P, _P, _P, _P],
+    "wbc_adjoint_newton_apply": [c_int64, _P, _P, _P],
+    "wbc_widen": [c_int64, _P, _P, _P],
+    "wbc_adjoint_linear_residual": [POINTER(SorParamsC), _P, _P, _P, _P, _P],
+    "wbc_adjoint_field_grads": [POINTER(SorParamsC), _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_contact_substep_region": [POINTER(NeighborGridC), _I, _F, _F, _F, POINTER(TissueRegionC), _P, _P, _P, _P],
     "wbc_sample_sdf": [POINTER(TissueRegionC), _I, _P, _P, _P],
     "wbc_lifecycle_decide": [POINTER(LifecycleParamsC), _I, _P, _P, _P, _P, _P, _P, _P, _P, _P],
@@ -272,7 +283,8 @@ SIGNATURES: dict[str, list] = {
 }
 _RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64,
             "wbc_sor_solve_workspace_bytes": c_size_t, "wbc_sor_batch_plan_bytes": c_size_t,
-            "wbc_batch_plan_bytes": c_size_t}
+            "wbc_batch_plan_bytes": c_size_t,
+    "wbc_contact_steps_workspace_bytes": c_size_t}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

@@ -74,8 +74,7 @@ __global__ void k_weighted_convert(int64_t nodes, long long* __restrict__ acc, f
 
 // ---- reverse: one contact step -----------------------------------------------------------------------
 // Sorted slot t (cell i) of the grid built at x_t: lambda_out_i = lambda_in_i + dt (J^T lambda_in)_i
-// and vdot_i = lambda_in_i . v_i(x_t) / rate, over the same candidates and conditions as the forward
-// step (contact_slot).
+// and vdot_i = lambda_in_i . v_i(x_t) / rate (adjoint_contact_slot in wbc_bodies.cuh).
 __global__ void __launch_bounds__(256) k_adjoint_contact(BucketMap map, int32_t n, const int32_t* __restrict__ bucket_start,
                                                          const int32_t* __restrict__ bucket_count,
                                                          const int32_t* __restrict__ sorted_id,
@@ -84,52 +83,10 @@ __global__ void __launch_bounds__(256) k_adjoint_contact(BucketMap map, int32_t 
                                                          float* __restrict__ lambda_out, float* __restrict__ vdot) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const float4 me = sorted_xyzr[t];
-    const int i = sorted_id[t];
-    const float lix = lambda_in[3 * static_cast<int64_t>(i)], liy = lambda_in[3 * static_cast<int64_t>(i) + 1],
-                liz = lambda_in[3 * static_cast<int64_t>(i) + 2];
-    const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
-    float gx = 0.0f, gy = 0.0f, gz = 0.0f;  // sum_j A_ij (lambda_i - lambda_j) / rate
-    float ux = 0.0f, uy = 0.0f, uz = 0.0f;  // v_i / rate
-    for (int ox = -1; ox <= 1; ++ox) {
-        for (int oy = -1; oy <= 1; ++oy) {
-            for (int oz = -1; oz <= 1; ++oz) {
-                const int b = map.bucket(cx + ox, cy + oy, cz + oz);
-                const int s = bucket_start[b];
-                const int e = s + bucket_count[b];
-                for (int u = s; u < e; ++u) {
-                    if (u == t) continue;
-                    const float4 q = sorted_xyzr[u];
-                    const float dx = me.x - q.x;
-                    const float dy = me.y - q.y;
-                    const float dz = me.z - q.z;
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
-                    if (!(d < query_radius)) continue;
-                    const float R = me.w + q.w;
-                    if (!(R - d > 0.0f && d > 1.0e-6f)) continue;
-                    const float inv_d = 1.0f / d;
-                    const float a = R * inv_d - 1.0f;
-                    ux += a * dx;
-                    uy += a * dy;
-                    uz += a * dz;
-                    const int j = sorted_id[u];
-                    const float ldx = lix - lambda_in[3 * static_cast<int64_t>(j)];
-                    const float ldy = liy - lambda_in[3 * static_cast<int64_t>(j) + 1];
-                    const float ldz = liz - lambda_in[3 * static_cast<int64_t>(j) + 2];
-                    const float proj = R * inv_d * inv_d * inv_d * (dx * ldx + dy * ldy + dz * ldz);
-                    gx += a * ldx - proj * dx;
-                    gy += a * ldy - proj * dy;
-                    gz += a * ldz - proj * dz;
-                }
-            }
-        }
-    }
-    const float f = dt * rate;
-    const int64_t o = 3 * static_cast<int64_t>(i);
-    lambda_out[o] = lix + f * gx;
-    lambda_out[o + 1] = liy + f * gy;
-    lambda_out[o + 2] = liz + f * gz;
-    vdot[i] = lix * ux + liy * uy + liz * uz;
+    int i;
+    const float v = adjoint_contact_slot(map, t, bucket_start, bucket_count, sorted_id, sorted_xyzr, query_radius,
+                                         rate, dt, lambda_in, lambda_out, &i);
+    vdot[i] = v;
 }
 
 // ---- reverse: the field ---------------------------------------------------------------------------------
@@ -310,6 +267,130 @@ __global__ void k_adjoint_cells(wbc_grid_geometry g, int32_t n, const float* __r
     grad_x[o + 2] += f * sz;
 }
 
+// ---- mixed-precision refinement of the field and of its adjoint ----------------------------------------
+// The fp32 solves stop near their rounding floor (a relative residual of about 1e-6), which leaves
+// errors of order 1e-5 in the field and in the adjoint, and so in the gradients. One Newton
+// correction of the field and one refinement step of the adjoint, with residuals formed in FP64
+// and the corrections solved by the same fp32 SOR, bring both to their FP64 values.
+
+template <typename T>
+__device__ __forceinline__ double value_at(const T* __restrict__ u, const wbc_sor_params& p, int i, int j, int k) {
+    // Neumann faces mirror; Dirichlet face nodes hold their own values in u.
+    const int ii = i < 0 ? 1 : (i > p.nx - 1 ? p.nx - 2 : i);
+    const int jj = j < 0 ? 1 : (j > p.ny - 1 ? p.ny - 2 : j);
+    const int kk = k < 0 ? 1 : (k > p.nz - 1 ? p.nz - 2 : k);
+    return static_cast<double>(u[(static_cast<int64_t>(ii) * p.ny + jj) * p.nz + kk]);
+}
+
+// Newton step of the steady field G(u) = sum_nb u - (6 + h U / (K + u)) u = 0 at the current u
+// (FP64): diag = 6 + h U K / (K + u)^2 (the negated Jacobian's diagonal) and rhs = G(u), so that
+// diag d - sum_nb d = rhs gives the correction d. A node is free where u > 0 or G(u) > 0 (a node at
+// the zero clamp with G <= 0 stays there); faces and held nodes get diag = -1, rhs = 0.
+__global__ void k_newton_prepare(wbc_sor_params p, const double* __restrict__ u, const float* __restrict__ U,
+                                 float* __restrict__ diag, float* __restrict__ rhs) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
+    if (a >= nodes) return;
+    const int k = static_cast<int>(a % p.nz);
+    const int64_t ij = a / p.nz;
+    const int j = static_cast<int>(ij % p.ny);
+    const int i = static_cast<int>(ij / p.ny);
+    if (is_dirichlet(p, i, j, k)) {
+        diag[a] = -1.0f;
+        rhs[a] = 0.0f;
+        return;
+    }
+    const double ua = u[a], K = p.michaelis_k, h = p.dx2_over_D, Ua = U[a];
+    const double nb = value_at(u, p, i - 1, j, k) + value_at(u, p, i + 1, j, k) + value_at(u, p, i, j - 1, k) +
+                      value_at(u, p, i, j + 1, k) + value_at(u, p, i, j, k - 1) + value_at(u, p, i, j, k + 1);
+    const double g = nb - (6.0 + h * Ua / (K + ua)) * ua;
+    if (!(ua > 0.0) && !(g > 0.0)) {
+        diag[a] = -1.0f;
+        rhs[a] = 0.0f;
+        return;
+    }
+    const double s = K + ua;
+    diag[a] = static_cast<float>(6.0 + h * Ua * K / (s * s));
+    rhs[a] = static_cast<float>(g);
+}
+
+// u += d, clamped at zero (FP64).
+__global__ void k_newton_apply(int64_t n, const float* __restrict__ d, double* __restrict__ u) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a < n) u[a] = fmax(u[a] + static_cast<double>(d[a]), 0.0);
+}
+
+__global__ void k_widen(int64_t n, const float* __restrict__ in, double* __restrict__ out) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = static_cast<double>(in[a]);
+}
+
+// r = b - (diag x - sum_nb x) in FP64 at the free nodes (diag > 0), 0 elsewhere.
+__global__ void k_linear_residual(wbc_sor_params p, const float* __restrict__ diag, const float* __restrict__ b,
+                                  const float* __restrict__ x, float* __restrict__ r) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
+    if (a >= nodes) return;
+    const float da = diag[a];
+    if (!(da > 0.0f)) {
+        r[a] = 0.0f;
+        return;
+    }
+    const int k = static_cast<int>(a % p.nz);
+    const int64_t ij = a / p.nz;
+    const int j = static_cast<int>(ij % p.ny);
+    const int i = static_cast<int>(ij / p.ny);
+    const double nb = value_at(x, p, i - 1, j, k) + value_at(x, p, i + 1, j, k) + value_at(x, p, i, j - 1, k) +
+                      value_at(x, p, i, j + 1, k) + value_at(x, p, i, j, k - 1) + value_at(x, p, i, j, k + 1);
+    r[a] = static_cast<float>(static_cast<double>(b[a]) - (static_cast<double>(da) * x[a] - nb));
+}
+
+// The field's gradient sums from the refined field u (FP64) and adjoint mu = mu0 + dmu (FP64):
+// phi_a = mu_a u_a / (K + u_a) and [0] dL/dK, [1] D dL/dD, [2] dL/dO_b, as k_adjoint_field_grads.
+__global__ void k_adjoint_field_grads_refined(wbc_sor_params p, const double* __restrict__ u,
+                                              const float* __restrict__ U, const float* __restrict__ mu0,
+                                              const float* __restrict__ dmu, const float* __restrict__ diag,
+                                              const float* __restrict__ g, float* __restrict__ phi,
+                                              double* __restrict__ sums) {
+    const int64_t nodes = static_cast<int64_t>(p.nx) * p.ny * p.nz;
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    double s_k = 0.0, s_d = 0.0, s_b = 0.0;
+    if (a < nodes) {
+        const int k = static_cast<int>(a % p.nz);
+        const int64_t ij = a / p.nz;
+        const int j = static_cast<int>(ij % p.ny);
+        const int i = static_cast<int>(ij / p.ny);
+        double ph = 0.0;
+        if (is_dirichlet(p, i, j, k)) {
+            s_b = g[a];
+        } else if (diag[a] > 0.0f) {
+            const double ua = u[a], m = static_cast<double>(mu0[a]) + static_cast<double>(dmu[a]);
+            const double s = p.michaelis_k + ua;
+            ph = m * ua / s;
+            const double hU = static_cast<double>(p.dx2_over_D) * U[a];
+            s_k = m * hU * ua / (s * s);
+            s_d = m * hU * ua / s;
+            int faces = 0;
+            faces += (p.bc_x == 0 && i == 1) + (p.bc_x == 0 && i == p.nx - 2);
+            faces += (p.bc_y == 0 && j == 1) + (p.bc_y == 0 && j == p.ny - 2);
+            faces += (p.bc_z == 0 && k == 1) + (p.bc_z == 0 && k == p.nz - 2);
+            s_b = m * faces;
+        }
+        phi[a] = static_cast<float>(ph);
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+        s_k += __shfl_xor_sync(0xffffffffu, s_k, d);
+        s_d += __shfl_xor_sync(0xffffffffu, s_d, d);
+        s_b += __shfl_xor_sync(0xffffffffu, s_b, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(sums, s_k);
+        atomicAdd(sums + 1, s_d);
+        atomicAdd(sums + 2, s_b);
+    }
+}
+
 static BucketMap bucket_map(const wbc_neighbor_grid* g) {
     BucketMap m;
     m.inv_edge = 1.0f / (g->cell_size * 1.0009765625f);
@@ -415,6 +496,53 @@ int wbc_adjoint_cells(const wbc_grid_geometry* geom, int32_t n, const float* pos
     k_adjoint_cells<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(*geom, n, position, vmax, phi, coef, grad_vmax,
                                                                     grad_x);
     return check_launch("wbc_adjoint_cells");
+}
+
+
+int wbc_adjoint_newton_prepare(const wbc_sor_params* p, const double* u, const float* U, float* diag, float* rhs,
+                               void* stream) {
+    if (!p || !u || !U || !diag || !rhs || p->nx < 3 || p->ny < 3 || p->nz < 3) return WBC_ERR_INVALID;
+    const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
+    k_newton_prepare<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(*p, u, U, diag, rhs);
+    return check_launch("wbc_adjoint_newton_prepare");
+}
+
+int wbc_adjoint_newton_apply(int64_t nodes, const float* delta, double* u, void* stream) {
+    if (nodes < 0 || (nodes > 0 && (!delta || !u))) return WBC_ERR_INVALID;
+    if (nodes == 0) return WBC_OK;
+    k_newton_apply<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, delta, u);
+    return check_launch("wbc_adjoint_newton_apply");
+}
+
+int wbc_widen(int64_t n, const float* in, double* out, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_widen<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, in, out);
+    return check_launch("wbc_widen");
+}
+
+int wbc_adjoint_linear_residual(const wbc_sor_params* p, const float* diag, const float* b, const float* x, float* r,
+                                void* stream) {
+    if (!p || !diag || !b || !x || !r || p->nx < 3 || p->ny < 3 || p->nz < 3) return WBC_ERR_INVALID;
+    const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
+    k_linear_residual<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(*p, diag, b, x, r);
+    return check_launch("wbc_adjoint_linear_residual");
+}
+
+int wbc_adjoint_field_grads(const wbc_sor_params* p, const double* u, const float* U, const float* mu0,
+                            const float* dmu, const float* diag, const float* grad_u, float* phi, double* sums,
+                            void* stream) {
+    if (!p || !u || !U || !mu0 || !dmu || !diag || !grad_u || !phi || !sums || p->nx < 3 || p->ny < 3 || p->nz < 3)
+        return WBC_ERR_INVALID;
+    const int64_t nodes = static_cast<int64_t>(p->nx) * p->ny * p->nz;
+    cudaStream_t s = as_stream(stream);
+    cudaError_t err = cudaMemsetAsync(sums, 0, 3 * sizeof(double), s);
+    if (err != cudaSuccess) {
+        set_error("wbc_adjoint_field_grads: cudaMemsetAsync", err);
+        return WBC_ERR_CUDA;
+    }
+    k_adjoint_field_grads_refined<<<grid_for(nodes), kThreads, 0, s>>>(*p, u, U, mu0, dmu, diag, grad_u, phi, sums);
+    return check_launch("wbc_adjoint_field_grads");
 }
 
 }  // extern "C"

@@ -157,6 +157,66 @@ __device__ __forceinline__ void contact_slot(BucketMap map, int t, const int32_t
     position[o + 2] = me.z + vz * dt;
 }
 
+// The reverse of one contact step for sorted slot t (cell i, returned in *cell) of the grid built
+// at x_t: lambda_out_i = lambda_in_i + dt (J^T lambda_in)_i with (J^T lambda)_i = rate sum_j A_ij
+// (lambda_i - lambda_j), A_ij = (R/d - 1) I - R e e^T / d^3 (e = x_i - x_j, R = r_i + r_j), over the
+// same candidates and conditions as contact_slot. Returns lambda_in_i . v_i(x_t) / rate, the cell's
+// term of dL/drate.
+__device__ __forceinline__ float adjoint_contact_slot(BucketMap map, int t, const int32_t* __restrict__ bucket_start,
+                                                      const int32_t* __restrict__ bucket_count,
+                                                      const int32_t* __restrict__ sorted_id,
+                                                      const float4* __restrict__ sorted_xyzr, float query_radius,
+                                                      float rate, float dt, const float* __restrict__ lambda_in,
+                                                      float* __restrict__ lambda_out, int* cell) {
+    const float4 me = sorted_xyzr[t];
+    const int i = sorted_id[t];
+    const float lix = lambda_in[3 * static_cast<int64_t>(i)], liy = lambda_in[3 * static_cast<int64_t>(i) + 1],
+                liz = lambda_in[3 * static_cast<int64_t>(i) + 2];
+    const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    float gx = 0.0f, gy = 0.0f, gz = 0.0f;  // sum_j A_ij (lambda_i - lambda_j) / rate
+    float ux = 0.0f, uy = 0.0f, uz = 0.0f;  // v_i / rate
+    for (int ox = -1; ox <= 1; ++ox) {
+        for (int oy = -1; oy <= 1; ++oy) {
+            for (int oz = -1; oz <= 1; ++oz) {
+                const int b = map.bucket(cx + ox, cy + oy, cz + oz);
+                const int s = bucket_start[b];
+                const int e = s + bucket_count[b];
+                for (int u = s; u < e; ++u) {
+                    if (u == t) continue;
+                    const float4 q = sorted_xyzr[u];
+                    const float dx = me.x - q.x;
+                    const float dy = me.y - q.y;
+                    const float dz = me.z - q.z;
+                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    if (!(d < query_radius)) continue;
+                    const float R = me.w + q.w;
+                    if (!(R - d > 0.0f && d > 1.0e-6f)) continue;
+                    const float inv_d = 1.0f / d;
+                    const float a = R * inv_d - 1.0f;
+                    ux += a * dx;
+                    uy += a * dy;
+                    uz += a * dz;
+                    const int j = sorted_id[u];
+                    const float ldx = lix - lambda_in[3 * static_cast<int64_t>(j)];
+                    const float ldy = liy - lambda_in[3 * static_cast<int64_t>(j) + 1];
+                    const float ldz = liz - lambda_in[3 * static_cast<int64_t>(j) + 2];
+                    const float proj = R * inv_d * inv_d * inv_d * (dx * ldx + dy * ldy + dz * ldz);
+                    gx += a * ldx - proj * dx;
+                    gy += a * ldy - proj * dy;
+                    gz += a * ldz - proj * dz;
+                }
+            }
+        }
+    }
+    const float f = dt * rate;
+    const int64_t o = 3 * static_cast<int64_t>(i);
+    lambda_out[o] = lix + f * gx;
+    lambda_out[o + 1] = liy + f * gy;
+    lambda_out[o + 2] = liz + f * gz;
+    *cell = i;
+    return lix * ux + liy * uy + liz * uz;
+}
+
 __device__ __forceinline__ void deposit_cell(const wbc_grid_geometry& g, int c, const float* __restrict__ position,
                                              const int32_t* __restrict__ cell_state,
                                              unsigned long long* __restrict__ acc) {

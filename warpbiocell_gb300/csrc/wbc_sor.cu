@@ -52,7 +52,8 @@ struct __align__(128) SorControl {
     float residual;
     int converged;
     int status;
-    int pad[25];
+    unsigned int scale_bits[2];  // linear solves: the residual's scale, max(6 |x|, |b|)
+    int pad[23];
 };
 static_assert(sizeof(SorControl) == 128, "SorControl is one 128-byte line");
 constexpr int kMaxCtas = 1024;     // barrier flags that follow the control block
@@ -323,7 +324,7 @@ __device__ __forceinline__ float neighbour_sum(const Sweep& w, const float* pv, 
 // colour planes. Every lane computes; only nodes with a coefficient are written, and the IEEE
 // division replaces the fast one only where the range tests above do not hold. An edge group also
 // stores every valid entry (unchanged ones too) to the exchange buffer with this half-sweep's tag.
-template <bool HAS_PROD, bool ZCLAMP>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
 __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, float* po, const float* pv,
                                             unsigned long long* xp, const int4& d, int off, unsigned mask, float du,
                                             float prod, int colour, int lane, unsigned int tag) {
@@ -332,6 +333,14 @@ __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, fl
     if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
     const bool active = du >= 0.0f;
     const float o = *po;
+    if (LINEAR) {
+        // d x - sum_nb x = b: du holds 1 / d, prod holds b; no clamp.
+        const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
+        const float v = w.one_minus_omega * o + w.omega * ((nb + prod) * du);
+        if (active) *po = v;
+        if (group_edge(d) && off + lane < d.w) store_tagged(xp, active ? v : o, tag);
+        return;
+    }
     const float b1 = w.K + o;
     const float cc = div_rn_fast_nonneg_zero(du, b1);
     const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
@@ -348,7 +357,7 @@ __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, fl
 
 // The groups of one colour, a warp per group, edge groups first; the next group's coefficients
 // (and production terms), which live in L2, are loaded before the current group is relaxed.
-template <bool HAS_PROD, bool ZCLAMP>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
 __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, int colour, int warp, int nwarps,
                                              int lane, unsigned int tag) {
     int q = warp;
@@ -384,8 +393,8 @@ __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, i
 #pragma unroll
         for (int r = 0; r < kSub; ++r)
             if (r == 0 || d.w > 32 * r)
-                relax_lanes<HAS_PROD, ZCLAMP>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r], du[r],
-                                              pr[r], colour, lane, tag);
+                relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
+                                                      du[r], pr[r], colour, lane, tag);
         if (!more) break;
         d = dn;
 #pragma unroll
@@ -430,6 +439,34 @@ __device__ __forceinline__ unsigned int residual_group(const SorArgs& a, const S
         if (active) bits = max(bits, __float_as_uint(val));
     }
     return bits;
+}
+
+// Linear solves: max |b + sum_nb x - d x| and max(6 |x|, |b|) over the group's nodes of colour
+// `colour`, as float bits, into *res and *scale.
+template <bool ZCLAMP>
+__device__ __forceinline__ void residual_group_linear(const SorArgs& a, const Sweep& w, int q, int colour, int lane,
+                                                      unsigned int& res, unsigned int& scale) {
+    const int4 d = w.relax[q];
+    const uint4 mk = w.masks[q];
+    const unsigned mw[4] = {mk.x, mk.y, mk.z, mk.w};
+#pragma unroll
+    for (int r = 0; r < kSub; ++r) {
+        const int off = 32 * r;
+        if (off >= d.w) break;
+        const float du = off + lane < d.w ? a.coeff[colour * w.gplane + d.y + off + lane] : -1.0f;
+        if (!(du >= 0.0f)) continue;
+        const float b = a.pcopy[colour * w.gplane + d.y + off + lane];
+        const int kp = ((mw[r] >> lane) & 1) ^ colour;
+        const float* po = w.s + colour * w.plane + d.x + off + lane;
+        const float* pv = w.s + (colour ^ 1) * w.plane + d.x + off + lane;
+        int m = 0, last = 0;
+        if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
+        const float o = *po;
+        const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
+        const float rr = fabsf(b + nb - __frcp_rn(du) * o);
+        res = max(res, __float_as_uint(rr));
+        scale = max(scale, __float_as_uint(fmaxf(6.0f * fabsf(o), fabsf(b))));
+    }
 }
 
 // Reads colour `colour` of the halo columns once every entry carries `tag` and stores the values
@@ -616,12 +653,14 @@ __device__ __forceinline__ void build_lists(const SorArgs& a, const TileRect& r,
 }
 
 // One tile (`tile` of `ntiles`) of one solve, for the whole solve. `claims` / `claims_needed`:
-// see WaitClock (batched solves; null for a single solve).
-template <bool HAS_PROD, bool ZCLAMP>
+// see WaitClock (batched solves; null for a single solve). LINEAR: the linear system
+// d x - sum_nb x = b (`density` holds d, d <= 0 holds x; `production` holds b).
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
 __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles, const unsigned int* claims = nullptr,
                                          unsigned int claims_needed = 0) {
     extern __shared__ __align__(128) float s[];
     __shared__ unsigned int s_red[32];
+    __shared__ unsigned int s_scale[32];
     __shared__ int s_outside_range;
     const int M = a.t.M, nz = a.p.nz, nx = a.p.nx, ny = a.p.ny;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -662,14 +701,22 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
                     const bool face = (pp.bc_x == 0 && (gi == 0 || gi == nx - 1)) ||
                                       (pp.bc_y == 0 && (gj == 0 || gj == ny - 1)) ||
                                       (pp.bc_z == 0 && (kk == 0 || kk == nz - 1));
-                    if (!face && !(a.fixed && a.fixed[idx] != 0)) u = a.density[idx] * pp.uptake_max;
-                    if (!coefficient_in_range(u, w.K, w.h)) s_outside_range = 1;
+                    if (LINEAR) {
+                        const float dd = a.density[idx];
+                        if (!face && dd > 0.0f) u = 1.0f / dd;
+                    } else {
+                        if (!face && !(a.fixed && a.fixed[idx] != 0)) u = a.density[idx] * pp.uptake_max;
+                        if (!coefficient_in_range(u, w.K, w.h)) s_outside_range = 1;
+                    }
                 }
                 const int64_t at = c * w.gplane + (static_cast<int64_t>(gi) * ny + gj) * M + (kk >> 1);
                 a.coeff[at] = u;
                 // The production term is fixed for the solve: computed once here (only where a node
                 // is updated, as the update itself would) instead of in every sweep.
-                if (HAS_PROD) a.pcopy[at] = u >= 0.0f ? prod_term(a, base + kk) : 0.0f;
+                if (LINEAR)
+                    a.pcopy[at] = u >= 0.0f ? a.production[base + kk] : 0.0f;
+                else if (HAS_PROD)
+                    a.pcopy[at] = u >= 0.0f ? prod_term(a, base + kk) : 0.0f;
                 // The edge columns start with tag 0 (half-sweeps are tagged from 1), so words a
                 // previous solve left in the buffer are never taken for this solve's.
                 if (k == kEdge) store_tagged(a.xchg + at, v, 0u);
@@ -690,7 +737,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
         for (int half = 0; half < 2 * chunk; ++half) {
             const int colour = half & 1;
             const unsigned int tag = static_cast<unsigned int>(2 * sweeps + half + 1);
-            relax_colour<HAS_PROD, ZCLAMP>(a, w, colour, warp, nwarps, lane, tag);
+            relax_colour<HAS_PROD || LINEAR, ZCLAMP, LINEAR>(a, w, colour, warp, nwarps, lane, tag);
             const bool fine = pull_halo(a, w, colour, tag, warp, nwarps, lane);
             if (__syncthreads_or(!fine)) {
                 if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
@@ -704,30 +751,60 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
         }
         if (!ok) break;
         sweeps += chunk;
-        // Max-norm residual of the current field over every updated node (both colours).
-        unsigned int bits = 0u;
+        // Max-norm residual of the current field over every updated node (both colours); for a
+        // linear solve also the scale it is compared against.
+        unsigned int bits = 0u, sbits = 0u;
         for (int q = warp; q < w.n_relax; q += nwarps) {
-            bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 0, lane));
-            bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 1, lane));
+            if (LINEAR) {
+                residual_group_linear<ZCLAMP>(a, w, q, 0, lane, bits, sbits);
+                residual_group_linear<ZCLAMP>(a, w, q, 1, lane, bits, sbits);
+            } else {
+                bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 0, lane));
+                bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 1, lane));
+            }
         }
 #pragma unroll
-        for (int dd = 16; dd > 0; dd >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
-        if (lane == 0) s_red[warp] = bits;
+        for (int dd = 16; dd > 0; dd >>= 1) {
+            bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
+            if (LINEAR) sbits = max(sbits, __shfl_xor_sync(0xffffffffu, sbits, dd));
+        }
+        if (lane == 0) {
+            s_red[warp] = bits;
+            if (LINEAR) s_scale[warp] = sbits;
+        }
         __syncthreads();
         const int slot = chunk_index & 1;
         if (warp == 0) {
             bits = lane < nwarps ? s_red[lane] : 0u;
+            sbits = LINEAR && lane < nwarps ? s_scale[lane] : 0u;
 #pragma unroll
-            for (int dd = 16; dd > 0; dd >>= 1) bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
-            if (lane == 0) atomicMax(&a.ctl->res_bits[slot], bits);
+            for (int dd = 16; dd > 0; dd >>= 1) {
+                bits = max(bits, __shfl_xor_sync(0xffffffffu, bits, dd));
+                if (LINEAR) sbits = max(sbits, __shfl_xor_sync(0xffffffffu, sbits, dd));
+            }
+            if (lane == 0) {
+                atomicMax(&a.ctl->res_bits[slot], bits);
+                if (LINEAR) atomicMax(&a.ctl->scale_bits[slot], sbits);
+            }
         }
         ok = grid_barrier(a.ctl, a.flags, epoch, tile, ntiles, claims, claims_needed);
         if (!ok) break;
         residual = __uint_as_float(load_acquire(&a.ctl->res_bits[slot]));
+        float scale = 1.0f;
+        if (LINEAR) scale = __uint_as_float(load_acquire(&a.ctl->scale_bits[slot]));
         // The next chunk's slot was last read before this chunk's first barrier: safe to clear.
-        if (tile == 0 && threadIdx.x == 0) atomicExch(&a.ctl->res_bits[slot ^ 1], 0u);
+        if (tile == 0 && threadIdx.x == 0) {
+            atomicExch(&a.ctl->res_bits[slot ^ 1], 0u);
+            if (LINEAR) atomicExch(&a.ctl->scale_bits[slot ^ 1], 0u);
+        }
         ++chunk_index;
-        if (static_cast<double>(residual) < a.tolerance) {
+        if (LINEAR) {
+            residual = scale > 0.0f ? residual / scale : 0.0f;  // relative to max(6 |x|, |b|)
+            if (static_cast<double>(residual) < a.tolerance || scale == 0.0f) {
+                converged = true;
+                break;
+            }
+        } else if (static_cast<double>(residual) < a.tolerance) {
             converged = true;
             break;
         }
@@ -755,9 +832,9 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
     }
 }
 
-template <bool HAS_PROD, bool ZCLAMP>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
 __global__ void __launch_bounds__(kSorThreads, 1) k_sor_resident(SorArgs a) {
-    sor_tile<HAS_PROD, ZCLAMP>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
+    sor_tile<HAS_PROD, ZCLAMP, LINEAR>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
 }
 
 // The solver's grid barrier alone, for the self-test of the bounded waits: `ntiles` tiles are
@@ -804,8 +881,8 @@ __global__ void __launch_bounds__(kSorThreads, 1)
         const int t = s_tile;
         if (t >= total) return;
         const int b = find_batch_item(tile_first, n, t);
-        sor_tile<HAS_PROD, ZCLAMP>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
-                                   static_cast<unsigned int>(tile_first[b + 1]));
+        sor_tile<HAS_PROD, ZCLAMP, false>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
+                                          static_cast<unsigned int>(tile_first[b + 1]));
     }
 }
 
@@ -825,9 +902,10 @@ __global__ void k_sor_batch_reset(const SorArgs* __restrict__ args, const int32_
 // ---- host side -------------------------------------------------------------------------------------------
 using KernelFn = void (*)(SorArgs);
 
-static KernelFn kernel_for(bool has_prod, bool zclamp) {
-    if (has_prod) return zclamp ? k_sor_resident<true, true> : k_sor_resident<true, false>;
-    return zclamp ? k_sor_resident<false, true> : k_sor_resident<false, false>;
+static KernelFn kernel_for(bool has_prod, bool zclamp, bool linear) {
+    if (linear) return zclamp ? k_sor_resident<true, true, true> : k_sor_resident<true, false, true>;
+    if (has_prod) return zclamp ? k_sor_resident<true, true, false> : k_sor_resident<true, false, false>;
+    return zclamp ? k_sor_resident<false, true, false> : k_sor_resident<false, false, false>;
 }
 
 struct DeviceInfo {
@@ -953,7 +1031,7 @@ static void place_workspace(const wbc_sor_params& p, void* workspace, SorArgs* a
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
                        float* field, float* residual_out, wbc_sor_report* report, void* workspace,
-                       const wbc_sor_tuning* tuning, cudaStream_t stream, bool* feasible) {
+                       const wbc_sor_tuning* tuning, cudaStream_t stream, bool* feasible, bool linear = false) {
     const DeviceInfo dev = device_info();
     const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;  // static shared memory of the kernel
     SorTiling t{};
@@ -962,7 +1040,7 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     *feasible = dev.sms > 0 && want_tiles <= dev.sms && choose_tiling(p, want_tiles, limit, want_strips, &t);
     if (!*feasible) return WBC_OK;
     const bool has_prod = production != nullptr || p.has_source;
-    KernelFn fn = kernel_for(has_prod, p.bc_z != 0);
+    KernelFn fn = kernel_for(has_prod, p.bc_z != 0, linear);
     cudaError_t err = cudaFuncSetAttribute(reinterpret_cast<const void*>(fn),
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(t.smem));
     if (err != cudaSuccess) {
@@ -1344,6 +1422,29 @@ int wbc_sor_autotune(const wbc_sor_params* p, int32_t check_every, const int32_t
         if (best_us_per_sweep) *best_us_per_sweep = best_ms[pick] * 1000.0f / sweeps;
     }
     return WBC_OK;
+}
+
+int wbc_sor_linear_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
+                         const float* diag, const float* rhs, float* x, wbc_sor_report* report, void* workspace,
+                         size_t workspace_bytes, void* stream) {
+    if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || check_every < 1 || max_sweeps < 1 || !diag || !rhs || !x ||
+        !report || !workspace || !(p->omega > 0.0f && p->omega < 2.0f))
+        return WBC_ERR_INVALID;
+    if (workspace_bytes < sor_workspace_bytes(*p)) return WBC_ERR_WORKSPACE;
+    if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0) {
+        set_error_msg("wbc_sor_linear_solve: the workspace must be 16-byte aligned");
+        return WBC_ERR_INVALID;
+    }
+    bool feasible = false;
+    wbc_sor_params q = *p;
+    q.has_source = 0;
+    const int rc = sor_solve_resident(q, check_every, max_sweeps, tolerance, nullptr, diag, rhs, nullptr, x, nullptr,
+                                      report, workspace, nullptr, as_stream(stream), &feasible, true);
+    if (rc == WBC_OK && !feasible) {
+        set_error_msg("wbc_sor_linear_solve: the grid does not fit the shared-memory resident solver");
+        return WBC_ERR_INVALID;
+    }
+    return rc;
 }
 
 int wbc_sor_wait_selftest(int32_t ctas, int32_t missing, int32_t rounds, void* workspace, size_t workspace_bytes,

@@ -12,7 +12,11 @@ differentiated with respect to the per-cell ``vmax`` and the scalars ``km``, ``d
 ``boundary`` and ``stiffness``. The backward pass solves the transposed linearised field operator
 with red-black SOR, forms the parameter and position gradients, and runs the contact steps in
 reverse over the neighbour sets of the forward steps, recomputing the positions of each
-segment of sqrt(K) steps from a checkpoint (so memory grows with sqrt(K) position arrays).
+segment of sqrt(K) steps from a checkpoint (so memory grows with sqrt(K) position arrays and
+sqrt(K) hash grids). The K forward steps run in one launch; each segment takes one launch to
+recompute and one to reverse. The steady field is the fp32 SOR solution corrected by Newton steps
+whose residuals are formed in FP64, and the field adjoint is refined the same way, so the
+gradients match an FP64 evaluation of the model.
 
 The reference has no differentiable path; the forward pieces are its contact law, deposit and SOR
 update (kernels/mechanics_kernels.py:26-67, kernels/field_kernels.py:78-116 and 185-212) with a
@@ -58,25 +62,59 @@ class AdjointSpheroid:
         self.settings = settings
         self.adjoint_tolerance = float(adjoint_tolerance)
         self.segment = max(1, int(math.ceil(math.sqrt(max(self.steps, 1)))))
-        self.grid = NeighborGrid(contact.query_radius, dim=128, device=self.device)
+        # Hash buckets: 64 per axis when the cells' extent (with room to move) spans fewer buckets,
+        # so no two cells closer than the query radius alias; any size finds the same pairs, a
+        # smaller one only scans fewer empty buckets per step.
+        extent = float((self.x0.max(dim=0).values - self.x0.min(dim=0).values).max().item()) if self.n else 0.0
+        dim = 64 if extent / contact.query_radius + 8 <= 64 else 128
+        self.grid = NeighborGrid(contact.query_radius, dim=dim, device=self.device)
         self.grid.reserve(self.n)
+        self._slots = max(2, self.segment)
+        lib = _lib.load()
+        ws_bytes = int(lib.wbc_contact_steps_workspace_bytes(dim, self.grid.struct.capacity, self._slots))
+        self._steps_ws = torch.empty(ws_bytes + 256, dtype=torch.uint8, device=self.device)
+        off = (-self._steps_ws.data_ptr()) % 256
+        self._steps_ws = self._steps_ws[off:off + ws_bytes]
+        nseg = max(1, (self.steps + self.segment - 1) // self.segment)
+        self._checkpoints = torch.empty(nseg, self.n, 3, dtype=torch.float32, device=self.device)
+        self._checkpoints_lo = torch.empty_like(self._checkpoints)
         self.velocity = torch.zeros(self.n, 3, dtype=torch.float32, device=self.device)
         self.neighbor_count = torch.zeros(self.n, dtype=torch.int32, device=self.device)
         self.accumulator = torch.zeros(geometry.node_count, dtype=torch.int64, device=self.device)
         self.uptake = torch.zeros(geometry.node_count, dtype=torch.float32, device=self.device)
         self._residual = torch.zeros(1, dtype=torch.float32, device=self.device)
+        nodes = geometry.node_count
+        self._diag = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._rhs = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._delta = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        probe = _lib.SorParamsC(nx=geometry.shape[0], ny=geometry.shape[1], nz=geometry.shape[2])
+        self._workspace = torch.empty(int(_lib.load().wbc_sor_solve_workspace_bytes(ctypes.byref(probe))),
+                                      dtype=torch.uint8, device=self.device)
+        # Newton corrections of the fp32 steady field and refinement of the adjoint solve, each to this
+        # relative residual (the correction problems are solved in fp32, their residuals in FP64).
+        self.newton_steps = 2
+        self.refine_tolerance = 1e-6
         self.last_forward_sweeps = 0
+        self.last_newton_sweeps = 0
         self.last_adjoint_sweeps = 0
 
     # ---- pieces ------------------------------------------------------------------------------------
-    def _step(self, pos: torch.Tensor, rate: float) -> None:
-        """One contact step in place (the plain path's contact_substep)."""
-        st = _lib.stream(self.device)
-        _lib.call("wbc_grid_build", ctypes.byref(self.grid.struct), self.n, _lib.ptr(pos), _lib.ptr(self.radii), st)
-        _lib.call("wbc_contact_substep", ctypes.byref(self.grid.struct), self.n, float(self.contact.query_radius),
-                  float(rate), self.dt, _lib.ptr(pos), _lib.ptr(self.velocity), _lib.ptr(self.neighbor_count), st)
+    def _steps(self, pos: torch.Tensor, lo: torch.Tensor, rate: float, steps: int, checkpoints: bool = False,
+               history: bool = False) -> None:
+        """`steps` contact steps in place on the compensated positions pos + lo (the plain path's
+        contact law, the positions kept to about 48 bits) in one launch; with `checkpoints`, x_t for
+        every t % segment == 0; with `history`, the grids of the steps' starting positions are kept
+        for the reverse pass and the last step only builds its grid."""
+        _lib.call("wbc_contact_steps", ctypes.byref(self.grid.struct), self.n, float(self.contact.query_radius),
+                  float(rate), self.dt, int(steps), _lib.ptr(pos), _lib.ptr(lo), _lib.ptr(self.radii),
+                  _lib.ptr(self.velocity), _lib.ptr(self.neighbor_count),
+                  _lib.ptr(self._checkpoints) if checkpoints else None,
+                  _lib.ptr(self._checkpoints_lo) if checkpoints else None, self.segment, self._slots, int(history),
+                  int(history), _lib.ptr(self._steps_ws), self._steps_ws.numel(), 1, _lib.stream(self.device))
 
     def _field(self, pos: torch.Tensor, vmax: torch.Tensor, km: float, diffusion: float, boundary: float):
+        """Deposit, the fp32 steady solve, then Newton corrections with FP64 residuals: returns the
+        field object and the refined field (float64, flat)."""
         st = _lib.stream(self.device)
         scale = float(vmax.mean().item())
         weight = (vmax / scale).to(torch.float32).contiguous()
@@ -89,23 +127,44 @@ class AdjointSpheroid:
         kin = UptakeKinetics(diffusion, 1.0, km)
         report = solve_steady_state(field, self.uptake, kin, self.settings, self._residual)
         self.last_forward_sweeps = report.sweeps
-        return field, report
+        nodes = self.geometry.node_count
+        u64 = torch.empty(nodes, dtype=torch.float64, device=self.device)
+        _lib.call("wbc_widen", nodes, _lib.ptr(field.values), _lib.ptr(u64), st)
+        params = sor_params(field, kin, self.settings.omega, False, 1.0)
+        sweeps = 0
+        for _ in range(self.newton_steps):
+            _lib.call("wbc_adjoint_newton_prepare", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(self.uptake),
+                      _lib.ptr(self._diag), _lib.ptr(self._rhs), st)
+            self._delta.zero_()
+            sweeps += self._linear_solve(params, self._diag, self._rhs, self._delta, self.refine_tolerance)
+            _lib.call("wbc_adjoint_newton_apply", nodes, _lib.ptr(self._delta), _lib.ptr(u64), st)
+        self.last_newton_sweeps = sweeps
+        return field, u64
+
+    def _linear_solve(self, params, diag: torch.Tensor, rhs: torch.Tensor, x: torch.Tensor, tolerance: float) -> int:
+        """diag x - sum_nb x = rhs from x's current values, in one resident launch; returns the sweeps."""
+        report = _lib.SorReportC()
+        ws = self._workspace
+        _lib.call("wbc_sor_linear_solve", ctypes.byref(params), int(self.settings.check_every),
+                  int(self.settings.max_sweeps), float(tolerance), _lib.ptr(diag), _lib.ptr(rhs), _lib.ptr(x),
+                  ctypes.byref(report), _lib.ptr(ws), ws.numel(), _lib.stream(self.device))
+        self.last_linear_converged = bool(report.converged)
+        return int(report.sweeps)
 
     # ---- forward / backward ------------------------------------------------------------------------
     def forward(self, vmax: torch.Tensor, km: float, diffusion: float, boundary: float, stiffness: float):
         """(u flat, x_K); keeps the checkpoints and the field state for :meth:`backward`."""
         rate = float(stiffness) / self.contact.damping
-        pos = self.x0.clone()
-        self._checkpoints = []
-        for t in range(self.steps):
-            if t % self.segment == 0:
-                self._checkpoints.append(pos.clone())
-            self._step(pos, rate)
-        field, report = self._field(pos, vmax, km, diffusion, boundary)
+        hi = self.x0.clone()
+        lo = torch.zeros_like(hi)
+        self._steps(hi, lo, rate, self.steps, checkpoints=True)
+        x64 = hi.double() + lo.double()
+        pos = x64.float()  # the cells' positions for the deposit
+        field, u64 = self._field(pos, vmax, km, diffusion, boundary)
         self._saved = dict(pos=pos, vmax=vmax.detach().contiguous(), km=float(km), diffusion=float(diffusion),
                            boundary=float(boundary), stiffness=float(stiffness), rate=rate, field=field,
-                           uptake=self.uptake.clone())
-        return field.values.reshape(-1).clone(), pos.clone()
+                           uptake=self.uptake.clone(), u64=u64)
+        return u64.clone(), x64
 
     def backward(self, grad_u: torch.Tensor | None, grad_x: torch.Tensor | None) -> dict:
         sv = self._saved
@@ -117,21 +176,27 @@ class AdjointSpheroid:
         lam = torch.zeros(self.n, 3, dtype=torch.float32, device=self.device) if grad_x is None else \
             grad_x.detach().to(torch.float32).contiguous().clone()
 
-        # field adjoint
+        # field adjoint: (6 + h kappa) mu - sum_nb mu = dL/du at the refined field, solved in fp32 and
+        # refined once with the residual in FP64 (mu = mu0 + dmu)
         kin = UptakeKinetics(sv["diffusion"], 1.0, sv["km"])
         params = sor_params(field, kin, self.settings.omega, False, 1.0)
-        mu = torch.zeros(nodes, dtype=torch.float32, device=self.device)
-        kappa = torch.empty_like(mu)
-        phi = torch.empty_like(mu)
-        sums = torch.zeros(3, dtype=torch.float64, device=self.device)
-        bits = torch.zeros(2, dtype=torch.int32, device=self.device)
-        report = _lib.SorReportC()
-        _lib.call("wbc_adjoint_field_solve", ctypes.byref(params), _lib.ptr(field.values), _lib.ptr(sv["uptake"]),
-                  _lib.ptr(g), _lib.ptr(mu), _lib.ptr(kappa), int(self.settings.check_every),
-                  int(self.settings.max_sweeps), self.adjoint_tolerance, _lib.ptr(phi), _lib.ptr(sums),
-                  _lib.ptr(bits), ctypes.byref(report), st)
-        self.last_adjoint_converged = bool(report.converged)
-        self.last_adjoint_sweeps = int(report.sweeps)
+        u64 = sv["u64"]
+        diag, rhs = self._diag, self._rhs
+        _lib.call("wbc_adjoint_newton_prepare", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(sv["uptake"]),
+                  _lib.ptr(diag), _lib.ptr(rhs), st)
+        mu0 = torch.zeros(nodes, dtype=torch.float32, device=self.device)
+        dmu = torch.zeros(nodes, dtype=torch.float32, device=self.device)
+        sweeps = self._linear_solve(params, diag, g, mu0, self.adjoint_tolerance)
+        converged = self.last_linear_converged
+        _lib.call("wbc_adjoint_linear_residual", ctypes.byref(params), _lib.ptr(diag), _lib.ptr(g), _lib.ptr(mu0),
+                  _lib.ptr(rhs), st)
+        sweeps += self._linear_solve(params, diag, rhs, dmu, self.adjoint_tolerance)
+        phi = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        sums = torch.empty(3, dtype=torch.float64, device=self.device)
+        _lib.call("wbc_adjoint_field_grads", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(sv["uptake"]),
+                  _lib.ptr(mu0), _lib.ptr(dmu), _lib.ptr(diag), _lib.ptr(g), _lib.ptr(phi), _lib.ptr(sums), st)
+        self.last_adjoint_converged = converged and self.last_linear_converged
+        self.last_adjoint_sweeps = sweeps
         d_km, d_diffusion_times_d, d_boundary = sums.tolist()
         h = params.dx2_over_D
         grad_vmax = torch.empty(self.n, dtype=torch.float32, device=self.device)
@@ -140,29 +205,24 @@ class AdjointSpheroid:
         _lib.call("wbc_adjoint_cells", ctypes.byref(geom), self.n, _lib.ptr(pos), _lib.ptr(vmax), _lib.ptr(phi),
                   coef, _lib.ptr(grad_vmax), _lib.ptr(lam), st)
 
-        # mechanics in reverse, one checkpointed segment at a time
+        # mechanics in reverse, one checkpointed segment at a time: the segment's positions are
+        # recomputed from its checkpoint in one launch that keeps each step's grid, then its steps
+        # run in reverse in one launch over those grids
         rate = sv["rate"]
-        d_rate = torch.zeros((), dtype=torch.float64, device=self.device)
-        lam_next = torch.empty_like(lam)
-        vdot = torch.empty(self.n, dtype=torch.float32, device=self.device)
-        for seg in range(len(self._checkpoints) - 1, -1, -1):
+        rate_dot = torch.zeros(1, dtype=torch.float64, device=self.device)
+        lam_tmp = torch.empty_like(lam)
+        work = torch.empty_like(self.x0)
+        work_lo = torch.empty_like(self.x0)
+        for seg in range((self.steps + self.segment - 1) // self.segment - 1, -1, -1):
             start = seg * self.segment
             stop = min(self.steps, start + self.segment)
-            states = [self._checkpoints[seg].clone()]
-            for _ in range(start, stop - 1):
-                nxt = states[-1].clone()
-                self._step(nxt, rate)
-                states.append(nxt)
-            for t in range(stop - 1, start - 1, -1):
-                xt = states[t - start]
-                _lib.call("wbc_grid_build", ctypes.byref(self.grid.struct), self.n, _lib.ptr(xt),
-                          _lib.ptr(self.radii), st)
-                _lib.call("wbc_adjoint_contact", ctypes.byref(self.grid.struct), self.n,
-                          float(self.contact.query_radius), float(rate), self.dt, _lib.ptr(lam), _lib.ptr(lam_next),
-                          _lib.ptr(vdot), st)
-                d_rate += vdot.sum(dtype=torch.float64)
-                lam, lam_next = lam_next, lam
-        d_rate = self.dt * float(d_rate.item())
+            work.copy_(self._checkpoints[seg])
+            work_lo.copy_(self._checkpoints_lo[seg])
+            self._steps(work, work_lo, rate, stop - start, history=True)
+            _lib.call("wbc_adjoint_steps", ctypes.byref(self.grid.struct), self.n, float(self.contact.query_radius),
+                      float(rate), self.dt, stop - start, 1, _lib.ptr(lam), _lib.ptr(lam_tmp), _lib.ptr(rate_dot),
+                      self._slots, _lib.ptr(self._steps_ws), self._steps_ws.numel(), 1, st)
+        d_rate = self.dt * float(rate_dot.item())
         return dict(vmax=grad_vmax, km=d_km, diffusion=d_diffusion_times_d / sv["diffusion"], boundary=d_boundary,
                     stiffness=d_rate / self.contact.damping, x0=lam)
 
