@@ -208,10 +208,10 @@ def stage_bytes(stage: str, cells: float, nodes: float, launches: int, daughters
     """Algorithmic (compulsory) bytes a stage moves, summed over its launches."""
     if stage == "sor":  # per colour launch: read the field once, n_eff and write the colour's half
         return launches * 8.0 * nodes
-    if stage == "deposit":  # position + state per cell (the atomics stay in L2)
-        return 16.0 * cells
-    if stage == "convert":  # read + clear 4 int64 layers, write 4 float layers + n_eff
-        return (32.0 + 32.0 + 16.0 + 4.0) * nodes
+    if stage == "deposit":  # position + state + visiting order per cell, the 32-bit low words cleared
+        return 20.0 * cells + 16.0 * nodes
+    if stage == "convert":  # read the 4 low-word layers, write n_eff
+        return (16.0 + 4.0) * nodes
     if stage == "contact":  # xyzr + id read, position/velocity/count write
         return (16.0 + 4.0 + 12.0 + 12.0 + 4.0) * cells
     if stage == "bin":  # position/radius read, ids + xyzr written

@@ -137,6 +137,23 @@ int wbc_deposit(const wbc_grid_geometry* geom, int32_t n, const float* position,
  * is read. `density` may be NULL when only the combination is wanted. */
 int wbc_density_convert(int64_t nodes, int64_t* accumulator, float inv_voxel_volume, float* density,
                         const float* weights4, float* combined, int32_t clear, void* stream);
+/* The same deposit as wbc_deposit (kernels/field_kernels.py:78-116, the same integer sums) into a
+ * 32-bit accumulator with an exact carry: `accumulator` holds uint32 low words [4][nodes], uint32
+ * high words [4][nodes] and a carry flag (wbc_deposit32_bytes(nodes) bytes, 16-byte aligned); the
+ * value of a state and node is high * 2^32 + low. The call clears the low words first (and the high
+ * words when the previous deposit carried), so the caller never clears it, and it keeps the sums
+ * until the next deposit. `order` (NULL = 0 .. n - 1) is a permutation of the cells to visit, e.g.
+ * the hash grid's sorted ids: the sums do not depend on it, but the atomics of neighbouring cells
+ * then hit nearby lines. Replaces
+ * fields/densities.py:26-43 (CellDensities.deposit's int64 accumulator). */
+size_t wbc_deposit32_bytes(int64_t nodes);
+int wbc_deposit32(const wbc_grid_geometry* geom, int32_t n, const float* position, const int32_t* cell_state,
+                  const int32_t* order, void* accumulator, size_t accumulator_bytes, void* stream);
+/* wbc_density_convert from the 32-bit accumulator, which it leaves as it is (the per-state densities
+ * can be produced later from the same deposit): density[4][nodes] when non-NULL and combined =
+ * sum_k weights4[k] density_k when non-NULL (kernels/field_kernels.py:119-142). */
+int wbc_convert32(int64_t nodes, const void* accumulator, float inv_voxel_volume, float* density,
+                  const float* weights4, float* combined, void* stream);
 /* out = sum_k weights[k] * density[k] (kernels/field_kernels.py:129-142, fields/densities.py:45-50). */
 int wbc_density_combine(int64_t nodes, const float* weights4, const float* density, float* out, void* stream);
 /* Clamped trilinear interpolation at each cell (kernels/field_kernels.py:153-182). */

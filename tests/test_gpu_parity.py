@@ -88,7 +88,53 @@ def test_deposit_bitwise_equals_oracle_and_golden(golden):
     d_ref, _ = orc.density_convert(ogeom, acc_ref)
     np.testing.assert_array_equal(dens.numpy(), d_ref)
     np.testing.assert_allclose(dens.numpy(), g["density"], atol=1e-8)
-    assert int(dens.accumulator.abs().sum().item()) == 0  # cleared by the conversion
+    # the next deposit replaces the sums (the accumulator is cleared by the deposit itself)
+    dens.deposit_fixed_point(pop)
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), acc_ref)
+
+
+def test_deposit_carry_into_high_words_is_exact():
+    """300 cells on one node put 300 * 2^24 > 2^32 into its state-0 word: the 32-bit accumulator
+    carries into the high word and the sums and densities equal the oracle's int64 ones."""
+    geom = GridGeometry((0.0, 0.0, 0.0), 10.0, (6, 6, 6))
+    rng = np.random.default_rng(12)
+    pos = np.concatenate([np.full((300, 3), 20.0), rng.uniform(5.0, 45.0, (500, 3))]).astype(np.float32)
+    states = np.concatenate([np.zeros(300), rng.integers(0, 4, 500)]).astype(np.int32)
+    pop = _pop_from(pos, states)
+    dens = CellDensities(geom, device=DEV)
+    dens.deposit_fixed_point(pop)
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    acc_ref = orc.deposit(ogeom, pos, states)
+    assert acc_ref.max() > 2**32
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), acc_ref)
+    d_ref, _ = orc.density_convert(ogeom, acc_ref)
+    np.testing.assert_array_equal(dens.numpy(), d_ref)
+    # a following deposit without the crowded node clears the high words again
+    dens.deposit_fixed_point(_pop_from(pos[300:], states[300:]))
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), orc.deposit(ogeom, pos[300:], states[300:]))
+
+
+def test_deposit_in_hash_grid_order_and_lazy_densities():
+    """The deposit visits the cells in the order of the last binning (same sums), and the plain
+    oxygen step's consuming density alone gives the per-state densities later from the same deposit."""
+    pos = uniform_ball(30000, 250.0, seed=8)
+    states = np.random.default_rng(8).integers(0, 4, 30000).astype(np.int32)
+    geom = GridGeometry.centered_cube(600.0, 15.0)
+    pop = _pop_from(pos, states)
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    acc_ref = orc.deposit(ogeom, pos, states)
+    grid = make_neighbor_grid(ContactParams(stiffness=1.0, damping=1.0, max_radius=10.0), DEV)
+    grid.build(pop)
+    order = pop.spatial_order()
+    assert order is not None and torch.equal(order[:pop.count].sort().values.cpu(), torch.arange(pop.count).int())
+    dens = CellDensities(geom, device=DEV)
+    dens.deposit_fixed_point(pop)
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), acc_ref)
+    combined = torch.empty(geom.shape, dtype=torch.float32, device=DEV)
+    dens.convert_combined((1.0, 1.0, 1.0, 0.0), combined)
+    d_ref, c_ref = orc.density_convert(ogeom, acc_ref, (1.0, 1.0, 1.0, 0.0))
+    np.testing.assert_array_equal(combined.cpu().numpy(), c_ref)
+    np.testing.assert_array_equal(dens.numpy(), d_ref)
 
 
 def test_deposit_large_is_order_independent_and_reproducible():

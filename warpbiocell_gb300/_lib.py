@@ -255,6 +255,9 @@ SIGNATURES: dict[str, list] = {
                                 POINTER(SorReportC), _P],
     "wbc_adjoint_cells": [POINTER(GridGeometryC), _I, _P, _P, _P, _F, _P, _P, _P],
     "wbc_contact_steps_workspace_bytes": [_I, c_int64, _I],
+    "wbc_deposit32_bytes": [c_int64],
+    "wbc_deposit32": [POINTER(GridGeometryC), _I, _P, _P, _P, _P, c_size_t, _P],
+    "wbc_convert32": [c_int64, _P, _F, _P, _P, _P, _P],
     "wbc_contact_steps": [POINTER(NeighborGridC), _I, _F, _F, _F, _I, _P, _P, _P, _P, _P, _P, _P, _I, _I, _I, _I, _P,
                           c_size_t, _I, _P],
     "wbc_adjoint_steps": [POINTER(NeighborGridC), _I, _F, _F, _F, _I, _I, _P, _P, _P, _I, _P, c_size_t, _I, _P],
@@ -284,7 +287,8 @@ SIGNATURES: dict[str, list] = {
 _RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64,
             "wbc_sor_solve_workspace_bytes": c_size_t, "wbc_sor_batch_plan_bytes": c_size_t,
             "wbc_batch_plan_bytes": c_size_t,
-    "wbc_contact_steps_workspace_bytes": c_size_t}
+    "wbc_contact_steps_workspace_bytes": c_size_t,
+    "wbc_deposit32_bytes": c_size_t}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

@@ -44,6 +44,9 @@ class CellPopulation:
     # scratch of commit_divisions: scan partials and the device-side daughter total
     _scan_workspace: torch.Tensor | None = None
     _daughters: torch.Tensor | None = None
+    # the hash grid's sorted slot ids of the last binning and the cell count they cover
+    _spatial_ids: torch.Tensor | None = None
+    _spatial_count: int = -1
 
     @classmethod
     def from_numpy(
@@ -106,6 +109,19 @@ class CellPopulation:
         return pop
 
     # ---- scratch -------------------------------------------------------------------------------
+    def note_spatial_order(self, sorted_ids: torch.Tensor) -> None:
+        """Record the slots in hash-grid order after a binning of the active prefix."""
+        self._spatial_ids = sorted_ids
+        self._spatial_count = self.count
+
+    def spatial_order(self) -> torch.Tensor | None:
+        """The active slots in the order of the last binning (a permutation of [0, count), cells
+        that are neighbours in space next to one another), or None when the population changed
+        size since; kernels whose result does not depend on the visiting order use it for locality."""
+        if self._spatial_ids is None or self._spatial_count != self.count:
+            return None
+        return self._spatial_ids
+
     def scan_workspace(self) -> tuple[torch.Tensor, torch.Tensor]:
         """Scan partials (capacity-sized, allocated once) and the int32 daughter total."""
         if self._scan_workspace is None:

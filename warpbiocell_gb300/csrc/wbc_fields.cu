@@ -12,6 +12,8 @@
 // Layout: fields are float[nx][ny][nz] with k fastest; the accumulator is int64[4][nodes].
 // Every float expression is evaluated in the reference's order (no contraction, see
 // wbc_common.cuh), so the field after a given number of sweeps is bit-identical to the oracle's.
+#include <algorithm>
+
 #include "wbc_bodies.cuh"
 
 namespace wbc {
@@ -26,6 +28,91 @@ __global__ void k_convert(int64_t nodes, long long* __restrict__ acc, float inv_
                           float w0, float w1, float w2, float w3, float* __restrict__ combined, int clear) {
     int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (node < nodes) convert_node(nodes, node, acc, inv_vol, density, w0, w1, w2, w3, combined, clear);
+}
+
+// ---- 32-bit deposit with an exact carry -------------------------------------------------------------
+// The same integer sums as the int64 accumulator, in half the bytes: each state layer is a uint32
+// low word per node; an add that wraps it increments the node's high word and raises a carry
+// flag, so value = high * 2^32 + low exactly, and the conversion reads the high words only when
+// some add wrapped (a node would need contributions worth more than 256 whole cells for that). The
+// cells are visited in the order given (the hash grid's, so that a warp's cells are neighbours in
+// space and their atomics hit nearby lines).
+// (Combining the lanes' additions first, by warp matching or in a shared-memory tile, was slower:
+// at about half a cell per grid cell a node receives only a few contributions, which rarely
+// share a warp or a block.)
+
+// the high words cleared when the previous deposit carried (otherwise they are all zero already)
+__global__ void k_deposit32_clear_high(int64_t words, uint32_t* __restrict__ hi, const uint32_t* __restrict__ carry) {
+    if (*carry == 0u) return;
+    for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < words;
+         q += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        hi[q] = 0u;
+}
+
+__global__ void k_deposit32(wbc_grid_geometry g, int32_t n, const float* __restrict__ position,
+                            const int32_t* __restrict__ cell_state, const int32_t* __restrict__ order,
+                            uint32_t* __restrict__ lo, uint32_t* __restrict__ hi, uint32_t* __restrict__ carry) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
+    // the cell rule and weights of deposit_cell (kernels/field_kernels.py:78-116)
+    bool ok = t < n;
+    int s = 0, i0 = 0, j0 = 0, k0 = 0;
+    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
+    if (ok) {
+        const int c = order ? order[t] : t;
+        s = cell_state[c];
+        const float* p = position + 3 * static_cast<int64_t>(c);
+        const float ux = (p[0] - g.origin_x) * g.inv_dx;
+        const float uy = (p[1] - g.origin_y) * g.inv_dx;
+        const float uz = (p[2] - g.origin_z) * g.inv_dx;
+        i0 = static_cast<int>(floorf(ux));
+        j0 = static_cast<int>(floorf(uy));
+        k0 = static_cast<int>(floorf(uz));
+        ok = s >= 0 && s < 4 && i0 >= 0 && j0 >= 0 && k0 >= 0 && i0 + 1 < g.nx && j0 + 1 < g.ny && k0 + 1 < g.nz;
+        fx = ux - static_cast<float>(i0);
+        fy = uy - static_cast<float>(j0);
+        fz = uz - static_cast<float>(k0);
+    }
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+        const float wx = di == 0 ? 1.0f - fx : fx;
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) {
+            const float wy = dj == 0 ? 1.0f - fy : fy;
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const float wz = dk == 0 ? 1.0f - fz : fz;
+                const float w = wx * wy * wz;
+                if (ok) {
+                    const unsigned int q = static_cast<unsigned int>(static_cast<int>(w * kFixedOne + 0.5f));
+                    const int64_t key = s * nodes + (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + (k0 + dk);
+                    const unsigned int old = atomicAdd(lo + key, q);
+                    if (old + q < old) {
+                        atomicAdd(hi + key, 1u);
+                        atomicOr(carry, 1u);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// density_s = value_s / 2^24 * inv_vol (value_s = high * 2^32 + low) per state, as convert_node.
+__global__ void k_convert32(int64_t nodes, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi,
+                            const uint32_t* __restrict__ carry, float inv_vol, float* __restrict__ density, float w0,
+                            float w1, float w2, float w3, float* __restrict__ combined) {
+    const int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (node >= nodes) return;
+    const bool wide = *carry != 0u;
+    float d[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        long long a = static_cast<long long>(lo[s * nodes + node]);
+        if (wide) a += static_cast<long long>(hi[s * nodes + node]) << 32;
+        d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
+        if (density) density[s * nodes + node] = d[s];
+    }
+    if (combined) combined[node] = w0 * d[0] + w1 * d[1] + w2 * d[2] + w3 * d[3];
 }
 
 __global__ void k_combine(int64_t nodes, float w0, float w1, float w2, float w3, const float* __restrict__ density,
@@ -236,6 +323,59 @@ int wbc_ftcs_step(const wbc_sor_params* p, float dt, const int32_t* fixed, const
     k_ftcs<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(*p, dt, fixed, density, production, source, field_in,
                                                                 field_out);
     return check_launch("wbc_ftcs_step");
+}
+
+
+size_t wbc_deposit32_bytes(int64_t nodes) {
+    // low words, high words ([4][nodes] uint32 each), then the carry flag
+    return nodes < 0 ? 0 : static_cast<size_t>(8 * 4 * nodes + 256);
+}
+
+int wbc_deposit32(const wbc_grid_geometry* geom, int32_t n, const float* position, const int32_t* cell_state,
+                  const int32_t* order, void* accumulator, size_t accumulator_bytes, void* stream) {
+    if (!geom_ok(geom) || n < 0 || !accumulator || (n > 0 && (!position || !cell_state))) return WBC_ERR_INVALID;
+    const int64_t nodes = static_cast<int64_t>(geom->nx) * geom->ny * geom->nz;
+    if (accumulator_bytes < wbc_deposit32_bytes(nodes) || reinterpret_cast<uintptr_t>(accumulator) % 16 != 0)
+        return WBC_ERR_WORKSPACE;
+    if (4 * nodes >= (1ll << 32) - 1) {
+        set_error_msg("wbc_deposit32: more than 2^32 - 2 state-node words");
+        return WBC_ERR_INVALID;
+    }
+    uint32_t* lo = static_cast<uint32_t*>(accumulator);
+    uint32_t* hi = lo + 4 * nodes;
+    uint32_t* carry = hi + 4 * nodes;
+    cudaStream_t s = as_stream(stream);
+    const int64_t words = 4 * nodes;
+    const int64_t want = (words + 4 * kThreads - 1) / (4 * kThreads);
+    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 65535)));
+    cudaError_t err = cudaMemsetAsync(lo, 0, static_cast<size_t>(words) * sizeof(uint32_t), s);
+    if (err != cudaSuccess) {
+        set_error("wbc_deposit32: cudaMemsetAsync", err);
+        return WBC_ERR_CUDA;
+    }
+    k_deposit32_clear_high<<<blocks, kThreads, 0, s>>>(words, hi, carry);
+    err = cudaMemsetAsync(carry, 0, sizeof(uint32_t), s);
+    if (err != cudaSuccess) {
+        set_error("wbc_deposit32: cudaMemsetAsync", err);
+        return WBC_ERR_CUDA;
+    }
+    if (n > 0) k_deposit32<<<grid_for(n), kThreads, 0, s>>>(*geom, n, position, cell_state, order, lo, hi, carry);
+    return check_launch("wbc_deposit32", n > 0 ? 2 : 1);
+}
+
+int wbc_convert32(int64_t nodes, const void* accumulator, float inv_voxel_volume, float* density,
+                  const float* weights4, float* combined, void* stream) {
+    if (nodes < 0 || !accumulator || (combined && !weights4)) return WBC_ERR_INVALID;
+    if (nodes == 0) return WBC_OK;
+    const uint32_t* lo = static_cast<const uint32_t*>(accumulator);
+    const uint32_t* hi = lo + 4 * nodes;
+    const uint32_t* carry = hi + 4 * nodes;
+    float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (weights4)
+        for (int k = 0; k < 4; ++k) w[k] = weights4[k];
+    k_convert32<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, lo, hi, carry, inv_voxel_volume, density,
+                                                                     w[0], w[1], w[2], w[3], combined);
+    return check_launch("wbc_convert32");
 }
 
 }  // extern "C"

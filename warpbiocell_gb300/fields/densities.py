@@ -1,9 +1,15 @@
 """Per-state cell number densities on the grid (reference: fields/densities.py:13-56).
 
-``deposit`` adds every cell's trilinear weights as int64 fixed point (2^24 per cell) into
-``accumulator[state]`` with ``wbc_deposit`` — integer atomics, so the result is bit-exact and
-independent of thread order — then converts to ``density[state]`` [cells/um^3]. The conversion
-also clears the accumulator for the next deposit, so no separate memset pass is needed.
+``deposit_fixed_point`` adds every cell's trilinear weights as fixed point (2^24 per cell) into a
+32-bit accumulator with an exact carry into high words (``wbc_deposit32``): integer atomics, so
+the sums are bit-exact and independent of thread order, the same as the reference's int64
+accumulator in half the bytes. The cells are visited in the hash grid's order when the population
+was binned at its current size, so that the atomics of a warp's cells hit nearby lines. The call
+clears the accumulator first; it then keeps the deposit until the next one.
+
+``convert`` produces the per-state densities [cells/um^3] (and optionally a weighted combination
+in the same pass); ``convert_combined`` produces only the combination, for the plain oxygen step,
+and leaves the per-state densities to be produced from the same deposit when ``density`` is read.
 """
 
 from __future__ import annotations
@@ -26,34 +32,64 @@ class CellDensities:
             raise RuntimeError("combine_densities assumes four cell states")
         self.geometry = geometry
         self.device = _lib.resolve_device(device)
-        shape = (NUM_STATES, *geometry.shape)
-        self._accumulator = torch.zeros(shape, dtype=torch.int64, device=self.device)
-        self.density = torch.zeros(shape, dtype=torch.float32, device=self.device)
+        nodes = geometry.node_count
+        nbytes = int(_lib.load().wbc_deposit32_bytes(nodes))
+        raw = torch.zeros(nbytes + 16, dtype=torch.uint8, device=self.device)
+        off = (-raw.data_ptr()) % 16
+        self._acc = raw[off:off + nbytes]
+        self._planes = torch.zeros((NUM_STATES, *geometry.shape), dtype=torch.float32, device=self.device)
+        self._planes_current = True  # the planes hold the densities of the latest deposit
         self._native = geometry.native()
+
+    # ---- views ---------------------------------------------------------------------------------
+    @property
+    def density(self) -> torch.Tensor:
+        """Per-state densities of the latest deposit, (4, nx, ny, nz) float32."""
+        if not self._planes_current:
+            self._convert(self._planes, None, None)
+            self._planes_current = True
+        return self._planes
 
     @property
     def accumulator(self) -> torch.Tensor:
-        """The int64 fixed-point accumulator (zero between deposits)."""
-        return self._accumulator
+        """The latest deposit's fixed-point sums as int64 (4, nx, ny, nz) (a copy, for inspection)."""
+        words = 4 * self.geometry.node_count
+        u32 = self._acc[: 8 * words].view(torch.int32)
+        lo = u32[:words].to(torch.int64) & 0xFFFFFFFF
+        hi = u32[words:].to(torch.int64)
+        carry = int(self._acc[8 * words: 8 * words + 4].view(torch.int32).item())
+        value = lo + (hi << 32) if carry else lo
+        return value.reshape(NUM_STATES, *self.geometry.shape)
 
+    # ---- deposit and conversion ------------------------------------------------------------------
     def deposit_fixed_point(self, population) -> None:
-        """Add the cells' weights to the (cleared) accumulator without converting."""
+        """Replace the accumulator's contents with the cells' weights (without converting)."""
         if population.device != self.device:
             raise RuntimeError("population and CellDensities must live on the same device")
-        if population.count > 0:
-            with profiling.stage("deposit"):
-                _lib.call("wbc_deposit", ctypes.byref(self._native), population.count, _lib.ptr(population.position),
-                          _lib.ptr(population.cell_state), _lib.ptr(self._accumulator), _lib.stream(self.device))
+        order = population.spatial_order()
+        with profiling.stage("deposit", launches=2):
+            _lib.call("wbc_deposit32", ctypes.byref(self._native), population.count, _lib.ptr(population.position),
+                      _lib.ptr(population.cell_state), _lib.ptr(order), _lib.ptr(self._acc), self._acc.numel(),
+                      _lib.stream(self.device))
+        self._planes_current = False
 
-    def convert(self, weights=None, combined: torch.Tensor | None = None) -> None:
-        """density = acc / 2^24 / dx^3 (and optionally combined = sum_k w_k density_k); clears acc."""
+    def _convert(self, density, weights, combined) -> None:
         w = None
         if weights is not None:
             w = (ctypes.c_float * 4)(*[float(x) for x in weights])
         with profiling.stage("convert"):
-            _lib.call("wbc_density_convert", self.geometry.node_count, _lib.ptr(self._accumulator),
-                      1.0 / self.geometry.voxel_volume, _lib.ptr(self.density), w, _lib.ptr(combined), 1,
-                      _lib.stream(self.device))
+            _lib.call("wbc_convert32", self.geometry.node_count, _lib.ptr(self._acc), 1.0 / self.geometry.voxel_volume,
+                      _lib.ptr(density), w, _lib.ptr(combined), _lib.stream(self.device))
+
+    def convert(self, weights=None, combined: torch.Tensor | None = None) -> None:
+        """density = acc / 2^24 / dx^3 (and optionally combined = sum_k w_k density_k)."""
+        self._convert(self._planes, weights, combined)
+        self._planes_current = True
+
+    def convert_combined(self, weights, combined: torch.Tensor) -> None:
+        """Only ``combined = sum_k weights[k] density_k``; the per-state densities are produced from
+        the same deposit if and when ``density`` is read."""
+        self._convert(None, weights, combined)
 
     def deposit(self, population) -> None:
         self.deposit_fixed_point(population)
@@ -67,6 +103,11 @@ class CellDensities:
         w = (ctypes.c_float * 4)(*weights)
         _lib.call("wbc_density_combine", self.geometry.node_count, w, _lib.ptr(self.density), _lib.ptr(out),
                   _lib.stream(self.device))
+
+    def planes_for_writing(self) -> torch.Tensor:
+        """The per-state density planes, for a caller that writes them itself (the batched step)."""
+        self._planes_current = True
+        return self._planes
 
     def numpy(self) -> np.ndarray:
         return self.density.cpu().numpy().copy()

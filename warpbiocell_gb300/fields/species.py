@@ -133,10 +133,13 @@ class SpeciesField:
         """Deposit the per-state densities (when this species owns them) and combine them."""
         if self.owns_densities:
             self.densities.deposit_fixed_point(population)
-            # One pass: per-state densities + this species' consuming density, accumulator cleared.
-            self.densities.convert(self.species.uptake_weights, self.density)
             if self.species.produces:
+                # per-state densities and this species' consuming density in one pass, then production
+                self.densities.convert(self.species.uptake_weights, self.density)
                 self.densities.combine(self.species.production, self.production)
+            else:
+                # only the consuming density; the per-state densities when someone reads them
+                self.densities.convert_combined(self.species.uptake_weights, self.density)
             return
         self.combine()
 

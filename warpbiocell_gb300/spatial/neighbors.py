@@ -79,3 +79,5 @@ class NeighborGrid:
         with profiling.stage("bin", launches=6):
             _lib.call("wbc_grid_build", ctypes.byref(self._struct), population.count, _lib.ptr(population.position),
                       _lib.ptr(population.radius), _lib.stream(self.device))
+        if hasattr(population, "note_spatial_order"):
+            population.note_spatial_order(self.sorted_id)
