@@ -273,3 +273,41 @@ def test_reference_configuration_files_load_with_their_values():
     assert net.network.enabled and net.network.update == "asynchronous" and net.network.updates_per_step == 200
     spec = load_sweep(REFERENCE_CONFIGS / "sweeps" / "oxygen_boundary.yaml")
     assert len(list(spec.runs())) == 15  # 5 boundary values x seeds [0, 1, 2]
+
+
+def test_run_directory_tables_and_metadata(tmp_path):
+    """The run directory's files, CSV headers and rows, and the metadata life cycle (reference:
+    io/run_output.py): the column names are the format's contract."""
+    import csv
+    import json
+
+    from warpbiocell_gb300.io.run_output import METRIC_COLUMNS, PROFILE_COLUMNS, RunOutput, make_run_dir
+
+    first = make_run_dir(tmp_path, "demo")
+    second = make_run_dir(tmp_path, "demo")
+    assert first != second and first.is_dir() and second.is_dir() and first.name.endswith("_demo")
+
+    cfg = config_from_dict({"name": "demo"}).to_dict()
+    out = RunOutput(first, None, cfg, "cpu", seed=5)
+    assert (first / "checkpoint").is_dir() and (first / "config.yaml").exists()
+    out.write_metrics({"time_h": 0.0, "cells": 10, "not_a_column": 1})
+    profile = {"r_outer": np.array([20.0, 40.0]), "cells": np.array([3, 7]), "oxygen_mean": np.array([30.0, 35.0]),
+               "lactate_mean": np.array([1.0, 2.0]),
+               **{f"fraction_{s}": np.array([0.5, 0.25]) for s in ("proliferative", "quiescent", "hypoxic", "dead")}}
+    out.write_profile(1.5, profile)
+    meta = json.loads((first / "metadata.json").read_text())
+    assert meta["status"] == "running" and meta["seed"] == 5 and meta["config"]["name"] == "demo"
+    out.finish("completed", 2.0, {"cells": 10})
+    meta = json.loads((first / "metadata.json").read_text())
+    assert meta["status"] == "completed" and meta["wall_s"] == 2.0 and meta["summary"] == {"cells": 10}
+    assert out.checkpoint_path(1.5).name == "state_0001.50h.npz"
+
+    with (first / "metrics.csv").open() as f:
+        rows = list(csv.DictReader(f))
+    assert list(rows[0]) == METRIC_COLUMNS and rows[0]["cells"] == "10" and rows[0]["wall_s"] == ""
+    with (first / "profiles.csv").open() as f:
+        rows = list(csv.DictReader(f))
+    assert list(rows[0]) == PROFILE_COLUMNS and len(rows) == 2
+    assert rows[1]["shell"] == "1" and rows[1]["cells"] == "7" and rows[1]["r_outer_um"] == "40.0"
+    assert rows[0]["glucose_mean_mM"] == "" and rows[0]["lactate_mean_mM"] == "1.0"
+    assert rows[0]["time_h"] == "1.5" and rows[0]["fraction_dead"] == "0.5"

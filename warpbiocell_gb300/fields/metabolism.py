@@ -1,10 +1,12 @@
-"""Several diffusible species on one grid, sharing the per-state cell densities
-(reference: fields/metabolism.py:27-111).
+"""Several diffusible species on one grid that share one deposit of the per-state cell densities
+(reference: fields/metabolism.py:27-111, whose class names, constructor parameters and report
+properties these keep).
 
-Oxygen is always first (the lifecycle reads ``oxygen_local``); glucose, when present, is sampled
-into ``glucose_local``; other species into ``population.extra_local[name]``. Species are solved
-in list order and may take their production source from an earlier species (lactate from
-glucose).
+The species are kept in solve order, oxygen first. Each species is coupled to the cells through
+its own per-state uptake (and production) weights over the shared densities; a species whose
+production is scaled by another species' concentration (lactate from glucose) must come after it,
+and reads that species' freshly solved field. Oxygen samples into ``oxygen_local``, glucose into
+``glucose_local`` and any other species into ``population.extra_local[name]``.
 """
 
 from __future__ import annotations
@@ -13,7 +15,7 @@ from dataclasses import dataclass
 
 from warpbiocell_gb300 import _lib
 from warpbiocell_gb300.fields.densities import CellDensities
-from warpbiocell_gb300.fields.diffusion import SolverSettings
+from warpbiocell_gb300.fields.diffusion import SolveReport, SolverSettings
 from warpbiocell_gb300.fields.oxygen import OxygenField, OxygenParams
 from warpbiocell_gb300.fields.scalar_field import Boundary, GridGeometry
 from warpbiocell_gb300.fields.species import SpeciesField, SpeciesParams
@@ -21,19 +23,25 @@ from warpbiocell_gb300.fields.species import SpeciesField, SpeciesParams
 
 @dataclass(frozen=True)
 class MetabolicReport:
+    """The solve reports of one update, by species name; the aggregate properties summarise them
+    (total sweeps, worst residual, all converged)."""
+
     reports: dict
+
+    def _all(self) -> list[SolveReport]:
+        return list(self.reports.values())
 
     @property
     def sweeps(self) -> int:
-        return sum(r.sweeps for r in self.reports.values())
+        return sum(report.sweeps for report in self._all())
 
     @property
     def residual(self) -> float:
-        return max(r.residual for r in self.reports.values())
+        return max(report.residual for report in self._all())
 
     @property
     def converged(self) -> bool:
-        return all(r.converged for r in self.reports.values())
+        return all(report.converged for report in self._all())
 
 
 class MetabolicFields:
@@ -43,25 +51,29 @@ class MetabolicFields:
                  fixed_outside=None, oxygen_state_factors: dict | None = None):
         self.device = _lib.resolve_device(device)
         self.densities = CellDensities(geometry, device=self.device)
+        # what every further species is built with
+        self._field_options = dict(settings=settings, boundary=boundary, device=self.device,
+                                   fixed_outside=fixed_outside, densities=self.densities)
         self.oxygen = OxygenField(geometry, oxygen_params, settings, boundary=boundary, device=self.device,
                                   fixed_outside=fixed_outside, densities=self.densities,
                                   uptake_state_factors=oxygen_state_factors)
         self.species_fields: dict[str, SpeciesField] = {"oxygen": self.oxygen}
-        self._settings, self._boundary, self._fixed_outside = settings, boundary, fixed_outside
+        self._sources: dict[str, SpeciesField | None] = {"oxygen": None}
         for params in species:
             self.add_species(params)
         self.last_report: MetabolicReport | None = None
 
     def add_species(self, params: SpeciesParams) -> SpeciesField:
-        """Append a species after oxygen (and after any species it takes its production from)."""
+        """Append a species to the solve order (its production source, if any, must already be there)."""
         if params.name in self.species_fields:
             raise ValueError(f"duplicate species {params.name!r}")
-        if params.production_source is not None and params.production_source not in self.species_fields:
-            raise ValueError(f"species {params.name!r}: production source {params.production_source!r} must be an earlier species")
-        fld = SpeciesField(self.geometry, params, self._settings, boundary=self._boundary, device=self.device,
-                           fixed_outside=self._fixed_outside, densities=self.densities)
-        self.species_fields[params.name] = fld
-        return fld
+        source = params.production_source
+        if source is not None and source not in self.species_fields:
+            raise ValueError(f"species {params.name!r}: production source {source!r} must be an earlier species")
+        added = SpeciesField(self.geometry, params, **self._field_options)
+        self.species_fields[params.name] = added
+        self._sources[params.name] = None if source is None else self.species_fields[source]
+        return added
 
     @property
     def geometry(self) -> GridGeometry:
@@ -82,14 +94,14 @@ class MetabolicFields:
         return self.species_fields[name]
 
     def update(self, population) -> MetabolicReport:
-        """Deposit the per-state densities once, then combine, solve and sample every species in order."""
+        """One deposit for all species, then, in order, each species' coupling, steady solve and
+        sampling at the cells."""
         self.densities.deposit(population)
-        reports = {}
+        reports: dict[str, SolveReport] = {}
         for name, species in self.species_fields.items():
             species.combine()
-            source = self.species_fields[species.species.production_source] if species.species.production_source else None
-            reports[name] = species.solve_steady_state(source)
+            reports[name] = species.solve_steady_state(self._sources[name])
             species.sample_at_cells(population)
-        self.last_report = MetabolicReport(reports)
         self.oxygen.last_report = reports["oxygen"]
+        self.last_report = MetabolicReport(reports)
         return self.last_report

@@ -1,10 +1,12 @@
-"""Synthetic tissue shapes as signed-distance functions, negative inside (reference:
-geometry/shapes.py). Lengths in um.
+"""Analytical tissue shapes as signed distances (negative inside), in um, for tissue regions
+(reference: geometry/shapes.py, whose class names, fields and defaults these keep).
 
-The sphere and the union (minimum of the members' distances) are exact. The ellipsoid uses the
-first-order distance of its implicit function f = |((x - c) / a)| - 1, namely k1 (k1 - 1) / k2
-with k1 = |(x - c) / a| and k2 = |(x - c) / a^2|: exact on the axes, a few percent off elsewhere
-for moderate aspect ratios; at the centre (k2 = 0) it is minus the smallest semi-axis.
+Every shape answers three questions: the signed distance at points, the axis-aligned box that
+contains it, and its volume. The sphere's distance is exact. For the ellipsoid with semi-axes
+a the distance is the first-order estimate of its implicit function |(x - c) / a| - 1,
+g (g - 1) / |(x - c) / a^2| with g = |(x - c) / a| (exact on the axes, within a few percent
+elsewhere for moderate aspect ratios; at the centre, where the gradient vanishes, it is minus the
+smallest semi-axis). A union is the pointwise minimum of its members' distances.
 """
 
 from __future__ import annotations
@@ -16,23 +18,43 @@ import numpy as np
 from warpbiocell_gb300.fields.scalar_field import GridGeometry
 
 
+def _norm(u, v, w):
+    return np.sqrt(u**2 + v**2 + w**2)
+
+
+def _relative(center, scale, x, y, z):
+    """The coordinates relative to ``center``, each divided by its ``scale``."""
+    return [(q - c) / s for q, c, s in zip((x, y, z), center, scale)]
+
+
+class _Shape:
+    """Shared helpers of the shapes (each defines ``sdf``, ``bounds`` and ``volume``)."""
+
+    def sdf_points(self, points: np.ndarray) -> np.ndarray:
+        """Signed distance at an (..., 3) array of points."""
+        points = np.asarray(points, dtype=float)
+        return self.sdf(points[..., 0], points[..., 1], points[..., 2])
+
+    def contains(self, points: np.ndarray) -> np.ndarray:
+        return self.sdf_points(points) < 0.0
+
+
 @dataclass(frozen=True)
-class Sphere:
+class Sphere(_Shape):
     center: tuple[float, float, float] = (0.0, 0.0, 0.0)
     radius: float = 200.0
 
     def __post_init__(self):
-        if self.radius <= 0.0:
+        if not self.radius > 0.0:
             raise ValueError("radius must be positive")
 
     def sdf(self, x, y, z) -> np.ndarray:
-        c = self.center
-        return np.sqrt((x - c[0]) ** 2 + (y - c[1]) ** 2 + (z - c[2]) ** 2) - self.radius
+        return _norm(*_relative(self.center, (1.0, 1.0, 1.0), x, y, z)) - self.radius
 
     @property
     def bounds(self) -> tuple[np.ndarray, np.ndarray]:
-        c = np.asarray(self.center, dtype=float)
-        return c - self.radius, c + self.radius
+        half = np.full(3, float(self.radius))
+        return np.asarray(self.center, dtype=float) - half, np.asarray(self.center, dtype=float) + half
 
     @property
     def volume(self) -> float:
@@ -40,55 +62,59 @@ class Sphere:
 
 
 @dataclass(frozen=True)
-class Ellipsoid:
+class Ellipsoid(_Shape):
     center: tuple[float, float, float] = (0.0, 0.0, 0.0)
     radii: tuple[float, float, float] = (300.0, 200.0, 150.0)  # semi-axes
 
     def __post_init__(self):
-        if min(self.radii) <= 0.0:
+        if not min(self.radii) > 0.0:
             raise ValueError("semi-axes must be positive")
 
     def sdf(self, x, y, z) -> np.ndarray:
-        c, a = self.center, self.radii
-        u, v, w = (x - c[0]) / a[0], (y - c[1]) / a[1], (z - c[2]) / a[2]
-        k1 = np.sqrt(u**2 + v**2 + w**2)
-        k2 = np.sqrt((u / a[0]) ** 2 + (v / a[1]) ** 2 + (w / a[2]) ** 2)
+        u = _relative(self.center, self.radii, x, y, z)
+        g = _norm(*u)
+        grad = _norm(*(ui / a for ui, a in zip(u, self.radii)))
+        inside_centre = -min(self.radii)
         with np.errstate(divide="ignore", invalid="ignore"):
-            return np.where(k2 > 0.0, k1 * (k1 - 1.0) / k2, -min(a))
+            return np.where(grad > 0.0, g * (g - 1.0) / grad, inside_centre)
 
     @property
     def bounds(self) -> tuple[np.ndarray, np.ndarray]:
-        c = np.asarray(self.center, dtype=float)
-        a = np.asarray(self.radii, dtype=float)
-        return c - a, c + a
+        half = np.asarray(self.radii, dtype=float)
+        return np.asarray(self.center, dtype=float) - half, np.asarray(self.center, dtype=float) + half
 
     @property
     def volume(self) -> float:
-        return 4.0 / 3.0 * np.pi * float(np.prod(self.radii))
+        a, b, c = self.radii
+        return 4.0 / 3.0 * np.pi * float(a * b * c)
 
 
 @dataclass(frozen=True)
-class Union:
+class Union(_Shape):
     shapes: tuple = field(default_factory=tuple)
 
     def __post_init__(self):
-        if not self.shapes:
+        if len(self.shapes) == 0:
             raise ValueError("a union needs at least one shape")
 
     def sdf(self, x, y, z) -> np.ndarray:
-        return np.minimum.reduce([s.sdf(x, y, z) for s in self.shapes])
+        distance = self.shapes[0].sdf(x, y, z)
+        for member in self.shapes[1:]:
+            distance = np.minimum(distance, member.sdf(x, y, z))
+        return distance
 
     @property
     def bounds(self) -> tuple[np.ndarray, np.ndarray]:
-        lows, highs = zip(*(s.bounds for s in self.shapes))
-        return np.minimum.reduce(lows), np.maximum.reduce(highs)
+        boxes = [member.bounds for member in self.shapes]
+        return np.min([lo for lo, _ in boxes], axis=0), np.max([hi for _, hi in boxes], axis=0)
 
     @property
     def volume(self) -> float:
-        return float("nan")  # overlaps unknown: measure it on the grid
+        """Not known analytically (the members may overlap): NaN; measure it on a grid."""
+        return float("nan")
 
 
 def evaluate_on_grid(shape, geometry: GridGeometry) -> np.ndarray:
-    """float32 signed distance at every grid node."""
-    x, y, z = np.meshgrid(*geometry.node_coordinates(), indexing="ij")
-    return shape.sdf(x, y, z).astype(np.float32)
+    """The signed distance at every node of ``geometry``, float32 (nx, ny, nz)."""
+    xs, ys, zs = geometry.node_coordinates()
+    return shape.sdf(xs[:, None, None], ys[None, :, None], zs[None, None, :]).astype(np.float32)

@@ -283,173 +283,204 @@ class ExperimentConfig:
 
     # ---- validation -------------------------------------------------------------------------------
     def validate(self, base_dir: str | Path | None = None) -> list[str]:
-        """Raise ConfigError on an inconsistent configuration; return warnings."""
-        warnings: list[str] = []
-        sim, cells = self.simulation, self.cells
-        if sim.duration_h <= 0.0:
-            raise ConfigError("simulation.duration_h must be positive")
-        if cells.initial_count < 1 or cells.max_cells < cells.initial_count:
-            raise ConfigError("cells.initial_count must be >= 1 and <= cells.max_cells")
-        if cells.radius_um <= 0.0:
-            raise ConfigError("cells.radius_um must be positive")
-        if self.output.metrics_every_h <= 0.0 or self.output.shell_width_um <= 0.0:
-            raise ConfigError("output intervals and shell width must be positive")
-        stepping = self.stepping()
-        self.contact_params().check_substep(stepping.dt_mechanics)
-        self.lifecycle_params()
+        """Raise ConfigError on an inconsistent configuration (ValueError from the parameter
+        objects' own checks); return the warnings about a consistent but doubtful one. The rules
+        and their messages follow reference simulation/config.py:331-422."""
+        checks = [self._check_ranges(), self._check_parameter_objects()]
         if self.oxygen.enabled:
-            warnings += self._validate_fields()
+            checks.append(self._check_fields())
         if self.geometry.enabled:
-            self._validate_geometry()
-            self.contact_params().check_substep(stepping.dt_mechanics)
-        warnings += self._validate_network(base_dir)
-        growth = cells.initial_count * np.exp(self.lifecycle.division_rate_per_h * sim.duration_h)
-        if growth > cells.max_cells and self.lifecycle.phenotype_model == "rules":
-            warnings.append(f"free exponential growth would reach {growth:.0f} cells > max_cells={cells.max_cells}; "
-                            "the run stops with status 'capacity_exceeded' if inhibition and death do not limit it")
-        return warnings
+            checks.append(self._check_geometry())
+        checks += [self._check_network(base_dir), self._check_growth()]
+        return [warning for check in checks for warning in check]
 
-    def _validate_fields(self) -> list[str]:
-        warnings = []
+    def _check_ranges(self) -> list[str]:
+        sim, cells, out = self.simulation, self.cells, self.output
+        _require(sim.duration_h > 0.0, "simulation.duration_h must be positive")
+        _require(1 <= cells.initial_count <= cells.max_cells, "cells.initial_count must be >= 1 and <= cells.max_cells")
+        _require(cells.radius_um > 0.0, "cells.radius_um must be positive")
+        _require(out.metrics_every_h > 0.0 and out.shell_width_um > 0.0,
+                 "output intervals and shell width must be positive")
+        return []
+
+    def _check_parameter_objects(self) -> list[str]:
+        # the contact law's substep bound and the lifecycle's own range checks raise ValueError
+        self.contact_params().check_substep(self.simulation.dt_mechanics_h)
+        self.lifecycle_params()
+        return []
+
+    def _check_fields(self) -> list[str]:
         self.oxygen_params()
         self.solver_settings()
         by_state(self.oxygen.uptake_state_factors or None, default=1.0)
-        names = ["oxygen"]
+        earlier = ["oxygen"]
         for sp in self.species:
-            if not sp.name or sp.name in names:
-                raise ConfigError(f"species need unique, non-empty names other than 'oxygen' (got {sp.name!r})")
-            if sp.production_source is not None and sp.production_source not in names:
-                raise ConfigError(f"species {sp.name!r}: production_source must be an earlier species")
+            _require(bool(sp.name) and sp.name not in earlier,
+                     f"species need unique, non-empty names other than 'oxygen' (got {sp.name!r})")
+            _require(sp.production_source in (None, *earlier),
+                     f"species {sp.name!r}: production_source must be an earlier species")
             sp.params()
-            names.append(sp.name)
+            earlier.append(sp.name)
+        # a random close packing (volume fraction 0.52) of the initial cells must sit inside the
+        # box with one voxel to spare
+        cells, box = self.cells, self.oxygen.grid.box_um
+        packed = cells.radius_um * cells.initial_spacing_factor * (cells.initial_count / 0.52) ** (1.0 / 3.0)
+        _require(packed + self.grid_geometry().dx <= 0.5 * box,
+                 f"initial cluster radius ~{packed:.0f} um does not fit in the {box:.0f} um box with a one-voxel margin")
+        warnings = []
         if self.lifecycle.necrosis_requires_glucose and not self.has_glucose:
             warnings.append("lifecycle.necrosis_requires_glucose is set but there is no species named 'glucose': "
                             "oxygen-only death applies")
-        geom = self.grid_geometry()
-        cells = self.cells
-        cluster = cells.radius_um * cells.initial_spacing_factor * (cells.initial_count / 0.52) ** (1.0 / 3.0)
-        if cluster + geom.dx > 0.5 * self.oxygen.grid.box_um:
-            raise ConfigError(f"initial cluster radius ~{cluster:.0f} um does not fit in the "
-                              f"{self.oxygen.grid.box_um:.0f} um box with a one-voxel margin")
         if self.lifecycle.hypoxia_threshold_mmHg >= self.oxygen.boundary_mmHg:
             warnings.append("hypoxia threshold is at or above the boundary oxygen: every cell will be hypoxic")
         return warnings
 
-    def _validate_geometry(self) -> None:
+    def _check_geometry(self) -> list[str]:
         g = self.geometry
-        if g.oxygen_source not in ("tissue_surface", "box"):
-            raise ConfigError("geometry.oxygen_source must be tissue_surface or box")
-        if len(g.center_um) != 3 or len(g.mask_origin_um) != 3:
-            raise ConfigError("geometry.center_um and mask_origin_um need three components")
+        _require(g.oxygen_source in ("tissue_surface", "box"), "geometry.oxygen_source must be tissue_surface or box")
+        _require(len(g.center_um) == 3 and len(g.mask_origin_um) == 3,
+                 "geometry.center_um and mask_origin_um need three components")
         if g.shape == "mask":
-            if not g.mask_file:
-                raise ConfigError("geometry.shape = mask needs geometry.mask_file")
+            _require(bool(g.mask_file), "geometry.shape = mask needs geometry.mask_file")
         else:
-            if g.shape == "spheres" and not g.spheres:
-                raise ConfigError("geometry.shape = spheres needs a non-empty geometry.spheres list")
+            _require(g.shape != "spheres" or bool(g.spheres),
+                     "geometry.shape = spheres needs a non-empty geometry.spheres list")
             try:
-                shape = self.tissue_shape()
+                lower, upper = self.tissue_shape().bounds
             except ValueError as exc:
                 raise ConfigError(f"geometry: {exc}") from exc
-            geom = self.grid_geometry()
-            lo, hi = shape.bounds
-            if np.any(lo < np.asarray(geom.origin) + geom.dx) or np.any(hi > np.asarray(geom.upper) - geom.dx):
-                raise ConfigError("the tissue shape does not fit in oxygen.grid with a one-voxel margin")
-        if g.seed_within_radius_um is not None and g.seed_within_radius_um <= 0.0:
-            raise ConfigError("geometry.seed_within_radius_um must be positive")
+            grid = self.grid_geometry()
+            inner_lo = np.asarray(grid.origin) + grid.dx
+            inner_hi = np.asarray(grid.upper) - grid.dx
+            _require(bool(np.all(lower >= inner_lo) and np.all(upper <= inner_hi)),
+                     "the tissue shape does not fit in oxygen.grid with a one-voxel margin")
+        _require(g.seed_within_radius_um is None or g.seed_within_radius_um > 0.0,
+                 "geometry.seed_within_radius_um must be positive")
+        return []
 
-    def _validate_network(self, base_dir) -> list[str]:
-        warnings = []
-        n = self.network
-        if self.lifecycle.phenotype_model == "network" and not n.enabled:
-            raise ConfigError("lifecycle.phenotype_model = network needs network.enabled = true")
+    def _check_network(self, base_dir) -> list[str]:
+        n, model = self.network, self.lifecycle.phenotype_model
+        _require(n.enabled or model != "network", "lifecycle.phenotype_model = network needs network.enabled = true")
         if not n.enabled:
-            return warnings
+            return []
         try:
             params = self.network_params(base_dir)
         except (OSError, ValueError) as exc:
             raise ConfigError(f"network: {exc}") from exc
-        available = ["constant"]
-        if self.oxygen.enabled:
-            names = [sp.name for sp in self.species]
-            available += ["oxygen"] + [x for x in names if x == "glucose"] + [x for x in names if x != "glucose"][:2]
+        sources = self._network_sources()
         for clamp in params.inputs:
-            if clamp.source not in available:
-                raise ConfigError(f"network input {clamp.node!r}: source {clamp.source!r} is not one of {available}")
-        clamped = {c.node for c in params.inputs}
-        p_on = {**{node.name: node.p_on for node in params.network.nodes}, **n.initial_states}
-        frozen = [x for x in params.network.input_names if x not in clamped and 0.0 < p_on[x] < 1.0]
-        if frozen:
-            warnings.append(f"network input nodes without a clamp are drawn once and then frozen: {frozen}")
-        if self.lifecycle.phenotype_model == "rules":
+            _require(clamp.source in sources,
+                     f"network input {clamp.node!r}: source {clamp.source!r} is not one of {sources}")
+        warnings = []
+        clamped = {clamp.node for clamp in params.inputs}
+        p_on = {node.name: node.p_on for node in params.network.nodes}
+        p_on.update(n.initial_states)
+        unclamped_random = [name for name in params.network.input_names
+                            if name not in clamped and 0.0 < p_on[name] < 1.0]
+        if unclamped_random:
+            warnings.append(f"network input nodes without a clamp are drawn once and then frozen: {unclamped_random}")
+        if model == "rules":
             warnings.append("the network runs and its fate counts are recorded, but lifecycle.phenotype_model = "
                             "rules decides the phenotypes")
-        elif not any(params.outputs.values()):
-            raise ConfigError("lifecycle.phenotype_model = network needs at least one network output node")
+        else:
+            _require(any(params.outputs.values()),
+                     "lifecycle.phenotype_model = network needs at least one network output node")
         return warnings
+
+    def _network_sources(self) -> list[str]:
+        """What an input clamp can read: a constant, and with the fields on, oxygen, glucose and up
+        to two further species (the runtime's local-value slots)."""
+        if not self.oxygen.enabled:
+            return ["constant"]
+        names = [sp.name for sp in self.species]
+        others = [name for name in names if name != "glucose"][:2]
+        return ["constant", "oxygen", *(["glucose"] if "glucose" in names else []), *others]
+
+    def _check_growth(self) -> list[str]:
+        if self.lifecycle.phenotype_model != "rules":
+            return []
+        cells = self.cells
+        unchecked = cells.initial_count * np.exp(self.lifecycle.division_rate_per_h * self.simulation.duration_h)
+        if unchecked <= cells.max_cells:
+            return []
+        return [f"free exponential growth would reach {unchecked:.0f} cells > max_cells={cells.max_cells}; "
+                "the run stops with status 'capacity_exceeded' if inhibition and death do not limit it"]
 
 
 # ---- loading ------------------------------------------------------------------------------------
 
+def _require(ok: bool, message: str) -> None:
+    if not ok:
+        raise ConfigError(message)
+
+
+# list-valued fields whose items are themselves sections
 _LIST_ITEMS = {(ExperimentConfig, "species"): SpeciesConfig, (NetworkConfig, "inputs"): NetworkInputConfig}
 
 
 def _resolve_path(name, base_dir) -> Path:
+    """``name`` against ``base_dir`` when it is relative and exists there (or nowhere else)."""
     path = Path(name).expanduser()
     if path.is_absolute() or base_dir is None:
         return path
-    candidate = Path(base_dir) / path
-    return candidate if candidate.exists() or not path.exists() else path
+    beside = Path(base_dir) / path
+    return path if path.exists() and not beside.exists() else beside
+
+
+def _as_bool(value, where):
+    _require(isinstance(value, bool), f"{where}: expected true/false, got {value!r}")
+    return value
+
+
+def _as_int(value, where):
+    integral = isinstance(value, (int, float)) and not isinstance(value, bool) and float(value).is_integer()
+    _require(integral, f"{where}: expected an integer, got {value!r}")
+    return int(value)
+
+
+def _as_float(value, where):
+    if isinstance(value, str):  # YAML 1.1 reads 1e-5 (no dot) as a string
+        try:
+            return float(value)
+        except ValueError:
+            raise ConfigError(f"{where}: expected a number, got {value!r}") from None
+    _require(isinstance(value, (int, float)) and not isinstance(value, bool),
+             f"{where}: expected a number, got {value!r}")
+    return float(value)
+
+
+def _as_str(value, where):
+    _require(isinstance(value, str), f"{where}: expected a string, got {value!r}")
+    return value
+
+
+# declared type -> conversion; other annotations (dicts, lists, optionals) pass values through
+_SCALARS = {bool: _as_bool, int: _as_int, float: _as_float, str: _as_str}
+
+
+def _convert(owner, key, declared, value, where):
+    if dataclasses.is_dataclass(declared):
+        return _build(declared, value, where)
+    item = _LIST_ITEMS.get((owner, key))
+    if item is not None:
+        _require(isinstance(value, list), f"{where} must be a list")
+        return [_build(item, entry, f"{where}[{i}]") for i, entry in enumerate(value)]
+    convert = _SCALARS.get(declared)
+    return value if convert is None else convert(value, where)
 
 
 def _build(cls, data, where: str):
-    if not isinstance(data, dict):
-        raise ConfigError(f"{where}: expected a mapping, got {type(data).__name__}")
-    hints = typing.get_type_hints(cls)
-    names = {f.name for f in dataclasses.fields(cls)}
-    unknown = sorted(set(data) - names)
-    if unknown:
-        raise ConfigError(f"{where}: unknown keys {unknown}; valid keys are {sorted(names)}")
-    kwargs = {}
-    for key, value in data.items():
-        target = hints[key]
-        if dataclasses.is_dataclass(target):
-            kwargs[key] = _build(target, value, f"{where}.{key}")
-        elif (cls, key) in _LIST_ITEMS:
-            if not isinstance(value, list):
-                raise ConfigError(f"{where}.{key} must be a list")
-            kwargs[key] = [_build(_LIST_ITEMS[(cls, key)], item, f"{where}.{key}[{i}]") for i, item in enumerate(value)]
-        else:
-            kwargs[key] = _coerce(target, value, f"{where}.{key}")
+    """The dataclass ``cls`` from a mapping; ``where`` names it in errors (``config.oxygen`` ...)."""
+    _require(isinstance(data, dict), f"{where}: expected a mapping, got {type(data).__name__}")
+    declared = typing.get_type_hints(cls)
+    valid = sorted(f.name for f in dataclasses.fields(cls))
+    unknown = sorted(key for key in data if key not in valid)
+    _require(not unknown, f"{where}: unknown keys {unknown}; valid keys are {valid}")
+    values = {key: _convert(cls, key, declared[key], value, f"{where}.{key}") for key, value in data.items()}
     try:
-        return cls(**kwargs)
+        return cls(**values)
     except TypeError as exc:
         raise ConfigError(f"{where}: {exc}") from exc
-
-
-def _coerce(target, value, where):
-    if target is bool:
-        if not isinstance(value, bool):
-            raise ConfigError(f"{where}: expected true/false, got {value!r}")
-        return value
-    if target is int:
-        if isinstance(value, bool) or not isinstance(value, (int, float)) or int(value) != value:
-            raise ConfigError(f"{where}: expected an integer, got {value!r}")
-        return int(value)
-    if target is float:
-        if isinstance(value, str):
-            try:
-                return float(value)
-            except ValueError:
-                raise ConfigError(f"{where}: expected a number, got {value!r}") from None
-        if isinstance(value, bool) or not isinstance(value, (int, float)):
-            raise ConfigError(f"{where}: expected a number, got {value!r}")
-        return float(value)
-    if target is str:
-        if not isinstance(value, str):
-            raise ConfigError(f"{where}: expected a string, got {value!r}")
-        return value
-    return value
 
 
 def config_from_dict(data: dict) -> ExperimentConfig:
@@ -457,19 +488,18 @@ def config_from_dict(data: dict) -> ExperimentConfig:
 
 
 def apply_overrides(data: dict, overrides: list[str]) -> dict:
-    """Apply ``section.key=value`` overrides (values read as YAML) to a nested dict, in place."""
+    """Apply ``section.key=value`` overrides (values read as YAML scalars) to a nested dict, in
+    place, creating missing sections."""
     for item in overrides:
-        if "=" not in item:
-            raise ConfigError(f"override {item!r} must look like section.key=value")
-        key, raw = item.split("=", 1)
-        parts = key.strip().split(".")
-        node = data
-        for part in parts[:-1]:
-            node = node.setdefault(part, {})
-            if not isinstance(node, dict):
-                raise ConfigError(f"override {item!r}: {part} is not a section")
+        dotted, equals, text = item.partition("=")
+        _require(bool(equals), f"override {item!r} must look like section.key=value")
+        *sections, leaf = dotted.strip().split(".")
+        target = data
+        for name in sections:
+            target = target.setdefault(name, {})
+            _require(isinstance(target, dict), f"override {item!r}: {name} is not a section")
         try:
-            node[parts[-1]] = yaml_subset.scalar(raw)
+            target[leaf] = yaml_subset.scalar(text)
         except ValueError as exc:
             raise ConfigError(f"override {item!r}: {exc}") from exc
     return data
@@ -478,10 +508,12 @@ def apply_overrides(data: dict, overrides: list[str]) -> dict:
 def resolve_file_references(data: dict, base_dir: str | Path) -> dict:
     """Make the network model and .cfg names absolute against ``base_dir`` where they exist there."""
     network = data.get("network")
-    if isinstance(network, dict):
-        for key in ("file", "cfg"):
-            if isinstance(network.get(key), str) and network[key]:
-                network[key] = str(_resolve_path(network[key], base_dir))
+    if not isinstance(network, dict):
+        return data
+    for key in ("file", "cfg"):
+        name = network.get(key)
+        if isinstance(name, str) and name:
+            network[key] = str(_resolve_path(name, base_dir))
     return data
 
 
