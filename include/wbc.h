@@ -138,10 +138,12 @@ int wbc_deposit(const wbc_grid_geometry* geom, int32_t n, const float* position,
 int wbc_density_convert(int64_t nodes, int64_t* accumulator, float inv_voxel_volume, float* density,
                         const float* weights4, float* combined, int32_t clear, void* stream);
 /* The same deposit as wbc_deposit (kernels/field_kernels.py:78-116, the same integer sums) into a
- * 32-bit accumulator with an exact carry: `accumulator` holds uint32 low words [4][nodes], uint32
- * high words [4][nodes] and a carry flag (wbc_deposit32_bytes(nodes) bytes, 16-byte aligned); the
- * value of a state and node is high * 2^32 + low. The call clears the low words first (and the high
- * words when the previous deposit carried), so the caller never clears it, and it keeps the sums
+ * 32-bit accumulator with an exact carry: `accumulator` holds uint32 low words L[4][nodes], uint32
+ * wrap counts C[4][nodes] and a carry flag (wbc_deposit32_bytes(nodes) bytes, 16-byte aligned).
+ * The low words are added to in aligned pairs (2m, 2m+1) by 64-bit atomics, so the sum of word w
+ * is L[w] + 2^32 C[w] for even w and L[w] + 2^32 C[w] - C[w-1] for odd w (C is all zero, and the
+ * sums are the low words, while the carry flag is 0). The call clears the low words first (and the
+ * counts when the previous deposit wrapped), so the caller never clears it, and it keeps the sums
  * until the next deposit. `order` (NULL = 0 .. n - 1) is a permutation of the cells to visit, e.g.
  * the hash grid's sorted ids: the sums do not depend on it, but the atomics of neighbouring cells
  * then hit nearby lines. Replaces

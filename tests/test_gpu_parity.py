@@ -94,24 +94,31 @@ def test_deposit_bitwise_equals_oracle_and_golden(golden):
 
 
 def test_deposit_carry_into_high_words_is_exact():
-    """300 cells on one node put 300 * 2^24 > 2^32 into its state-0 word: the 32-bit accumulator
-    carries into the high word and the sums and densities equal the oracle's int64 ones."""
+    """Crowded nodes put more than 2^32 into single words, in every way a paired 64-bit add can
+    wrap: the even word of a pair (300 cells on node (2,2,2), state 0), the odd word alone (300 on
+    (2,2,3)), both words in one add (600 half-way between (3,3,2) and (3,3,3), state 2), and the two
+    halves of neighbouring pairs (600 half-way between (4,1,3) and (4,1,4), state 3). The sums and
+    densities equal the oracle's int64 ones."""
     geom = GridGeometry((0.0, 0.0, 0.0), 10.0, (6, 6, 6))
     rng = np.random.default_rng(12)
-    pos = np.concatenate([np.full((300, 3), 20.0), rng.uniform(5.0, 45.0, (500, 3))]).astype(np.float32)
-    states = np.concatenate([np.zeros(300), rng.integers(0, 4, 500)]).astype(np.int32)
+    crowds = [((20.0, 20.0, 20.0), 300, 0), ((20.0, 20.0, 30.0), 300, 1), ((30.0, 30.0, 25.0), 600, 2),
+              ((40.0, 10.0, 35.0), 600, 3)]
+    pos = np.concatenate([np.tile(np.float32(at), (k, 1)) for at, k, _ in crowds] +
+                         [rng.uniform(5.0, 45.0, (500, 3))]).astype(np.float32)
+    states = np.concatenate([np.full(k, st) for _, k, st in crowds] + [rng.integers(0, 4, 500)]).astype(np.int32)
+    crowded = sum(k for _, k, _ in crowds)
     pop = _pop_from(pos, states)
     dens = CellDensities(geom, device=DEV)
     dens.deposit_fixed_point(pop)
     ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
     acc_ref = orc.deposit(ogeom, pos, states)
-    assert acc_ref.max() > 2**32
+    assert (acc_ref > 2**32).sum() >= 6
     np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), acc_ref)
     d_ref, _ = orc.density_convert(ogeom, acc_ref)
     np.testing.assert_array_equal(dens.numpy(), d_ref)
-    # a following deposit without the crowded node clears the high words again
-    dens.deposit_fixed_point(_pop_from(pos[300:], states[300:]))
-    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), orc.deposit(ogeom, pos[300:], states[300:]))
+    # a following deposit without the crowds clears the wrap counts again
+    dens.deposit_fixed_point(_pop_from(pos[crowded:], states[crowded:]))
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), orc.deposit(ogeom, pos[crowded:], states[crowded:]))
 
 
 def test_deposit_in_hash_grid_order_and_lazy_densities():

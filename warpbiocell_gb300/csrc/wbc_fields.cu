@@ -9,7 +9,8 @@
 //   residual   max-norm of the dimensionless residual, block-reduced    field_kernels.py:215-243
 //   FTCS       explicit reference step (validation only)                field_kernels.py:246-273
 //
-// Layout: fields are float[nx][ny][nz] with k fastest; the accumulator is int64[4][nodes].
+// Layout: fields are float[nx][ny][nz] with k fastest; the int64 accumulator is int64[4][nodes], the
+// 32-bit one uint32 low words [4][nodes], uint32 wrap counts [4][nodes] and a carry flag.
 // Every float expression is evaluated in the reference's order (no contraction, see
 // wbc_common.cuh), so the field after a given number of sweeps is bit-identical to the oracle's.
 #include <algorithm>
@@ -31,27 +32,51 @@ __global__ void k_convert(int64_t nodes, long long* __restrict__ acc, float inv_
 }
 
 // ---- 32-bit deposit with an exact carry -------------------------------------------------------------
-// The same integer sums as the int64 accumulator, in half the bytes: each state layer is a uint32
-// low word per node; an add that wraps it increments the node's high word and raises a carry
-// flag, so value = high * 2^32 + low exactly, and the conversion reads the high words only when
-// some add wrapped (a node would need contributions worth more than 256 whole cells for that). The
-// cells are visited in the order given (the hash grid's, so that a warp's cells are neighbours in
-// space and their atomics hit nearby lines).
+// The same integer sums as the int64 accumulator, in half the bytes. Each state layer is a uint32
+// low word per node, and the low words are added to in aligned pairs (words 2m and 2m+1) by 64-bit
+// atomics: the two z-corners k0, k0+1 of a cell's (i, j) column are adjacent words, so when the
+// first is even one atomic adds both (otherwise two, each adding to one half of a pair). A 64-bit
+// add carries out of the even word into the odd one and out of the pair altogether; the first
+// wrap increments the even word's count c[2m], the second the odd word's count c[2m+1]. With those
+// counts the exact sums are
+//     S[2m]   = low[2m]   + 2^32 c[2m]
+//     S[2m+1] = low[2m+1] + 2^32 c[2m+1] - c[2m]
+// (the pair's 64-bit total is S[2m] + 2^32 S[2m+1] = low + 2^64 c[2m+1]). A carry flag records
+// whether any add wrapped; without one the low words are the sums (a node would need
+// contributions worth 256 whole cells for a wrap). The cells are visited in the order given (the
+// hash grid's, so that a warp's cells are neighbours in space and their atomics hit nearby lines).
 // (Combining the lanes' additions first, by warp matching or in a shared-memory tile, was slower:
 // at about half a cell per grid cell a node receives only a few contributions, which rarely
 // share a warp or a block.)
 
-// the high words cleared when the previous deposit carried (otherwise they are all zero already)
-__global__ void k_deposit32_clear_high(int64_t words, uint32_t* __restrict__ hi, const uint32_t* __restrict__ carry) {
-    if (*carry == 0u) return;
-    for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < words;
-         q += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        hi[q] = 0u;
+// Zeroes the low words, and the wrap counts when the previous deposit wrapped (otherwise they are
+// zero already); `words` is a multiple of 4, the buffers are 16-byte aligned.
+__global__ void k_deposit32_clear(int64_t words, uint4* __restrict__ lo, uint4* __restrict__ count,
+                                  const uint32_t* __restrict__ carry) {
+    const bool wrapped = *carry != 0u;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    const int64_t quads = words / 4;
+    for (int64_t q = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; q < quads;
+         q += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+        lo[q] = zero;
+        if (wrapped) count[q] = zero;
+    }
+}
+
+// adds `add` (low half to word `even`, high half to word `even` + 1) and counts the wraps
+__device__ __forceinline__ void add_pair(uint32_t* lo, uint32_t* count, uint32_t* carry, int64_t even,
+                                         unsigned long long add) {
+    const unsigned long long old = atomicAdd(reinterpret_cast<unsigned long long*>(lo + even), add);
+    const bool low_wrap = ((old & 0xffffffffull) + (add & 0xffffffffull)) >> 32;
+    const bool pair_wrap = old + add < old;
+    if (low_wrap) atomicAdd(count + even, 1u);
+    if (pair_wrap) atomicAdd(count + even + 1, 1u);
+    if (low_wrap || pair_wrap) atomicOr(carry, 1u);
 }
 
 __global__ void k_deposit32(wbc_grid_geometry g, int32_t n, const float* __restrict__ position,
                             const int32_t* __restrict__ cell_state, const int32_t* __restrict__ order,
-                            uint32_t* __restrict__ lo, uint32_t* __restrict__ hi, uint32_t* __restrict__ carry) {
+                            uint32_t* __restrict__ lo, uint32_t* __restrict__ count, uint32_t* __restrict__ carry) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
     // the cell rule and weights of deposit_cell (kernels/field_kernels.py:78-116)
@@ -73,42 +98,47 @@ __global__ void k_deposit32(wbc_grid_geometry g, int32_t n, const float* __restr
         fy = uy - static_cast<float>(j0);
         fz = uz - static_cast<float>(k0);
     }
+    if (!ok) return;
 #pragma unroll
     for (int di = 0; di < 2; ++di) {
         const float wx = di == 0 ? 1.0f - fx : fx;
 #pragma unroll
         for (int dj = 0; dj < 2; ++dj) {
             const float wy = dj == 0 ? 1.0f - fy : fy;
-#pragma unroll
-            for (int dk = 0; dk < 2; ++dk) {
-                const float wz = dk == 0 ? 1.0f - fz : fz;
-                const float w = wx * wy * wz;
-                if (ok) {
-                    const unsigned int q = static_cast<unsigned int>(static_cast<int>(w * kFixedOne + 0.5f));
-                    const int64_t key = s * nodes + (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + (k0 + dk);
-                    const unsigned int old = atomicAdd(lo + key, q);
-                    if (old + q < old) {
-                        atomicAdd(hi + key, 1u);
-                        atomicOr(carry, 1u);
-                    }
-                }
+            const float w0 = wx * wy * (1.0f - fz);
+            const float w1 = wx * wy * fz;
+            const unsigned long long q0 = static_cast<unsigned int>(static_cast<int>(w0 * kFixedOne + 0.5f));
+            const unsigned long long q1 = static_cast<unsigned int>(static_cast<int>(w1 * kFixedOne + 0.5f));
+            // word of corner k0; corner k0 + 1 is the next word (4 * nodes is even, so both pairs
+            // touched below lie inside the layer array)
+            const int64_t key = s * nodes + (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + k0;
+            if ((key & 1) == 0) {
+                add_pair(lo, count, carry, key, q0 | (q1 << 32));
+            } else {
+                add_pair(lo, count, carry, key - 1, q0 << 32);
+                add_pair(lo, count, carry, key + 1, q1);
             }
         }
     }
 }
 
-// density_s = value_s / 2^24 * inv_vol (value_s = high * 2^32 + low) per state, as convert_node.
-__global__ void k_convert32(int64_t nodes, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ hi,
+// density_s = S_s / 2^24 * inv_vol per state, as convert_node, with S_s the exact sum of the paired
+// low words and their wrap counts (the formula above k_deposit32_clear).
+__global__ void k_convert32(int64_t nodes, const uint32_t* __restrict__ lo, const uint32_t* __restrict__ count,
                             const uint32_t* __restrict__ carry, float inv_vol, float* __restrict__ density, float w0,
                             float w1, float w2, float w3, float* __restrict__ combined) {
     const int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     if (node >= nodes) return;
-    const bool wide = *carry != 0u;
+    const bool wrapped = *carry != 0u;
     float d[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        long long a = static_cast<long long>(lo[s * nodes + node]);
-        if (wide) a += static_cast<long long>(hi[s * nodes + node]) << 32;
+        const int64_t w = s * nodes + node;
+        long long a = static_cast<long long>(lo[w]);
+        if (wrapped) {
+            a += static_cast<long long>(count[w]) << 32;
+            if (w & 1) a -= static_cast<long long>(count[w - 1]);
+        }
         d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
         if (density) density[s * nodes + node] = d[s];
     }
@@ -342,24 +372,20 @@ int wbc_deposit32(const wbc_grid_geometry* geom, int32_t n, const float* positio
         return WBC_ERR_INVALID;
     }
     uint32_t* lo = static_cast<uint32_t*>(accumulator);
-    uint32_t* hi = lo + 4 * nodes;
-    uint32_t* carry = hi + 4 * nodes;
+    uint32_t* count = lo + 4 * nodes;
+    uint32_t* carry = count + 4 * nodes;
     cudaStream_t s = as_stream(stream);
     const int64_t words = 4 * nodes;
-    const int64_t want = (words + 4 * kThreads - 1) / (4 * kThreads);
-    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 65535)));
-    cudaError_t err = cudaMemsetAsync(lo, 0, static_cast<size_t>(words) * sizeof(uint32_t), s);
+    const int64_t want = (words / 4 + kThreads - 1) / kThreads;
+    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 4 * 152)));
+    k_deposit32_clear<<<blocks, kThreads, 0, s>>>(words, reinterpret_cast<uint4*>(lo), reinterpret_cast<uint4*>(count),
+                                                  carry);
+    cudaError_t err = cudaMemsetAsync(carry, 0, sizeof(uint32_t), s);
     if (err != cudaSuccess) {
         set_error("wbc_deposit32: cudaMemsetAsync", err);
         return WBC_ERR_CUDA;
     }
-    k_deposit32_clear_high<<<blocks, kThreads, 0, s>>>(words, hi, carry);
-    err = cudaMemsetAsync(carry, 0, sizeof(uint32_t), s);
-    if (err != cudaSuccess) {
-        set_error("wbc_deposit32: cudaMemsetAsync", err);
-        return WBC_ERR_CUDA;
-    }
-    if (n > 0) k_deposit32<<<grid_for(n), kThreads, 0, s>>>(*geom, n, position, cell_state, order, lo, hi, carry);
+    if (n > 0) k_deposit32<<<grid_for(n), kThreads, 0, s>>>(*geom, n, position, cell_state, order, lo, count, carry);
     return check_launch("wbc_deposit32", n > 0 ? 2 : 1);
 }
 
@@ -368,12 +394,12 @@ int wbc_convert32(int64_t nodes, const void* accumulator, float inv_voxel_volume
     if (nodes < 0 || !accumulator || (combined && !weights4)) return WBC_ERR_INVALID;
     if (nodes == 0) return WBC_OK;
     const uint32_t* lo = static_cast<const uint32_t*>(accumulator);
-    const uint32_t* hi = lo + 4 * nodes;
-    const uint32_t* carry = hi + 4 * nodes;
+    const uint32_t* count = lo + 4 * nodes;
+    const uint32_t* carry = count + 4 * nodes;
     float w[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (weights4)
         for (int k = 0; k < 4; ++k) w[k] = weights4[k];
-    k_convert32<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, lo, hi, carry, inv_voxel_volume, density,
+    k_convert32<<<grid_for(nodes), kThreads, 0, as_stream(stream)>>>(nodes, lo, count, carry, inv_voxel_volume, density,
                                                                      w[0], w[1], w[2], w[3], combined);
     return check_launch("wbc_convert32");
 }

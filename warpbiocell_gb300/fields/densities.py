@@ -1,9 +1,9 @@
 """Per-state cell number densities on the grid (reference: fields/densities.py:13-56).
 
 ``deposit_fixed_point`` adds every cell's trilinear weights as fixed point (2^24 per cell) into a
-32-bit accumulator with an exact carry into high words (``wbc_deposit32``): integer atomics, so
-the sums are bit-exact and independent of thread order, the same as the reference's int64
-accumulator in half the bytes. The cells are visited in the hash grid's order when the population
+32-bit accumulator with exact wrap counts (``wbc_deposit32``): integer atomics, so the sums are
+bit-exact and independent of thread order, the same as the reference's int64 accumulator in half
+the bytes. The cells are visited in the hash grid's order when the population
 was binned at its current size, so that the atomics of a warp's cells hit nearby lines. The call
 clears the accumulator first; it then keeps the deposit until the next one.
 
@@ -55,10 +55,13 @@ class CellDensities:
         """The latest deposit's fixed-point sums as int64 (4, nx, ny, nz) (a copy, for inspection)."""
         words = 4 * self.geometry.node_count
         u32 = self._acc[: 8 * words].view(torch.int32)
-        lo = u32[:words].to(torch.int64) & 0xFFFFFFFF
-        hi = u32[words:].to(torch.int64)
-        carry = int(self._acc[8 * words: 8 * words + 4].view(torch.int32).item())
-        value = lo + (hi << 32) if carry else lo
+        value = u32[:words].to(torch.int64) & 0xFFFFFFFF
+        if int(self._acc[8 * words: 8 * words + 4].view(torch.int32).item()):
+            # low words are added to in pairs (2m, 2m+1) by 64-bit atomics: a wrap of word 2m
+            # carries into word 2m+1 and is counted in count[2m]; a wrap out of the pair in count[2m+1]
+            count = u32[words:].to(torch.int64) & 0xFFFFFFFF
+            value = value + (count << 32)
+            value[1::2] -= count[0::2]
         return value.reshape(NUM_STATES, *self.geometry.shape)
 
     # ---- deposit and conversion ------------------------------------------------------------------
