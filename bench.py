@@ -90,11 +90,11 @@ WORKLOADS = {
                              cells_lo=2_000, cells_hi=200_000, nodes_lo=41, nodes_hi=121, box_over_radius=2.5),
 }
 
-# ncu figures of one warm k_sor_resident launch (one steady-state solve) of the 1M-cell / 161^3
+# ncu figures of one k_sor_resident launch (the initial solve, 780 sweeps) of the 1M-cell / 161^3
 # workload, `profiles/k_sor_resident_spheroid_1M_161.md`: DRAM bytes read + written by the launch,
 # the sweeps it ran, its warp instructions per node update and its issue-active fraction.
-SOR_NCU = {"dram_bytes": 36.9e6, "sweeps": 780, "warp_inst_per_node_update": 11.99e9 / (780 * 4173281.0),
-           "issue_active": 0.788, "source": "profiles/k_sor_resident_spheroid_1M_161.md"}
+SOR_NCU = {"dram_bytes": 35.6e6, "sweeps": 780, "warp_inst_per_node_update": 10.924e9 / (780 * 4173281.0),
+           "issue_active": 0.783, "source": "profiles/k_sor_resident_spheroid_1M_161.md"}
 
 DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
 VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
@@ -301,11 +301,13 @@ def run_gpu(args, rank: int, world: int) -> dict | None:
     sweeps = []
     daughters = 0
     start_ev.record()
+    torch.cuda.nvtx.range_push("timed_steps")  # the launch lists under profiles/ capture this range
     for _ in range(args.steps):
         cell_steps += pop.count
         rep = step()
         sweeps.append(rep.field_sweeps)
         daughters += rep.daughters
+    torch.cuda.nvtx.range_pop()
     end_ev.record()
     barrier()
     elapsed_ms = start_ev.elapsed_time(end_ev)
@@ -848,11 +850,13 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     specs = [all_specs[i] for i in share]
     stepping = P["stepping"]
 
-    def timed(fn):
+    def timed(fn, name):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
+        torch.cuda.nvtx.range_push(name)
         out = fn()
+        torch.cuda.nvtx.range_pop()
         e1.record()
         torch.cuda.synchronize()
         return out, e0.elapsed_time(e1)
@@ -872,7 +876,7 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     sampler = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     sampler.start()
     time.sleep(0.3)
-    plain_cells, plain_ms = timed(lambda: run_plain(args.steps))
+    plain_cells, plain_ms = timed(lambda: run_plain(args.steps), "sequential_steps")
 
     # The same 15 runs as one batch: the first warm-up step outside the graph, then capture.
     members = [build_member(sp, P, dev) for sp in specs]
@@ -883,7 +887,7 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     batch.capture()
     if args.warmup > 1:
         batch.step(args.warmup - 1)
-    _, batch_ms = timed(lambda: batch.step(args.steps))
+    _, batch_ms = timed(lambda: batch.step(args.steps), "timed_steps")
     clocks = sampler.stop()
     counts = batch.sync()
     identical = batch.status_codes() == [0] * len(specs)
@@ -981,11 +985,13 @@ def run_adjoint(args) -> dict:
         xd = x.double()
         return ((u.double() - u_t) ** 2).sum() + (((xd - xd.mean(dim=0)).norm(dim=1) - rho_t) ** 2).sum()
 
-    def timed(fn):
+    def timed(fn, name):
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
+        torch.cuda.nvtx.range_push(name)
         out = fn()
+        torch.cuda.nvtx.range_pop()
         e1.record()
         torch.cuda.synchronize()
         return out, e0.elapsed_time(e1)
@@ -1000,9 +1006,9 @@ def run_adjoint(args) -> dict:
         v = v0.clone().requires_grad_(True)
         scal = {k: torch.tensor(val, dtype=torch.float64, requires_grad=True) for k, val in theta.items()}
         (u, x), f_ms = timed(lambda: CoupledSteadyState.apply(v, scal["km"], scal["diffusion"], scal["boundary"],
-                                                                scal["stiffness"], model))
+                                                                scal["stiffness"], model), "adjoint_forward")
         loss = loss_of(u, x)
-        _, b_ms = timed(loss.backward)
+        _, b_ms = timed(loss.backward, "adjoint_backward")
         if rep >= max(1, args.warmup):
             fwd_ms.append(f_ms)
             bwd_ms.append(b_ms)

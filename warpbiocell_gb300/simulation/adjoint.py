@@ -232,14 +232,23 @@ class CoupledSteadyState(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, vmax, km, diffusion, boundary, stiffness, model: AdjointSpheroid):
-        u, x = model.forward(vmax.detach(), float(km), float(diffusion), float(boundary), float(stiffness))
+        # NVTX ranges name the passes for profilers (the backward runs on autograd's device thread)
+        torch.cuda.nvtx.range_push("wbc_adjoint_forward")
+        try:
+            u, x = model.forward(vmax.detach(), float(km), float(diffusion), float(boundary), float(stiffness))
+        finally:
+            torch.cuda.nvtx.range_pop()
         ctx.model = model
         ctx.scalar_like = [torch.as_tensor(v) for v in (km, diffusion, boundary, stiffness)]
         return u, x
 
     @staticmethod
     def backward(ctx, grad_u, grad_x):
-        grads = ctx.model.backward(grad_u, grad_x)
+        torch.cuda.nvtx.range_push("wbc_adjoint_backward")
+        try:
+            grads = ctx.model.backward(grad_u, grad_x)
+        finally:
+            torch.cuda.nvtx.range_pop()
         like = ctx.scalar_like
 
         def scalar(value, ref):
