@@ -1180,12 +1180,25 @@ def main() -> None:
 def metric_extras(args) -> dict:
     """The other two parts of the metric, measured on the same GPU after the headline steps: the
     15-spheroid batched sweep against the same runs looped through the plain path, and the
-    adjoint's backward time over its forward time with its gradients checked against FP64."""
+    adjoint's backward time over its forward time with its gradients checked against FP64; then
+    the two other single-spheroid configurations (10k cells on 41^3, and the three-species
+    100k-cell run with Boolean networks on 81^3), each with its full-size bitwise parity check."""
     import copy
 
     import torch
 
     out = {}
+    configs = {}
+    for workload in ("spheroid_10k_41", "metabolic_network_100k_81"):
+        c_args = copy.copy(args)
+        c_args.workload = workload
+        c_args.steps = min(args.steps, 10)
+        c = report_gpu(c_args, [run_gpu(c_args, 0, 1)], 1)
+        keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "e2e", "gpu_launches",
+                "parity_full_size_bitwise", "cpu_baseline", "clocks", "config")
+        configs[workload] = {k: c[k] for k in keep if k in c}
+        torch.cuda.empty_cache()
+    out["configs"] = configs
     b_args = copy.copy(args)
     b_args.workload = "batched_sweep_15"
     b = run_batched(b_args)
