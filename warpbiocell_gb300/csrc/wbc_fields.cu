@@ -49,6 +49,20 @@ __global__ void k_convert(int64_t nodes, long long* __restrict__ acc, float inv_
 // at about half a cell per grid cell a node receives only a few contributions, which rarely
 // share a warp or a block.)
 
+// Streaming multiprocessors of the current device (cached per device).
+static int sm_count() {
+    static int cache[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 152;
+    if (cache[dev] == 0) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = sms > 0 ? sms : 152;
+    }
+    return cache[dev];
+}
+
 // Zeroes the low words, and the wrap counts when the previous deposit wrapped (otherwise they are
 // zero already); `words` is a multiple of 4, the buffers are 16-byte aligned.
 __global__ void k_deposit32_clear(int64_t words, uint4* __restrict__ lo, uint4* __restrict__ count,
@@ -377,7 +391,7 @@ int wbc_deposit32(const wbc_grid_geometry* geom, int32_t n, const float* positio
     cudaStream_t s = as_stream(stream);
     const int64_t words = 4 * nodes;
     const int64_t want = (words / 4 + kThreads - 1) / kThreads;
-    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 4 * 152)));
+    const unsigned blocks = static_cast<unsigned>(std::max<int64_t>(1, std::min<int64_t>(want, 4 * sm_count())));
     k_deposit32_clear<<<blocks, kThreads, 0, s>>>(words, reinterpret_cast<uint4*>(lo), reinterpret_cast<uint4*>(count),
                                                   carry);
     cudaError_t err = cudaMemsetAsync(carry, 0, sizeof(uint32_t), s);
