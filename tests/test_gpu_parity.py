@@ -121,6 +121,29 @@ def test_deposit_carry_into_high_words_is_exact():
     np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), orc.deposit(ogeom, pos[crowded:], states[crowded:]))
 
 
+def test_deposit_skips_cells_outside_the_grid_and_empty_populations():
+    """Cells outside the trilinear support (below the origin, on or past the last node) are skipped
+    as the oracle skips them, on an odd-sized grid whose z-corner pairs straddle the ends of
+    columns; a deposit of no cells then leaves every sum and density zero."""
+    geom = GridGeometry((-5.0, 0.0, 3.0), 7.0, (5, 6, 7))
+    rng = np.random.default_rng(21)
+    pos = np.concatenate([rng.uniform(-15.0, 50.0, (4000, 3)),
+                          np.array([[-5.0, 0.0, 3.0], [23.0, 35.0, 45.0], [22.99, 34.99, 44.99], [-5.001, 10.0, 10.0]])]
+                         ).astype(np.float32)
+    states = rng.integers(0, 4, pos.shape[0]).astype(np.int32)
+    ogeom = orc.Geometry(geom.origin, geom.dx, geom.shape)
+    dens = CellDensities(geom, device=DEV)
+    dens.deposit_fixed_point(_pop_from(pos, states))
+    acc_ref = orc.deposit(ogeom, pos, states)
+    assert 0 < np.count_nonzero(acc_ref) < acc_ref.size
+    np.testing.assert_array_equal(dens.accumulator.cpu().numpy(), acc_ref)
+    np.testing.assert_array_equal(dens.numpy(), orc.density_convert(ogeom, acc_ref)[0])
+    empty = _pop_from(np.zeros((0, 3), np.float32), np.zeros(0, np.int32), capacity=16)
+    dens.deposit_fixed_point(empty)
+    assert not dens.accumulator.any()
+    assert not dens.density.any()
+
+
 def test_deposit_in_hash_grid_order_and_lazy_densities():
     """The deposit visits the cells in the order of the last binning (same sums), and the plain
     oxygen step's consuming density alone gives the per-state densities later from the same deposit."""

@@ -104,6 +104,14 @@ __device__ __forceinline__ void confine(const wbc_tissue_region& R, float x, flo
     vz = vz - s * nz;
 }
 
+// A float at or above r * r (r > 0): RN(r * r) raised by one ulp. A candidate whose squared
+// distance d2 reaches it has sqrt(d2) >= r exactly, so the correctly rounded sqrtf(d2) is >= r too
+// (rounding is monotonic and r is a float), and the test d < r fails: the candidate is skipped
+// before its square root, with the same outcome. (r * r = inf gives NaN, which skips nothing.)
+__device__ __forceinline__ float cutoff_squared_above(float r) {
+    return __int_as_float(__float_as_int(__fmul_rn(r, r)) + 1);
+}
+
 // Sorted slot t: neighbour count, overlap-repulsion velocity (plus the region's push when REGION)
 // and the Euler step of its cell.
 template <bool REGION = false>
@@ -117,6 +125,7 @@ __device__ __forceinline__ void contact_slot(BucketMap map, int t, const int32_t
     const float4 me = sorted_xyzr[t];
     const int i = sorted_id[t];
     const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    const float cut2 = cutoff_squared_above(query_radius);
     float vx = 0.0f, vy = 0.0f, vz = 0.0f;
     int count = 0;
     for (int ox = -1; ox <= 1; ++ox) {
@@ -131,7 +140,9 @@ __device__ __forceinline__ void contact_slot(BucketMap map, int t, const int32_t
                     const float dx = me.x - q.x;
                     const float dy = me.y - q.y;
                     const float dz = me.z - q.z;
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 >= cut2) continue;
+                    const float d = sqrtf(d2);
                     if (d < query_radius) {
                         ++count;
                         const float overlap = me.w + q.w - d;
@@ -173,6 +184,7 @@ __device__ __forceinline__ float adjoint_contact_slot(BucketMap map, int t, cons
     const float lix = lambda_in[3 * static_cast<int64_t>(i)], liy = lambda_in[3 * static_cast<int64_t>(i) + 1],
                 liz = lambda_in[3 * static_cast<int64_t>(i) + 2];
     const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    const float cut2 = cutoff_squared_above(query_radius);
     float gx = 0.0f, gy = 0.0f, gz = 0.0f;  // sum_j A_ij (lambda_i - lambda_j) / rate
     float ux = 0.0f, uy = 0.0f, uz = 0.0f;  // v_i / rate
     for (int ox = -1; ox <= 1; ++ox) {
@@ -187,7 +199,9 @@ __device__ __forceinline__ float adjoint_contact_slot(BucketMap map, int t, cons
                     const float dx = me.x - q.x;
                     const float dy = me.y - q.y;
                     const float dz = me.z - q.z;
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 >= cut2) continue;
+                    const float d = sqrtf(d2);
                     if (!(d < query_radius)) continue;
                     const float R = me.w + q.w;
                     if (!(R - d > 0.0f && d > 1.0e-6f)) continue;

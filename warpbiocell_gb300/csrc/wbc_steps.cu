@@ -179,6 +179,7 @@ __device__ __forceinline__ void contact_slot_compensated(BucketMap map, int t, c
     const float4 ml = sorted_lo[t];
     const int i = sorted_id[t];
     const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    const float cut2 = cutoff_squared_above(query_radius);
     float vx = 0.0f, vy = 0.0f, vz = 0.0f;
     int count = 0;
     for (int ox = -1; ox <= 1; ++ox)
@@ -194,7 +195,9 @@ __device__ __forceinline__ void contact_slot_compensated(BucketMap map, int t, c
                     const float dx = (me.x - q.x) + (ml.x - ql.x);
                     const float dy = (me.y - q.y) + (ml.y - ql.y);
                     const float dz = (me.z - q.z) + (ml.z - ql.z);
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 >= cut2) continue;
+                    const float d = sqrtf(d2);
                     if (d < query_radius) {
                         ++count;
                         const float overlap = me.w + q.w - d;
@@ -238,6 +241,7 @@ __device__ __forceinline__ float adjoint_slot_compensated(BucketMap map, int t, 
     const float lix = lambda_in[3 * static_cast<int64_t>(i)], liy = lambda_in[3 * static_cast<int64_t>(i) + 1],
                 liz = lambda_in[3 * static_cast<int64_t>(i) + 2];
     const int cx = map.coord(me.x), cy = map.coord(me.y), cz = map.coord(me.z);
+    const float cut2 = cutoff_squared_above(query_radius);
     float gx = 0.0f, gy = 0.0f, gz = 0.0f, ux = 0.0f, uy = 0.0f, uz = 0.0f;
     for (int ox = -1; ox <= 1; ++ox)
         for (int oy = -1; oy <= 1; ++oy)
@@ -252,7 +256,9 @@ __device__ __forceinline__ float adjoint_slot_compensated(BucketMap map, int t, 
                     const float dx = (me.x - q.x) + (ml.x - ql.x);
                     const float dy = (me.y - q.y) + (ml.y - ql.y);
                     const float dz = (me.z - q.z) + (ml.z - ql.z);
-                    const float d = sqrtf(dx * dx + dy * dy + dz * dz);
+                    const float d2 = dx * dx + dy * dy + dz * dz;
+                    if (d2 >= cut2) continue;
+                    const float d = sqrtf(d2);
                     if (!(d < query_radius)) continue;
                     const float R = me.w + q.w;
                     if (!(R - d > 0.0f && d > 1.0e-6f)) continue;
