@@ -451,6 +451,18 @@ int wbc_adjoint_newton_prepare(const wbc_sor_params* p, const double* u, const f
 int wbc_adjoint_newton_apply(int64_t nodes, const float* delta, double* u, void* stream);
 /* out[i] = (double) in[i]. */
 int wbc_widen(int64_t n, const float* in, double* out, void* stream);
+/* Small device helpers of the adjoint's host code, so that its passes launch only this library's
+ * kernels: out[i] = (float) in[i]; out[i] = value; `bytes` zero bytes at ptr (a memset);
+ * out[i] = in[i] / divisor; x64[i] = (double) hi[i] + lo[i] with pos[i] = (float) x64[i]; and
+ * scratch[0] = the mean of x[0 .. n) in FP64 by a fixed-order reduction (0 for n = 0), scratch
+ * holding WBC_MEAN_SCRATCH doubles. */
+#define WBC_MEAN_SCRATCH 257
+int wbc_narrow(int64_t n, const double* in, float* out, void* stream);
+int wbc_fill(int64_t n, float value, float* out, void* stream);
+int wbc_zero(void* ptr, size_t bytes, void* stream);
+int wbc_divide(int64_t n, const float* in, float divisor, float* out, void* stream);
+int wbc_compensated_sum(int64_t n, const float* hi, const float* lo, double* x64, float* pos, void* stream);
+int wbc_mean(int64_t n, const float* x, double* scratch, void* stream);
 /* r = b - (diag x - sum_nb x) in FP64 where diag > 0, 0 elsewhere (the adjoint's refinement step). */
 int wbc_adjoint_linear_residual(const wbc_sor_params* p, const float* diag, const float* b, const float* x, float* r,
                                 void* stream);

@@ -648,3 +648,40 @@ def test_resident_solver_runs_the_benchmark_grid():
     assert ib["path"] == 2 and ib["tiles"] > 100
     assert (ra.sweeps, ra.residual) == (rb.sweeps, rb.residual)
     np.testing.assert_array_equal(a, b)
+
+
+def test_adjoint_host_helpers():
+    """The small kernels the adjoint's host code uses instead of eager torch operations: the
+    fixed-order FP64 mean (the same bits on every call, within 1e-12 of numpy's), narrowing,
+    filling, division and the compensated sum, each equal to its numpy counterpart."""
+    rng = np.random.default_rng(31)
+    st = _lib.stream(DEV)
+    for n in (0, 1, 1000, 1_000_003):
+        x = torch.from_numpy(rng.lognormal(0.0, 0.5, n).astype(np.float32)).to(DEV)
+        scratch = torch.empty(257, dtype=torch.float64, device=DEV)
+        _lib.call("wbc_mean", n, _lib.ptr(x), _lib.ptr(scratch), st)
+        first = float(scratch[0].item())
+        _lib.call("wbc_mean", n, _lib.ptr(x), _lib.ptr(scratch), st)
+        assert float(scratch[0].item()) == first
+        ref = float(x.cpu().numpy().astype(np.float64).mean()) if n else 0.0
+        assert abs(first - ref) <= 1e-12 * max(1.0, abs(ref))
+    n = 4099
+    d = torch.from_numpy(rng.normal(0.0, 1e3, n)).to(DEV)
+    f = torch.empty(n, dtype=torch.float32, device=DEV)
+    _lib.call("wbc_narrow", n, _lib.ptr(d), _lib.ptr(f), st)
+    np.testing.assert_array_equal(f.cpu().numpy(), d.cpu().numpy().astype(np.float32))
+    _lib.call("wbc_fill", n, 38.5, _lib.ptr(f), st)
+    assert bool((f == 38.5).all())
+    a = torch.from_numpy(rng.lognormal(0.0, 1.0, n).astype(np.float32)).to(DEV)
+    _lib.call("wbc_divide", n, _lib.ptr(a), 3.7, _lib.ptr(f), st)
+    np.testing.assert_array_equal(f.cpu().numpy(), a.cpu().numpy() / np.float32(3.7))
+    hi = torch.from_numpy(rng.uniform(-500, 500, n).astype(np.float32)).to(DEV)
+    lo = torch.from_numpy((rng.uniform(-1, 1, n) * 1e-5).astype(np.float32)).to(DEV)
+    x64 = torch.empty(n, dtype=torch.float64, device=DEV)
+    pos = torch.empty(n, dtype=torch.float32, device=DEV)
+    _lib.call("wbc_compensated_sum", n, _lib.ptr(hi), _lib.ptr(lo), _lib.ptr(x64), _lib.ptr(pos), st)
+    want = hi.cpu().numpy().astype(np.float64) + lo.cpu().numpy().astype(np.float64)
+    np.testing.assert_array_equal(x64.cpu().numpy(), want)
+    np.testing.assert_array_equal(pos.cpu().numpy(), want.astype(np.float32))
+    _lib.call("wbc_zero", _lib.ptr(pos), pos.numel() * 4, st)
+    assert not pos.any()

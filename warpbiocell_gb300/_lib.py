@@ -266,6 +266,12 @@ SIGNATURES: dict[str, list] = {
     "wbc_adjoint_newton_prepare": [POINTER(SorParamsC), _P, _P, _P, _P, _P],
     "wbc_adjoint_newton_apply": [c_int64, _P, _P, _P],
     "wbc_widen": [c_int64, _P, _P, _P],
+    "wbc_narrow": [c_int64, _P, _P, _P],
+    "wbc_fill": [c_int64, c_float, _P, _P],
+    "wbc_zero": [_P, c_size_t, _P],
+    "wbc_divide": [c_int64, _P, c_float, _P, _P],
+    "wbc_compensated_sum": [c_int64, _P, _P, _P, _P, _P],
+    "wbc_mean": [c_int64, _P, _P, _P],
     "wbc_adjoint_linear_residual": [POINTER(SorParamsC), _P, _P, _P, _P, _P],
     "wbc_adjoint_field_grads": [POINTER(SorParamsC), _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "wbc_contact_substep_region": [POINTER(NeighborGridC), _I, _F, _F, _F, POINTER(TissueRegionC), _P, _P, _P, _P],

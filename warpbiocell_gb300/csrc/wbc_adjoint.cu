@@ -325,6 +325,64 @@ __global__ void k_widen(int64_t n, const float* __restrict__ in, double* __restr
     if (a < n) out[a] = static_cast<double>(in[a]);
 }
 
+__global__ void k_narrow(int64_t n, const double* __restrict__ in, float* __restrict__ out) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = static_cast<float>(in[a]);
+}
+
+__global__ void k_fill(int64_t n, float value, float* __restrict__ out) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = value;
+}
+
+__global__ void k_divide(int64_t n, const float* __restrict__ in, float divisor, float* __restrict__ out) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a < n) out[a] = in[a] / divisor;
+}
+
+// x64 = hi + lo in FP64 (exact for the compensated pairs, whose lo is below half an ulp of hi) and
+// pos = x64 rounded to float.
+__global__ void k_compensated_sum(int64_t n, const float* __restrict__ hi, const float* __restrict__ lo,
+                                  double* __restrict__ x64, float* __restrict__ pos) {
+    const int64_t a = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const double x = static_cast<double>(hi[a]) + static_cast<double>(lo[a]);
+    x64[a] = x;
+    pos[a] = static_cast<float>(x);
+}
+
+// The mean of n floats in FP64 in a fixed order: block b sums elements b, b + B, b + 2B, ... per
+// thread in order and combines its threads by a fixed tree into partial[b + 1]; one block then
+// combines the B partials the same way into partial[0]. Nothing depends on scheduling.
+constexpr int kMeanThreads = 256;
+constexpr int kMeanBlocks = 256;  // partials; WBC_MEAN_SCRATCH = kMeanBlocks + 1 doubles
+__device__ __forceinline__ double block_sum(double v, double* part) {
+    part[threadIdx.x] = v;
+    __syncthreads();
+    for (int width = kMeanThreads / 2; width > 0; width >>= 1) {
+        if (static_cast<int>(threadIdx.x) < width) part[threadIdx.x] += part[threadIdx.x + width];
+        __syncthreads();
+    }
+    return part[0];
+}
+
+__global__ void __launch_bounds__(kMeanThreads) k_mean_partial(int64_t n, const float* __restrict__ x,
+                                                               double* __restrict__ partial) {
+    __shared__ double part[kMeanThreads];
+    double sum = 0.0;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * kMeanThreads;
+    for (int64_t a = static_cast<int64_t>(blockIdx.x) * kMeanThreads + threadIdx.x; a < n; a += stride)
+        sum += static_cast<double>(x[a]);
+    const double total = block_sum(sum, part);
+    if (threadIdx.x == 0) partial[blockIdx.x + 1] = total;
+}
+
+__global__ void __launch_bounds__(kMeanThreads) k_mean_final(int64_t n, int blocks, double* __restrict__ partial) {
+    __shared__ double part[kMeanThreads];
+    const double total = block_sum(static_cast<int>(threadIdx.x) < blocks ? partial[threadIdx.x + 1] : 0.0, part);
+    if (threadIdx.x == 0) partial[0] = n > 0 ? total / static_cast<double>(n) : 0.0;
+}
+
 // r = b - (diag x - sum_nb x) in FP64 at the free nodes (diag > 0), 0 elsewhere.
 __global__ void k_linear_residual(wbc_sor_params p, const float* __restrict__ diag, const float* __restrict__ b,
                                   const float* __restrict__ x, float* __restrict__ r) {
@@ -519,6 +577,55 @@ int wbc_widen(int64_t n, const float* in, double* out, void* stream) {
     if (n == 0) return WBC_OK;
     k_widen<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, in, out);
     return check_launch("wbc_widen");
+}
+
+int wbc_narrow(int64_t n, const double* in, float* out, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_narrow<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, in, out);
+    return check_launch("wbc_narrow");
+}
+
+int wbc_fill(int64_t n, float value, float* out, void* stream) {
+    if (n < 0 || (n > 0 && !out)) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_fill<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, value, out);
+    return check_launch("wbc_fill");
+}
+
+int wbc_zero(void* ptr, size_t bytes, void* stream) {
+    if (bytes > 0 && !ptr) return WBC_ERR_INVALID;
+    if (bytes == 0) return WBC_OK;
+    const cudaError_t err = cudaMemsetAsync(ptr, 0, bytes, as_stream(stream));
+    if (err != cudaSuccess) {
+        set_error("wbc_zero: cudaMemsetAsync", err);
+        return WBC_ERR_CUDA;
+    }
+    return WBC_OK;
+}
+
+int wbc_divide(int64_t n, const float* in, float divisor, float* out, void* stream) {
+    if (n < 0 || (n > 0 && (!in || !out))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_divide<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, in, divisor, out);
+    return check_launch("wbc_divide");
+}
+
+int wbc_compensated_sum(int64_t n, const float* hi, const float* lo, double* x64, float* pos, void* stream) {
+    if (n < 0 || (n > 0 && (!hi || !lo || !x64 || !pos))) return WBC_ERR_INVALID;
+    if (n == 0) return WBC_OK;
+    k_compensated_sum<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(n, hi, lo, x64, pos);
+    return check_launch("wbc_compensated_sum");
+}
+
+int wbc_mean(int64_t n, const float* x, double* scratch, void* stream) {
+    if (n < 0 || !scratch || (n > 0 && !x)) return WBC_ERR_INVALID;
+    static_assert(kMeanBlocks <= kMeanThreads, "the final block combines every partial");
+    const int blocks = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(kMeanBlocks, (n + 4095) / 4096)));
+    cudaStream_t s = as_stream(stream);
+    k_mean_partial<<<blocks, kMeanThreads, 0, s>>>(n, x, scratch);
+    k_mean_final<<<1, kMeanThreads, 0, s>>>(n, blocks, scratch);
+    return check_launch("wbc_mean", 2);
 }
 
 int wbc_adjoint_linear_residual(const wbc_sor_params* p, const float* diag, const float* b, const float* x, float* r,

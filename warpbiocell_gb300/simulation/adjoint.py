@@ -90,6 +90,22 @@ class AdjointSpheroid:
         probe = _lib.SorParamsC(nx=geometry.shape[0], ny=geometry.shape[1], nz=geometry.shape[2])
         self._workspace = torch.empty(int(_lib.load().wbc_sor_solve_workspace_bytes(ctypes.byref(probe))),
                                       dtype=torch.uint8, device=self.device)
+        # Per-pass buffers (filled by the library's kernels, so a pass launches no other kernel) and
+        # the field object every forward pass refills.
+        self._hi = torch.empty(self.n, 3, dtype=torch.float32, device=self.device)
+        self._lo = torch.empty_like(self._hi)
+        self._weight = torch.empty(self.n, dtype=torch.float32, device=self.device)
+        self._mean = torch.empty(257, dtype=torch.float64, device=self.device)  # WBC_MEAN_SCRATCH
+        self._g = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._mu0 = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._dmu = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._phi = torch.empty(nodes, dtype=torch.float32, device=self.device)
+        self._sums = torch.empty(3, dtype=torch.float64, device=self.device)
+        self._rate_dot = torch.empty(1, dtype=torch.float64, device=self.device)
+        self._lam_tmp = torch.empty_like(self._hi)
+        self._work = torch.empty_like(self._hi)
+        self._work_lo = torch.empty_like(self._hi)
+        self._field_object = None
         # Newton corrections of the fp32 steady field and refinement of the adjoint solve, each to this
         # relative residual (the correction problems are solved in fp32, their residuals in FP64).
         self.newton_steps = 2
@@ -112,22 +128,31 @@ class AdjointSpheroid:
                   _lib.ptr(self._checkpoints_lo) if checkpoints else None, self.segment, self._slots, int(history),
                   int(history), _lib.ptr(self._steps_ws), self._steps_ws.numel(), 1, _lib.stream(self.device))
 
+    def _zero(self, t: torch.Tensor) -> None:
+        _lib.call("wbc_zero", _lib.ptr(t), t.numel() * t.element_size(), _lib.stream(self.device))
+
     def _field(self, pos: torch.Tensor, vmax: torch.Tensor, km: float, diffusion: float, boundary: float):
         """Deposit, the fp32 steady solve, then Newton corrections with FP64 residuals: returns the
-        field object and the refined field (float64, flat)."""
+        solver parameters and the refined field (float64, flat)."""
         st = _lib.stream(self.device)
-        scale = float(vmax.mean().item())
-        weight = (vmax / scale).to(torch.float32).contiguous()
+        # per-cell weights Vmax_i / mean(Vmax), the mean in FP64 by a fixed-order reduction
+        _lib.call("wbc_mean", self.n, _lib.ptr(vmax), _lib.ptr(self._mean), st)
+        scale = float(self._mean[0].item())
+        _lib.call("wbc_divide", self.n, _lib.ptr(vmax), scale, _lib.ptr(self._weight), st)
         geom = self.geometry.native()
-        _lib.call("wbc_deposit_weighted", ctypes.byref(geom), self.n, _lib.ptr(pos), _lib.ptr(weight),
+        _lib.call("wbc_deposit_weighted", ctypes.byref(geom), self.n, _lib.ptr(pos), _lib.ptr(self._weight),
                   _lib.ptr(self.accumulator), st)
         _lib.call("wbc_weighted_convert", self.geometry.node_count, _lib.ptr(self.accumulator),
                   scale / self.geometry.voxel_volume, _lib.ptr(self.uptake), 1, st)
-        field = ScalarField.create(self.geometry, boundary, device=self.device)
+        nodes = self.geometry.node_count
+        if self._field_object is None:
+            self._field_object = ScalarField.create(self.geometry, boundary, device=self.device)
+        field = self._field_object
+        field.boundary_value = float(boundary)  # a cold start from the boundary value, as a new field
+        _lib.call("wbc_fill", nodes, float(boundary), _lib.ptr(field.values), st)
         kin = UptakeKinetics(diffusion, 1.0, km)
         report = solve_steady_state(field, self.uptake, kin, self.settings, self._residual)
         self.last_forward_sweeps = report.sweeps
-        nodes = self.geometry.node_count
         u64 = torch.empty(nodes, dtype=torch.float64, device=self.device)
         _lib.call("wbc_widen", nodes, _lib.ptr(field.values), _lib.ptr(u64), st)
         params = sor_params(field, kin, self.settings.omega, False, 1.0)
@@ -135,11 +160,11 @@ class AdjointSpheroid:
         for _ in range(self.newton_steps):
             _lib.call("wbc_adjoint_newton_prepare", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(self.uptake),
                       _lib.ptr(self._diag), _lib.ptr(self._rhs), st)
-            self._delta.zero_()
+            self._zero(self._delta)
             sweeps += self._linear_solve(params, self._diag, self._rhs, self._delta, self.refine_tolerance)
             _lib.call("wbc_adjoint_newton_apply", nodes, _lib.ptr(self._delta), _lib.ptr(u64), st)
         self.last_newton_sweeps = sweeps
-        return field, u64
+        return params, u64
 
     def _linear_solve(self, params, diag: torch.Tensor, rhs: torch.Tensor, x: torch.Tensor, tolerance: float) -> int:
         """diag x - sum_nb x = rhs from x's current values, in one resident launch; returns the sweeps."""
@@ -154,50 +179,63 @@ class AdjointSpheroid:
     # ---- forward / backward ------------------------------------------------------------------------
     def forward(self, vmax: torch.Tensor, km: float, diffusion: float, boundary: float, stiffness: float):
         """(u flat, x_K); keeps the checkpoints and the field state for :meth:`backward`."""
+        st = _lib.stream(self.device)
+        vmax = vmax.detach()
+        if vmax.dtype != torch.float32 or not vmax.is_contiguous() or vmax.device != self.device:
+            vmax = vmax.to(self.device, torch.float32).contiguous()
+        if vmax.shape != (self.n,):
+            raise ValueError(f"vmax must have shape ({self.n},)")
         rate = float(stiffness) / self.contact.damping
-        hi = self.x0.clone()
-        lo = torch.zeros_like(hi)
+        hi, lo = self._hi, self._lo
+        hi.copy_(self.x0)
+        self._zero(lo)
         self._steps(hi, lo, rate, self.steps, checkpoints=True)
-        x64 = hi.double() + lo.double()
-        pos = x64.float()  # the cells' positions for the deposit
-        field, u64 = self._field(pos, vmax, km, diffusion, boundary)
-        self._saved = dict(pos=pos, vmax=vmax.detach().contiguous(), km=float(km), diffusion=float(diffusion),
-                           boundary=float(boundary), stiffness=float(stiffness), rate=rate, field=field,
-                           uptake=self.uptake.clone(), u64=u64)
-        return u64.clone(), x64
+        x64 = torch.empty(self.n, 3, dtype=torch.float64, device=self.device)
+        pos = torch.empty(self.n, 3, dtype=torch.float32, device=self.device)  # positions for the deposit
+        _lib.call("wbc_compensated_sum", 3 * self.n, _lib.ptr(hi), _lib.ptr(lo), _lib.ptr(x64), _lib.ptr(pos), st)
+        params, u64 = self._field(pos, vmax, km, diffusion, boundary)
+        uptake = torch.empty_like(self.uptake)
+        uptake.copy_(self.uptake)
+        self._saved = dict(pos=pos, vmax=vmax, km=float(km), diffusion=float(diffusion), boundary=float(boundary),
+                           stiffness=float(stiffness), rate=rate, params=params, uptake=uptake, u64=u64)
+        u = torch.empty_like(u64)
+        u.copy_(u64)
+        return u, x64
 
     def backward(self, grad_u: torch.Tensor | None, grad_x: torch.Tensor | None) -> dict:
         sv = self._saved
         st = _lib.stream(self.device)
         nodes = self.geometry.node_count
-        pos, vmax, field = sv["pos"], sv["vmax"], sv["field"]
-        g = torch.zeros(nodes, dtype=torch.float32, device=self.device) if grad_u is None else \
-            grad_u.detach().to(torch.float32).reshape(-1).contiguous()
-        lam = torch.zeros(self.n, 3, dtype=torch.float32, device=self.device) if grad_x is None else \
-            grad_x.detach().to(torch.float32).contiguous().clone()
+        pos, vmax, params = sv["pos"], sv["vmax"], sv["params"]
+        g = self._g
+        if grad_u is None:
+            self._zero(g)
+        else:
+            self._narrow_into(grad_u, g)
+        lam = torch.empty(self.n, 3, dtype=torch.float32, device=self.device)  # becomes dL/dx_0
+        if grad_x is None:
+            self._zero(lam)
+        else:
+            self._narrow_into(grad_x, lam)
 
         # field adjoint: (6 + h kappa) mu - sum_nb mu = dL/du at the refined field, solved in fp32 and
         # refined once with the residual in FP64 (mu = mu0 + dmu)
-        kin = UptakeKinetics(sv["diffusion"], 1.0, sv["km"])
-        params = sor_params(field, kin, self.settings.omega, False, 1.0)
         u64 = sv["u64"]
-        diag, rhs = self._diag, self._rhs
+        diag, rhs, mu0, dmu = self._diag, self._rhs, self._mu0, self._dmu
         _lib.call("wbc_adjoint_newton_prepare", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(sv["uptake"]),
                   _lib.ptr(diag), _lib.ptr(rhs), st)
-        mu0 = torch.zeros(nodes, dtype=torch.float32, device=self.device)
-        dmu = torch.zeros(nodes, dtype=torch.float32, device=self.device)
+        self._zero(mu0)
+        self._zero(dmu)
         sweeps = self._linear_solve(params, diag, g, mu0, self.adjoint_tolerance)
         converged = self.last_linear_converged
         _lib.call("wbc_adjoint_linear_residual", ctypes.byref(params), _lib.ptr(diag), _lib.ptr(g), _lib.ptr(mu0),
                   _lib.ptr(rhs), st)
         sweeps += self._linear_solve(params, diag, rhs, dmu, self.adjoint_tolerance)
-        phi = torch.empty(nodes, dtype=torch.float32, device=self.device)
-        sums = torch.empty(3, dtype=torch.float64, device=self.device)
+        phi, sums = self._phi, self._sums
         _lib.call("wbc_adjoint_field_grads", ctypes.byref(params), _lib.ptr(u64), _lib.ptr(sv["uptake"]),
                   _lib.ptr(mu0), _lib.ptr(dmu), _lib.ptr(diag), _lib.ptr(g), _lib.ptr(phi), _lib.ptr(sums), st)
         self.last_adjoint_converged = converged and self.last_linear_converged
         self.last_adjoint_sweeps = sweeps
-        d_km, d_diffusion_times_d, d_boundary = sums.tolist()
         h = params.dx2_over_D
         grad_vmax = torch.empty(self.n, dtype=torch.float32, device=self.device)
         coef = -h / self.geometry.voxel_volume
@@ -209,10 +247,8 @@ class AdjointSpheroid:
         # recomputed from its checkpoint in one launch that keeps each step's grid, then its steps
         # run in reverse in one launch over those grids
         rate = sv["rate"]
-        rate_dot = torch.zeros(1, dtype=torch.float64, device=self.device)
-        lam_tmp = torch.empty_like(lam)
-        work = torch.empty_like(self.x0)
-        work_lo = torch.empty_like(self.x0)
+        rate_dot, lam_tmp, work, work_lo = self._rate_dot, self._lam_tmp, self._work, self._work_lo
+        self._zero(rate_dot)
         for seg in range((self.steps + self.segment - 1) // self.segment - 1, -1, -1):
             start = seg * self.segment
             stop = min(self.steps, start + self.segment)
@@ -222,9 +258,18 @@ class AdjointSpheroid:
             _lib.call("wbc_adjoint_steps", ctypes.byref(self.grid.struct), self.n, float(self.contact.query_radius),
                       float(rate), self.dt, stop - start, 1, _lib.ptr(lam), _lib.ptr(lam_tmp), _lib.ptr(rate_dot),
                       self._slots, _lib.ptr(self._steps_ws), self._steps_ws.numel(), 1, st)
+        d_km, d_diffusion_times_d, d_boundary = sums.tolist()
         d_rate = self.dt * float(rate_dot.item())
         return dict(vmax=grad_vmax, km=d_km, diffusion=d_diffusion_times_d / sv["diffusion"], boundary=d_boundary,
                     stiffness=d_rate / self.contact.damping, x0=lam)
+
+    def _narrow_into(self, src: torch.Tensor, dst: torch.Tensor) -> None:
+        """dst = src as float32 (a float64 gradient narrowed by the library, a float32 one copied)."""
+        src = src.detach().reshape(dst.shape)
+        if src.dtype == torch.float64 and src.is_contiguous() and src.device == self.device:
+            _lib.call("wbc_narrow", dst.numel(), _lib.ptr(src), _lib.ptr(dst), _lib.stream(self.device))
+        else:
+            dst.copy_(src)
 
 
 class CoupledSteadyState(torch.autograd.Function):
