@@ -59,7 +59,7 @@ static_assert(sizeof(SorControl) == 128, "SorControl is one 128-byte line");
 constexpr int kMaxCtas = 1024;     // barrier flags that follow the control block
 constexpr int kSorThreads = 1024;  // threads per CTA of the resident solver
 constexpr int kMaxEntries = 1023;  // entries per colour column (nz <= 2045): 10 bits of a chunk word
-constexpr int kPlaneSlack = 64;    // floats past the largest box: lanes beyond a run's end read there
+constexpr int kPlaneSlack = 128;   // floats past the largest box: lanes beyond a group's end read there
 
 // Shared-memory layout of one tile, sized for the largest tile of the solve.
 struct SorTiling {
@@ -392,9 +392,8 @@ __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, i
         unsigned long long* xp = xrow + d.y;
 #pragma unroll
         for (int r = 0; r < kSub; ++r)
-            if (r == 0 || d.w > 32 * r)
-                relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
-                                                      du[r], pr[r], colour, lane, tag);
+            relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
+                                                  du[r], pr[r], colour, lane, tag);
         if (!more) break;
         d = dn;
 #pragma unroll
