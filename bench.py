@@ -93,8 +93,8 @@ WORKLOADS = {
 # ncu figures of one k_sor_resident launch (the initial solve, 780 sweeps) of the 1M-cell / 161^3
 # workload, `profiles/k_sor_resident_spheroid_1M_161.md`: DRAM bytes read + written by the launch,
 # the sweeps it ran, its warp instructions per node update and its issue-active fraction.
-SOR_NCU = {"dram_bytes": 35.6e6, "sweeps": 780, "warp_inst_per_node_update": 10.924e9 / (780 * 4173281.0),
-           "issue_active": 0.783, "source": "profiles/k_sor_resident_spheroid_1M_161.md"}
+SOR_NCU = {"dram_bytes": 35.4e6, "sweeps": 780, "warp_inst_per_node_update": 10.787e9 / (780 * 4173281.0),
+           "issue_active": 0.793, "source": "profiles/k_sor_resident_spheroid_1M_161.md"}
 
 DIFFUSION = 7.2e6  # um^2/h (2000 um^2/s)
 VMAX = 20e-18 / 1.3e-21 * 3600.0  # 20 amol/s over O2 solubility 1.3e-21 mol/(um^3 mmHg) -> mmHg um^3/h
