@@ -357,7 +357,7 @@ __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, fl
 
 // The groups of one colour, a warp per group, edge groups first; the next group's coefficients
 // (and production terms), which live in L2, are loaded before the current group is relaxed.
-template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR, bool BRANCH_FREE>
 __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, int colour, int warp, int nwarps,
                                              int lane, unsigned int tag) {
     int q = warp;
@@ -390,10 +390,15 @@ __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, i
         float* po = own + d.x;
         const float* pv = oth + d.x;
         unsigned long long* xp = xrow + d.y;
+        // BRANCH_FREE: every chunk of the group, without branches between them, so that their
+        // dependency chains interleave (lanes past the group's end compute on in-bounds slack and
+        // store nothing); otherwise only the chunks with entries (the batched solves of small grids,
+        // whose short runs end in many partial groups, run faster that way).
 #pragma unroll
         for (int r = 0; r < kSub; ++r)
-            relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
-                                                  du[r], pr[r], colour, lane, tag);
+            if (BRANCH_FREE || r == 0 || d.w > 32 * r)
+                relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
+                                                      du[r], pr[r], colour, lane, tag);
         if (!more) break;
         d = dn;
 #pragma unroll
@@ -654,7 +659,7 @@ __device__ __forceinline__ void build_lists(const SorArgs& a, const TileRect& r,
 // One tile (`tile` of `ntiles`) of one solve, for the whole solve. `claims` / `claims_needed`:
 // see WaitClock (batched solves; null for a single solve). LINEAR: the linear system
 // d x - sum_nb x = b (`density` holds d, d <= 0 holds x; `production` holds b).
-template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR, bool BRANCH_FREE>
 __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles, const unsigned int* claims = nullptr,
                                          unsigned int claims_needed = 0) {
     extern __shared__ __align__(128) float s[];
@@ -736,7 +741,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
         for (int half = 0; half < 2 * chunk; ++half) {
             const int colour = half & 1;
             const unsigned int tag = static_cast<unsigned int>(2 * sweeps + half + 1);
-            relax_colour<HAS_PROD || LINEAR, ZCLAMP, LINEAR>(a, w, colour, warp, nwarps, lane, tag);
+            relax_colour<HAS_PROD || LINEAR, ZCLAMP, LINEAR, BRANCH_FREE>(a, w, colour, warp, nwarps, lane, tag);
             const bool fine = pull_halo(a, w, colour, tag, warp, nwarps, lane);
             if (__syncthreads_or(!fine)) {
                 if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
@@ -833,7 +838,7 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
 
 template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
 __global__ void __launch_bounds__(kSorThreads, 1) k_sor_resident(SorArgs a) {
-    sor_tile<HAS_PROD, ZCLAMP, LINEAR>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
+    sor_tile<HAS_PROD, ZCLAMP, LINEAR, true>(a, static_cast<int>(blockIdx.x), static_cast<int>(gridDim.x));
 }
 
 // The solver's grid barrier alone, for the self-test of the bounded waits: `ntiles` tiles are
@@ -880,7 +885,7 @@ __global__ void __launch_bounds__(kSorThreads, 1)
         const int t = s_tile;
         if (t >= total) return;
         const int b = find_batch_item(tile_first, n, t);
-        sor_tile<HAS_PROD, ZCLAMP, false>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
+        sor_tile<HAS_PROD, ZCLAMP, false, false>(args[b], t - tile_first[b], tile_first[b + 1] - tile_first[b], next_tile,
                                           static_cast<unsigned int>(tile_first[b + 1]));
     }
 }
