@@ -504,8 +504,10 @@ typedef struct wbc_batch_instance {
     float contact_dt;             /* dt_mechanics                                                    */
     int32_t contact_substeps;
     wbc_grid_geometry geom;       /* the oxygen grid                                                 */
-    int64_t* accumulator;         /* int64[4][nodes], cleared by wbc_batch_deposit after reading it  */
-    float* density;               /* float[4][nodes] per-state densities, or NULL                    */
+    void* accumulator;            /* the 32-bit accumulator of wbc_deposit32 (wbc_deposit32_bytes(   */
+                                  /* nodes) bytes, 16-byte aligned), cleared by each batched deposit  */
+    float* density;               /* unused: per-state densities are converted from the accumulator  */
+                                  /* by wbc_convert32 when they are wanted                           */
     float* uptake_density;        /* the solver's combined uptake density, float[nodes]              */
     float uptake_weights[4];
     float inv_voxel_volume;
@@ -531,7 +533,8 @@ int wbc_batch_prepare(int32_t n, const wbc_batch_instance* insts, void* plan, si
 int wbc_batch_grid_build(const wbc_batch* b, const int32_t* counts, void* stream);
 /* wbc_contact_substep for every instance (one substep). */
 int wbc_batch_contact(const wbc_batch* b, const int32_t* counts, void* stream);
-/* wbc_deposit then wbc_density_convert (clearing the accumulator) for every instance. */
+/* wbc_deposit32 (cells in slot order) then wbc_convert32 of the combined uptake density only, for
+ * every instance. */
 int wbc_batch_deposit(const wbc_batch* b, const int32_t* counts, void* stream);
 /* wbc_sample of `field` into oxygen_local for every instance. */
 int wbc_batch_sample(const wbc_batch* b, const int32_t* counts, void* stream);

@@ -153,9 +153,22 @@ __global__ void __launch_bounds__(kChunk) k_b_contact(BatchPlan P, const int32_t
     }
 }
 
+// An instance's 32-bit accumulator (the layout of wbc_deposit32): low words, wrap counts, carry.
+struct Acc32 {
+    uint32_t* lo;
+    uint32_t* count;
+    uint32_t* carry;
+};
+__device__ __forceinline__ Acc32 acc32_of(const wbc_batch_instance& I) {
+    const int64_t nodes = static_cast<int64_t>(I.geom.nx) * I.geom.ny * I.geom.nz;
+    uint32_t* lo = static_cast<uint32_t*>(I.accumulator);
+    return Acc32{lo, lo + 4 * nodes, lo + 8 * nodes};
+}
+
 __global__ void __launch_bounds__(kChunk) k_b_deposit(BatchPlan P, const int32_t* __restrict__ counts) {
     WBC_CELL_LOOP
-        deposit_cell(I.geom, i, I.position, I.cell_state, reinterpret_cast<unsigned long long*>(I.accumulator));
+        const Acc32 A = acc32_of(I);
+        deposit32_cell(I.geom, i, I.position, I.cell_state, A.lo, A.count, A.carry);
     }
 }
 
@@ -197,16 +210,42 @@ __global__ void k_b_commit(BatchPlan P, int32_t* __restrict__ counts, int32_t* _
 #undef WBC_CELL_LOOP
 
 // ---- per-node stage --------------------------------------------------------------------------------
+// Zeroes every instance's low words, and its wrap counts when its previous deposit wrapped.
+__global__ void __launch_bounds__(kChunk) k_b_clear32(BatchPlan P) {
+    for (int c = blockIdx.x; c < P.node_first[P.n]; c += gridDim.x) {
+        const int b = find_item(P.node_first, P.n, c);
+        const wbc_batch_instance& I = P.inst[b];
+        const int64_t nodes = static_cast<int64_t>(I.geom.nx) * I.geom.ny * I.geom.nz;
+        const int64_t node = static_cast<int64_t>(c - P.node_first[b]) * kChunk + threadIdx.x;
+        if (node >= nodes) continue;
+        const Acc32 A = acc32_of(I);
+        const bool wrapped = *A.carry != 0u;
+#pragma unroll
+        for (int st = 0; st < 4; ++st) {
+            A.lo[st * nodes + node] = 0u;
+            if (wrapped) A.count[st * nodes + node] = 0u;
+        }
+    }
+}
+
+// Clears the carry flags once every clear has read them.
+__global__ void k_b_reset_carry(BatchPlan P) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < P.n) *acc32_of(P.inst[b]).carry = 0u;
+}
+
+// The solver's combined uptake density of every instance from its deposit; the per-state densities
+// are left to be converted from the same sums when they are read.
 __global__ void __launch_bounds__(kChunk) k_b_convert(BatchPlan P) {
     for (int c = blockIdx.x; c < P.node_first[P.n]; c += gridDim.x) {
         const int b = find_item(P.node_first, P.n, c);
         const wbc_batch_instance& I = P.inst[b];
         const int64_t nodes = static_cast<int64_t>(I.geom.nx) * I.geom.ny * I.geom.nz;
         const int64_t node = static_cast<int64_t>(c - P.node_first[b]) * kChunk + threadIdx.x;
-        if (node < nodes)
-            convert_node(nodes, node, reinterpret_cast<long long*>(I.accumulator), I.inv_voxel_volume, I.density,
-                         I.uptake_weights[0], I.uptake_weights[1], I.uptake_weights[2], I.uptake_weights[3],
-                         I.uptake_density, 1);
+        if (node >= nodes) continue;
+        const Acc32 A = acc32_of(I);
+        convert32_node(nodes, node, A.lo, A.count, *A.carry != 0u, I.inv_voxel_volume, nullptr, I.uptake_weights[0],
+                       I.uptake_weights[1], I.uptake_weights[2], I.uptake_weights[3], I.uptake_density);
     }
 }
 
@@ -363,7 +402,8 @@ int wbc_batch_prepare(int32_t n, const wbc_batch_instance* insts, void* plan, si
         const wbc_batch_instance& I = insts[b];
         if (I.capacity < 0 || I.grid.dim < 3 || I.grid.dim > 1290 || !(I.grid.cell_size > 0.0f) ||
             I.grid.capacity < I.capacity || !(I.query_radius <= I.grid.cell_size) || I.contact_substeps < 1 ||
-            I.geom.nx < 2 || I.geom.ny < 2 || I.geom.nz < 2 || !I.accumulator || !I.uptake_density || !I.field) {
+            I.geom.nx < 2 || I.geom.ny < 2 || I.geom.nz < 2 || !I.accumulator || !I.uptake_density || !I.field ||
+            reinterpret_cast<uintptr_t>(I.accumulator) % 16 != 0) {
             set_error_msg("wbc_batch_prepare: invalid instance description");
             return WBC_ERR_INVALID;
         }
@@ -424,9 +464,11 @@ int wbc_batch_deposit(const wbc_batch* b, const int32_t* counts, void* stream) {
     if (!batch_ok(b) || !counts) return WBC_ERR_INVALID;
     const BatchPlan P = plan_of(b);
     cudaStream_t s = as_stream(stream);
+    k_b_clear32<<<grid_of(b->node_chunks), kChunk, 0, s>>>(P);
+    k_b_reset_carry<<<grid_of((b->instances + 127) / 128), 128, 0, s>>>(P);
     k_b_deposit<<<grid_of(b->cell_chunks), kChunk, 0, s>>>(P, counts);
     k_b_convert<<<grid_of(b->node_chunks), kChunk, 0, s>>>(P);
-    return check_launch("wbc_batch_deposit", 2);
+    return check_launch("wbc_batch_deposit", 4);
 }
 
 int wbc_batch_sample(const wbc_batch* b, const int32_t* counts, void* stream) {

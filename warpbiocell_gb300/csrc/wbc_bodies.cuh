@@ -104,6 +104,84 @@ __device__ __forceinline__ void confine(const wbc_tissue_region& R, float x, flo
     vz = vz - s * nz;
 }
 
+// ---- 32-bit deposit with exact wrap counts (wbc_deposit32, the batched deposit) -------------------
+// Low words [4][nodes] added to in aligned pairs (2m, 2m+1) by 64-bit atomics; a wrap out of the
+// even word increments count[2m], a wrap out of the pair count[2m+1], and any wrap sets *carry:
+//     S[2m] = low[2m] + 2^32 count[2m],   S[2m+1] = low[2m+1] + 2^32 count[2m+1] - count[2m].
+
+// adds `add` (low half to word `even`, high half to word `even` + 1) and counts the wraps
+__device__ __forceinline__ void add_pair32(uint32_t* lo, uint32_t* count, uint32_t* carry, int64_t even,
+                                           unsigned long long add) {
+    const unsigned long long old = atomicAdd(reinterpret_cast<unsigned long long*>(lo + even), add);
+    const bool low_wrap = ((old & 0xffffffffull) + (add & 0xffffffffull)) >> 32;
+    const bool pair_wrap = old + add < old;
+    if (low_wrap) atomicAdd(count + even, 1u);
+    if (pair_wrap) atomicAdd(count + even + 1, 1u);
+    if (low_wrap || pair_wrap) atomicOr(carry, 1u);
+}
+
+// Cell c's trilinear weights (the cell rule and weights of deposit_cell, kernels/field_kernels.py:
+// 78-116) into the 32-bit accumulator: for each (i, j) column of its corners one pair add when the
+// word of corner k0 is even, else two (4 * nodes is even, so both pairs lie inside the array).
+__device__ __forceinline__ void deposit32_cell(const wbc_grid_geometry& g, int c, const float* __restrict__ position,
+                                               const int32_t* __restrict__ cell_state, uint32_t* lo, uint32_t* count,
+                                               uint32_t* carry) {
+    const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
+    const int s = cell_state[c];
+    const float* p = position + 3 * static_cast<int64_t>(c);
+    const float ux = (p[0] - g.origin_x) * g.inv_dx;
+    const float uy = (p[1] - g.origin_y) * g.inv_dx;
+    const float uz = (p[2] - g.origin_z) * g.inv_dx;
+    const int i0 = static_cast<int>(floorf(ux));
+    const int j0 = static_cast<int>(floorf(uy));
+    const int k0 = static_cast<int>(floorf(uz));
+    if (!(s >= 0 && s < 4 && i0 >= 0 && j0 >= 0 && k0 >= 0 && i0 + 1 < g.nx && j0 + 1 < g.ny && k0 + 1 < g.nz))
+        return;
+    const float fx = ux - static_cast<float>(i0);
+    const float fy = uy - static_cast<float>(j0);
+    const float fz = uz - static_cast<float>(k0);
+#pragma unroll
+    for (int di = 0; di < 2; ++di) {
+        const float wx = di == 0 ? 1.0f - fx : fx;
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj) {
+            const float wy = dj == 0 ? 1.0f - fy : fy;
+            const float w0 = wx * wy * (1.0f - fz);
+            const float w1 = wx * wy * fz;
+            const unsigned long long q0 = static_cast<unsigned int>(static_cast<int>(w0 * kFixedOne + 0.5f));
+            const unsigned long long q1 = static_cast<unsigned int>(static_cast<int>(w1 * kFixedOne + 0.5f));
+            const int64_t key = s * nodes + (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + k0;
+            if ((key & 1) == 0) {
+                add_pair32(lo, count, carry, key, q0 | (q1 << 32));
+            } else {
+                add_pair32(lo, count, carry, key - 1, q0 << 32);
+                add_pair32(lo, count, carry, key + 1, q1);
+            }
+        }
+    }
+}
+
+// One node's per-state densities S_s / 2^24 * inv_vol (convert_node's expression; `density` may be
+// null) and their combination `combined` = sum_s w_s density_s (may be null).
+__device__ __forceinline__ void convert32_node(int64_t nodes, int64_t node, const uint32_t* __restrict__ lo,
+                                               const uint32_t* __restrict__ count, bool wrapped, float inv_vol,
+                                               float* __restrict__ density, float w0, float w1, float w2, float w3,
+                                               float* __restrict__ combined) {
+    float d[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        const int64_t w = s * nodes + node;
+        long long a = static_cast<long long>(lo[w]);
+        if (wrapped) {
+            a += static_cast<long long>(count[w]) << 32;
+            if (w & 1) a -= static_cast<long long>(count[w - 1]);
+        }
+        d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
+        if (density) density[s * nodes + node] = d[s];
+    }
+    if (combined) combined[node] = w0 * d[0] + w1 * d[1] + w2 * d[2] + w3 * d[3];
+}
+
 // A float at or above r * r (r > 0): RN(r * r) raised by one ulp. A candidate whose squared
 // distance d2 reaches it has sqrt(d2) >= r exactly, so the correctly rounded sqrtf(d2) is >= r too
 // (rounding is monotonic and r is a float), and the test d < r fails: the candidate is skipped

@@ -77,63 +77,11 @@ __global__ void k_deposit32_clear(int64_t words, uint4* __restrict__ lo, uint4* 
     }
 }
 
-// adds `add` (low half to word `even`, high half to word `even` + 1) and counts the wraps
-__device__ __forceinline__ void add_pair(uint32_t* lo, uint32_t* count, uint32_t* carry, int64_t even,
-                                         unsigned long long add) {
-    const unsigned long long old = atomicAdd(reinterpret_cast<unsigned long long*>(lo + even), add);
-    const bool low_wrap = ((old & 0xffffffffull) + (add & 0xffffffffull)) >> 32;
-    const bool pair_wrap = old + add < old;
-    if (low_wrap) atomicAdd(count + even, 1u);
-    if (pair_wrap) atomicAdd(count + even + 1, 1u);
-    if (low_wrap || pair_wrap) atomicOr(carry, 1u);
-}
-
 __global__ void k_deposit32(wbc_grid_geometry g, int32_t n, const float* __restrict__ position,
                             const int32_t* __restrict__ cell_state, const int32_t* __restrict__ order,
                             uint32_t* __restrict__ lo, uint32_t* __restrict__ count, uint32_t* __restrict__ carry) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int64_t nodes = static_cast<int64_t>(g.nx) * g.ny * g.nz;
-    // the cell rule and weights of deposit_cell (kernels/field_kernels.py:78-116)
-    bool ok = t < n;
-    int s = 0, i0 = 0, j0 = 0, k0 = 0;
-    float fx = 0.0f, fy = 0.0f, fz = 0.0f;
-    if (ok) {
-        const int c = order ? order[t] : t;
-        s = cell_state[c];
-        const float* p = position + 3 * static_cast<int64_t>(c);
-        const float ux = (p[0] - g.origin_x) * g.inv_dx;
-        const float uy = (p[1] - g.origin_y) * g.inv_dx;
-        const float uz = (p[2] - g.origin_z) * g.inv_dx;
-        i0 = static_cast<int>(floorf(ux));
-        j0 = static_cast<int>(floorf(uy));
-        k0 = static_cast<int>(floorf(uz));
-        ok = s >= 0 && s < 4 && i0 >= 0 && j0 >= 0 && k0 >= 0 && i0 + 1 < g.nx && j0 + 1 < g.ny && k0 + 1 < g.nz;
-        fx = ux - static_cast<float>(i0);
-        fy = uy - static_cast<float>(j0);
-        fz = uz - static_cast<float>(k0);
-    }
-    if (!ok) return;
-#pragma unroll
-    for (int di = 0; di < 2; ++di) {
-        const float wx = di == 0 ? 1.0f - fx : fx;
-#pragma unroll
-        for (int dj = 0; dj < 2; ++dj) {
-            const float wy = dj == 0 ? 1.0f - fy : fy;
-            const float w0 = wx * wy * (1.0f - fz);
-            const float w1 = wx * wy * fz;
-            const unsigned long long q0 = static_cast<unsigned int>(static_cast<int>(w0 * kFixedOne + 0.5f));
-            const unsigned long long q1 = static_cast<unsigned int>(static_cast<int>(w1 * kFixedOne + 0.5f));
-            // word of corner k0; corner k0 + 1 is the next word (4 * nodes is even, so both pairs
-            // touched below lie inside the layer array)
-            const int64_t key = s * nodes + (static_cast<int64_t>(i0 + di) * g.ny + (j0 + dj)) * g.nz + k0;
-            if ((key & 1) == 0) {
-                add_pair(lo, count, carry, key, q0 | (q1 << 32));
-            } else {
-                add_pair(lo, count, carry, key - 1, q0 << 32);
-                add_pair(lo, count, carry, key + 1, q1);
-            }
-        }
-    }
+    if (t < n) deposit32_cell(g, order ? order[t] : t, position, cell_state, lo, count, carry);
 }
 
 // density_s = S_s / 2^24 * inv_vol per state, as convert_node, with S_s the exact sum of the paired
@@ -142,21 +90,7 @@ __global__ void k_convert32(int64_t nodes, const uint32_t* __restrict__ lo, cons
                             const uint32_t* __restrict__ carry, float inv_vol, float* __restrict__ density, float w0,
                             float w1, float w2, float w3, float* __restrict__ combined) {
     const int64_t node = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
-    if (node >= nodes) return;
-    const bool wrapped = *carry != 0u;
-    float d[4];
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-        const int64_t w = s * nodes + node;
-        long long a = static_cast<long long>(lo[w]);
-        if (wrapped) {
-            a += static_cast<long long>(count[w]) << 32;
-            if (w & 1) a -= static_cast<long long>(count[w - 1]);
-        }
-        d[s] = static_cast<float>(a) / kFixedOne * inv_vol;
-        if (density) density[s * nodes + node] = d[s];
-    }
-    if (combined) combined[node] = w0 * d[0] + w1 * d[1] + w2 * d[2] + w3 * d[3];
+    if (node < nodes) convert32_node(nodes, node, lo, count, *carry != 0u, inv_vol, density, w0, w1, w2, w3, combined);
 }
 
 __global__ void k_combine(int64_t nodes, float w0, float w1, float w2, float w3, const float* __restrict__ density,

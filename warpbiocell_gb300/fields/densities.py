@@ -107,10 +107,11 @@ class CellDensities:
         _lib.call("wbc_density_combine", self.geometry.node_count, w, _lib.ptr(self.density), _lib.ptr(out),
                   _lib.stream(self.device))
 
-    def planes_for_writing(self) -> torch.Tensor:
-        """The per-state density planes, for a caller that writes them itself (the batched step)."""
-        self._planes_current = True
-        return self._planes
+    def accumulator_for_writing(self) -> torch.Tensor:
+        """The 32-bit accumulator, for a caller that deposits into it itself (the batched step); the
+        per-state densities are then converted from it when ``density`` is read."""
+        self._planes_current = False
+        return self._acc
 
     def numpy(self) -> np.ndarray:
         return self.density.cpu().numpy().copy()

@@ -59,7 +59,6 @@ class SpheroidBatch:
                 raise ValueError("batched members have a single consumed species (oxygen)")
             m.contact.check_substep(stepping.dt_mechanics)
         self.settings = settings
-        self._accumulators: list[torch.Tensor] = []
         n = len(members)
         self.counts = torch.tensor([m.population.count for m in members], dtype=torch.int32, device=self.device)
         self.status = torch.zeros(n, dtype=torch.int32, device=self.device)
@@ -123,12 +122,11 @@ class SpheroidBatch:
         inst.contact_dt = float(self.stepping.dt_mechanics)
         inst.contact_substeps = self.stepping.mechanics_substeps
         inst.geom = fld.geometry.native()
-        # the batched deposit keeps its own int64 accumulator per member and writes the per-state
-        # densities itself
-        acc = torch.zeros((4, *fld.geometry.shape), dtype=torch.int64, device=self.device)
-        self._accumulators.append(acc)
-        inst.accumulator = _lib.ptr(acc)
-        inst.density = _lib.ptr(dens.planes_for_writing())
+        # the batched deposit writes into the member's own 32-bit accumulator and produces only the
+        # combined uptake density; the member's per-state densities are converted from the same sums
+        # when they are read, as on the plain path
+        inst.accumulator = _lib.ptr(dens.accumulator_for_writing())
+        inst.density = None
         inst.uptake_density = _lib.ptr(fld.density)
         inst.uptake_weights = (ctypes.c_float * 4)(*[float(x) for x in w])
         inst.inv_voxel_volume = 1.0 / fld.geometry.voxel_volume
