@@ -1,6 +1,6 @@
 """Batched spheroids against plain runs: every member of a SpheroidBatch must end bit-identical to
-running cell_step on it alone (populations, fields, cell counts, solver sweeps), with and
-without CUDA-graph capture of the step."""
+running cell_step on it alone (populations, fields, deposits and densities, cell counts, solver
+sweeps), with and without CUDA-graph capture of the step."""
 
 import numpy as np
 import pytest
@@ -46,7 +46,10 @@ def _snapshot(m):
     n = pop.count
     arrays = [pop.position[:n], pop.radius[:n], pop.cell_state[:n], pop.age[:n], pop.oxygen_local[:n],
               pop.rng_state, pop.velocity[:n], pop.neighbor_count[:n]]
-    return n, [a.cpu().numpy().copy() for a in arrays] + [m.oxygen.field.values.cpu().numpy().copy()]
+    # the field, the solver's uptake density, and the per-state densities converted on reading
+    # from the last deposit's sums
+    fields = [m.oxygen.field.values, m.oxygen.density, m.oxygen.densities.density, m.oxygen.densities.accumulator]
+    return n, [a.cpu().numpy().copy() for a in arrays + fields]
 
 
 def _plain(steps):
