@@ -289,10 +289,11 @@ __global__ void __launch_bounds__(kScanThreads) k_b_scan_reduce(BatchPlan P, con
         const Segment g = S::get(P, counts, b);
         const int local = t - first[b];
         const int64_t base = static_cast<int64_t>(local) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+        int32_t vals[kScanItems];
+        load_items(g.in, base, g.n, vals);
         int32_t s = 0;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k)
-            if (base + k < g.n) s += g.in[base + k];
+        for (int k = 0; k < kScanItems; ++k) s += vals[k];
         int32_t total;
         block_exclusive(s, &total);
         if (threadIdx.x == 0) g.partials[local] = total;
@@ -332,20 +333,20 @@ __global__ void __launch_bounds__(kScanThreads) k_b_scan_apply(BatchPlan P, cons
         const int local = t - first[b];
         const int64_t base = static_cast<int64_t>(local) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
         int32_t vals[kScanItems];
+        load_items(g.in, base, g.n, vals);
         int32_t s = 0;
 #pragma unroll
-        for (int k = 0; k < kScanItems; ++k) {
-            vals[k] = base + k < g.n ? g.in[base + k] : 0;
-            s += vals[k];
-        }
+        for (int k = 0; k < kScanItems; ++k) s += vals[k];
         int32_t total;
         int32_t run = block_exclusive(s, &total) + g.partials[local];
+        int32_t res[kScanItems];
 #pragma unroll
         for (int k = 0; k < kScanItems; ++k) {
             if (S::kInclusive) run += vals[k];
-            if (base + k < g.n) g.out[base + k] = run;
+            res[k] = run;
             if (!S::kInclusive) run += vals[k];
         }
+        store_items(g.out, base, g.n, res);
     }
 }
 

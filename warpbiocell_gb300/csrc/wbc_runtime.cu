@@ -38,12 +38,11 @@ int64_t scan_partials_count(int64_t n) { return (n + kScanTile - 1) / kScanTile 
 
 __global__ void scan_reduce_tiles(const int32_t* __restrict__ in, int64_t n, int32_t* __restrict__ partials) {
     const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
+    int32_t vals[kScanItems];
+    load_items(in, base, n, vals);
     int32_t s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        int64_t idx = base + k;
-        if (idx < n) s += in[idx];
-    }
+    for (int k = 0; k < kScanItems; ++k) s += vals[k];
     int32_t total;
     block_exclusive(s, &total);
     if (threadIdx.x == 0) partials[blockIdx.x] = total;
@@ -69,22 +68,20 @@ __global__ void scan_tiles(const int32_t* __restrict__ in, int32_t* __restrict__
                            const int32_t* __restrict__ partials, bool inclusive) {
     const int64_t base = static_cast<int64_t>(blockIdx.x) * kScanTile + static_cast<int64_t>(threadIdx.x) * kScanItems;
     int32_t vals[kScanItems];
+    load_items(in, base, n, vals);
     int32_t s = 0;
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        int64_t idx = base + k;
-        vals[k] = idx < n ? in[idx] : 0;
-        s += vals[k];
-    }
+    for (int k = 0; k < kScanItems; ++k) s += vals[k];
     int32_t total;
     int32_t run = block_exclusive(s, &total) + partials[blockIdx.x];
+    int32_t res[kScanItems];
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        int64_t idx = base + k;
         if (inclusive) run += vals[k];
-        if (idx < n) out[idx] = run;
+        res[k] = run;
         if (!inclusive) run += vals[k];
     }
+    store_items(out, base, n, res);
 }
 
 int scan_i32(const int32_t* in, int32_t* out, int64_t n, bool inclusive, int32_t* partials, int32_t* total,
