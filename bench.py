@@ -542,9 +542,10 @@ def report_gpu(args, results: list[dict], world: int) -> dict:
                         "what": "the solve is on chip and bound by instruction issue, not HBM",
                         "node_updates_per_s": round(updates_per_s, 1),
                         "half_sweep_us": round(half_us, 3),
-                        "warp_inst_per_node_update_ncu": round(SOR_NCU["warp_inst_per_node_update"], 3),
-                        "issue_active_ncu": SOR_NCU["issue_active"],
-                        "source": SOR_NCU["source"]},
+                        "warp_inst_per_node_update_ncu": (round(SOR_NCU["warp_inst_per_node_update"], 3)
+                                                          if args.workload == "spheroid_1M_161" else None),
+                        "issue_active_ncu": SOR_NCU["issue_active"] if args.workload == "spheroid_1M_161" else None,
+                        "source": SOR_NCU["source"] if args.workload == "spheroid_1M_161" else None},
                     "streaming_equivalent_GBps": round(8.0 * nodes / (half_us / 1e6) / 1e9, 1)}
     elif dominant:
         s = stages[dominant]
