@@ -216,6 +216,19 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
                   const int32_t* fixed, const float* density, const float* production, const float* source,
                   float* field, float* residual_out, wbc_sor_report* report, void* workspace,
                   size_t workspace_bytes, int32_t path, const wbc_sor_tuning* tuning, void* stream);
+/* wbc_sor_solve without waiting for its report: the resident solve copies its report into
+ * `record` (host memory of wbc_sor_report_record_bytes() bytes, pinned so that the copy stays
+ * asynchronous) in stream order and the call returns at once; wbc_sor_report_decode reads it once
+ * the stream has passed the solve (after a synchronisation the caller makes anyway, e.g. reading
+ * the division count). A grid that is solved on the streaming path is solved synchronously and
+ * its record is final at once. The same solve, sweeps and bits as wbc_sor_solve. */
+size_t wbc_sor_report_record_bytes(void);
+int wbc_sor_solve_deferred(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
+                           const int32_t* fixed, const float* density, const float* production, const float* source,
+                           float* field, float* residual_out, void* record, void* workspace, size_t workspace_bytes,
+                           int32_t path, const wbc_sor_tuning* tuning, void* stream);
+/* The report of a deferred solve (WBC_ERR_TIMEOUT if one of its device waits timed out). */
+int wbc_sor_report_decode(const void* record, wbc_sor_report* report);
 /* The linear system d_a x_a - sum_nb x_nb = b_a (d_a > 0; nodes with d_a <= 0 and Dirichlet faces
  * keep their values in x) by red-black SOR with relaxation p->omega in the same resident
  * launch as wbc_sor_solve, from x's current values, checking every `check_every` sweeps whether

@@ -234,6 +234,10 @@ SIGNATURES: dict[str, list] = {
     "wbc_sor_wait_selftest": [_I, _I, _I, _P, c_size_t, _P],
     "wbc_sor_solve": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, _P, POINTER(SorReportC),
                       _P, c_size_t, _I, POINTER(SorTuningC), _P],
+    "wbc_sor_report_record_bytes": [],
+    "wbc_sor_solve_deferred": [POINTER(SorParamsC), _I, _I, ctypes.c_double, _P, _P, _P, _P, _P, _P, _P, _P,
+                               c_size_t, _I, POINTER(SorTuningC), _P],
+    "wbc_sor_report_decode": [_P, POINTER(SorReportC)],
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
                          POINTER(c_float), _P],
     "wbc_sor_batch_plan_bytes": [_I],
@@ -292,9 +296,8 @@ SIGNATURES: dict[str, list] = {
 }
 _RESTYPE = {"wbc_last_error": ctypes.c_char_p, "wbc_scan_workspace_bytes": c_size_t, "wbc_launch_count": c_int64,
             "wbc_sor_solve_workspace_bytes": c_size_t, "wbc_sor_batch_plan_bytes": c_size_t,
-            "wbc_batch_plan_bytes": c_size_t,
-    "wbc_contact_steps_workspace_bytes": c_size_t,
-    "wbc_deposit32_bytes": c_size_t}
+            "wbc_batch_plan_bytes": c_size_t, "wbc_contact_steps_workspace_bytes": c_size_t,
+            "wbc_deposit32_bytes": c_size_t, "wbc_sor_report_record_bytes": c_size_t}
 
 _lock = threading.Lock()
 _lib: ctypes.CDLL | None = None

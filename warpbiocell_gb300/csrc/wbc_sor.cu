@@ -1032,10 +1032,20 @@ static void place_workspace(const wbc_sor_params& p, void* workspace, SorArgs* a
     a->pcopy = reinterpret_cast<float*>(base + off);
 }
 
+// Host record of a deferred solve's report (wbc_sor_solve_deferred): the solver's control line,
+// copied by the solve's stream, and what the host knew at launch. `ready` = 1 when `report` is
+// already final (a solve on the streaming path, which reads its residual on the host anyway).
+struct SorReportRecord {
+    SorControl ctl;
+    int32_t ready, path, tiles, strips;
+    wbc_sor_report report;
+};
+
 int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps, double tolerance,
                        const int32_t* fixed, const float* density, const float* production, const float* source,
                        float* field, float* residual_out, wbc_sor_report* report, void* workspace,
-                       const wbc_sor_tuning* tuning, cudaStream_t stream, bool* feasible, bool linear = false) {
+                       const wbc_sor_tuning* tuning, cudaStream_t stream, bool* feasible, bool linear = false,
+                       SorReportRecord* deferred = nullptr) {
     const DeviceInfo dev = device_info();
     const size_t limit = static_cast<size_t>(dev.smem_optin) - 1024;  // static shared memory of the kernel
     SorTiling t{};
@@ -1085,6 +1095,19 @@ int sor_solve_resident(const wbc_sor_params& p, int check_every, int max_sweeps,
     }
     int rc = check_launch("wbc_sor_solve", 1);
     if (rc != WBC_OK) return rc;
+    if (deferred) {
+        // the control line reaches the record when the stream gets there; nothing waits here
+        deferred->ready = 0;
+        deferred->path = 2;
+        deferred->tiles = t.tiles;
+        deferred->strips = t.strips;
+        err = cudaMemcpyAsync(&deferred->ctl, args.ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, stream);
+        if (err != cudaSuccess) {
+            set_error("wbc_sor_solve_deferred: copying the report", err);
+            return WBC_ERR_CUDA;
+        }
+        return WBC_OK;
+    }
     SorControl host{};
     err = cudaMemcpyAsync(&host, args.ctl, sizeof(SorControl), cudaMemcpyDeviceToHost, stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(stream);
@@ -1538,6 +1561,59 @@ int wbc_sor_solve(const wbc_sor_params* p, int32_t check_every, int32_t max_swee
     report->path = 1;
     report->tiles = 0;
     report->strips = 0;
+    return WBC_OK;
+}
+
+size_t wbc_sor_report_record_bytes(void) { return sizeof(SorReportRecord); }
+
+int wbc_sor_solve_deferred(const wbc_sor_params* p, int32_t check_every, int32_t max_sweeps, double tolerance,
+                           const int32_t* fixed, const float* density, const float* production, const float* source,
+                           float* field, float* residual_out, void* record, void* workspace, size_t workspace_bytes,
+                           int32_t path, const wbc_sor_tuning* tuning, void* stream) {
+    if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || check_every < 1 || max_sweeps < 1 || !density || !field ||
+        !record || !workspace || (p->has_source && !source) || path < 0 || path > 2)
+        return WBC_ERR_INVALID;
+    if (workspace_bytes < sor_workspace_bytes(*p)) return WBC_ERR_WORKSPACE;
+    if (reinterpret_cast<uintptr_t>(workspace) % 16 != 0) {
+        set_error_msg("wbc_sor_solve_deferred: the workspace must be 16-byte aligned");
+        return WBC_ERR_INVALID;
+    }
+    SorReportRecord* rec = static_cast<SorReportRecord*>(record);
+    cudaStream_t s = as_stream(stream);
+    if (path != 1) {
+        bool feasible = false;
+        wbc_sor_report unused{};
+        int rc = sor_solve_resident(*p, check_every, max_sweeps, tolerance, fixed, density, production, source, field,
+                                    residual_out, &unused, workspace, tuning, s, &feasible, false, rec);
+        if (rc != WBC_OK || feasible) return rc;
+    }
+    // not resident: the synchronous solve (its report is final at once)
+    wbc_sor_report report{};
+    int rc = wbc_sor_solve(p, check_every, max_sweeps, tolerance, fixed, density, production, source, field,
+                           residual_out, &report, workspace, workspace_bytes, path, tuning, stream);
+    if (rc != WBC_OK) return rc;
+    rec->ready = 1;
+    rec->report = report;
+    return WBC_OK;
+}
+
+int wbc_sor_report_decode(const void* record, wbc_sor_report* report) {
+    if (!record || !report) return WBC_ERR_INVALID;
+    const SorReportRecord* rec = static_cast<const SorReportRecord*>(record);
+    if (rec->ready) {
+        *report = rec->report;
+        return WBC_OK;
+    }
+    if (rec->ctl.status != 0) {
+        set_error_msg("wbc_sor_solve_deferred: a device wait timed out");
+        return WBC_ERR_TIMEOUT;
+    }
+    report->sweeps = rec->ctl.sweeps;
+    report->residual = rec->ctl.residual;
+    report->converged = rec->ctl.converged;
+    report->path = rec->path;
+    report->tiles = rec->tiles;
+    report->strips = rec->strips;
     return WBC_OK;
 }
 

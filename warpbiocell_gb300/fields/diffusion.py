@@ -89,6 +89,47 @@ def sor_chunk(field: ScalarField, density: torch.Tensor, params: _lib.SorParamsC
                   _lib.ptr(residual_buffer), _lib.stream(field.device))
 
 
+class PendingSolve:
+    """A solve launched without waiting for its report (``solve_steady_state(..., defer=True)``):
+    the report is copied into a pinned host record in stream order and read by :meth:`result`,
+    which waits only if the stream has not passed the solve yet (in a cell step it has: the
+    division count is read after the solve)."""
+
+    def __init__(self, field: ScalarField, record: torch.Tensor, on_result=None):
+        self._field = field
+        self._record = record
+        self._event = torch.cuda.Event()
+        self._event.record(torch.cuda.current_stream(field.device))
+        self._on_result = on_result
+        self._report: SolveReport | None = None
+
+    def result(self) -> SolveReport:
+        if self._report is None:
+            self._event.synchronize()
+            rep = _lib.SorReportC()
+            _lib.call("wbc_sor_report_decode", self._record.data_ptr(), ctypes.byref(rep))  # pinned host memory
+            last_solve.update(sweeps=rep.sweeps, path=rep.path, tiles=rep.tiles, strips=rep.strips)
+            self._report = SolveReport(sweeps=int(rep.sweeps), residual=float(rep.residual),
+                                       converged=bool(rep.converged))
+            if getattr(self._field, "_pending_solve", None) is self:
+                self._field._pending_solve = None
+            if self._on_result is not None:
+                self._on_result(self._report)
+        return self._report
+
+
+def _report_record(field: ScalarField) -> torch.Tensor:
+    """The field's pinned host record for deferred reports (allocated once, 128-byte aligned)."""
+    record = getattr(field, "_report_record", None)
+    if record is None:
+        nbytes = int(_lib.load().wbc_sor_report_record_bytes())
+        raw = torch.empty(nbytes + 128, dtype=torch.uint8, pin_memory=True)
+        off = (-raw.data_ptr()) % 128
+        record = raw[off:off + nbytes]
+        field._report_record = record
+    return record
+
+
 def solve_steady_state(
     field: ScalarField,
     density: torch.Tensor,
@@ -98,11 +139,15 @@ def solve_steady_state(
     production: torch.Tensor | None = None,
     source: torch.Tensor | None = None,
     source_k: float = 1.0,
-) -> SolveReport:
+    defer: bool = False,
+    on_result=None,
+):
     """Iterate SOR sweeps in place, starting from the field's current values (warm start).
 
     ``production`` [conc/h] is an optional zero-order source per node, scaled by
-    ``S/(source_k + S)`` of the ``source`` field when one is given.
+    ``S/(source_k + S)`` of the ``source`` field when one is given. With ``defer`` the solve is
+    launched without waiting for its report and a :class:`PendingSolve` is returned (its
+    ``result()`` gives the SolveReport and calls ``on_result`` with it).
     """
     if residual_buffer.dtype != torch.float32 or residual_buffer.device != field.device or residual_buffer.numel() < 1:
         raise ValueError("residual_buffer must be a float32 tensor of at least one element on the field's device")
@@ -117,6 +162,21 @@ def solve_steady_state(
     else:
         tuning = None
     # The library writes the final residual into residual_buffer[0] itself (no extra kernel).
+    if defer:
+        earlier = getattr(field, "_pending_solve", None)
+        if earlier is not None:
+            earlier.result()  # its record is about to be reused
+        record = _report_record(field)
+        with profiling.stage("sor"):
+            _lib.call("wbc_sor_solve_deferred", ctypes.byref(params), int(settings.check_every),
+                      int(settings.max_sweeps), float(settings.tolerance), _lib.ptr(field.fixed_or_none()),
+                      _lib.ptr(density), _lib.ptr(prod), _lib.ptr(src), _lib.ptr(field.values),
+                      _lib.ptr(residual_buffer), record.data_ptr(), _lib.ptr(workspace), workspace.numel(),
+                      int(solver_path), ctypes.byref(tuning) if tuning is not None else None,
+                      _lib.stream(field.device))
+        pending = PendingSolve(field, record, on_result)
+        field._pending_solve = pending
+        return pending
     with profiling.stage("sor"):
         _lib.call("wbc_sor_solve", ctypes.byref(params), int(settings.check_every), int(settings.max_sweeps),
                   float(settings.tolerance), _lib.ptr(field.fixed_or_none()), _lib.ptr(density), _lib.ptr(prod),
@@ -124,7 +184,10 @@ def solve_steady_state(
                   _lib.ptr(workspace), workspace.numel(), int(solver_path),
                   ctypes.byref(tuning) if tuning is not None else None, _lib.stream(field.device))
     last_solve.update(sweeps=report.sweeps, path=report.path, tiles=report.tiles, strips=report.strips)
-    return SolveReport(sweeps=int(report.sweeps), residual=float(report.residual), converged=bool(report.converged))
+    result = SolveReport(sweeps=int(report.sweeps), residual=float(report.residual), converged=bool(report.converged))
+    if on_result is not None:
+        on_result(result)
+    return result
 
 
 # 0: the shared-memory resident solver when the grid fits on chip, else streaming colour launches;

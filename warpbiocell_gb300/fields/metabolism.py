@@ -93,15 +93,32 @@ class MetabolicFields:
     def __getitem__(self, name: str) -> SpeciesField:
         return self.species_fields[name]
 
-    def update(self, population) -> MetabolicReport:
+    def update(self, population, defer: bool = False):
         """One deposit for all species, then, in order, each species' coupling, steady solve and
-        sampling at the cells."""
+        sampling at the cells (with ``defer``, a pending report whose ``result()`` gives the
+        MetabolicReport)."""
         self.densities.deposit(population)
-        reports: dict[str, SolveReport] = {}
+        pending = {}
         for name, species in self.species_fields.items():
             species.combine()
-            reports[name] = species.solve_steady_state(self._sources[name])
+            pending[name] = species.solve_steady_state(self._sources[name], defer=True)
             species.sample_at_cells(population)
-        self.oxygen.last_report = reports["oxygen"]
-        self.last_report = MetabolicReport(reports)
-        return self.last_report
+        report = _PendingMetabolic(self, pending)
+        return report if defer else report.result()
+
+
+class _PendingMetabolic:
+    """The species' deferred solves of one update; ``result()`` reads them all."""
+
+    def __init__(self, fields: MetabolicFields, pending: dict):
+        self._fields = fields
+        self._pending = pending
+        self._report: MetabolicReport | None = None
+
+    def result(self) -> MetabolicReport:
+        if self._report is None:
+            reports = {name: p.result() for name, p in self._pending.items()}
+            self._fields.oxygen.last_report = reports["oxygen"]
+            self._report = MetabolicReport(reports)
+            self._fields.last_report = self._report
+        return self._report

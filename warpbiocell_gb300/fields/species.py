@@ -158,15 +158,19 @@ class SpeciesField:
                       population.count, _lib.ptr(population.position), _lib.ptr(target), _lib.stream(self.device))
 
     # ---- solvers --------------------------------------------------------------------------
-    def solve_steady_state(self, source: SpeciesField | None = None) -> SolveReport:
-        report = solve_steady_state(
+    def solve_steady_state(self, source: SpeciesField | None = None, defer: bool = False):
+        """The steady solve; with ``defer`` a PendingSolve whose ``result()`` gives the report
+        (and records it as ``last_report``)."""
+        return solve_steady_state(
             self.field, self.density, self.species.kinetics, self.settings, self._residual,
             production=self.production if self.species.produces else None,
             source=source.field.values if source is not None else None,
             source_k=source.species.michaelis_k if source is not None else 1.0,
+            defer=defer, on_result=self._record_report,
         )
+
+    def _record_report(self, report: SolveReport) -> None:
         self.last_report = report
-        return report
 
     def explicit_step(self, dt: float, source: SpeciesField | None = None) -> None:
         explicit_step(
@@ -176,9 +180,11 @@ class SpeciesField:
             source_k=source.species.michaelis_k if source is not None else 1.0,
         )
 
-    def update(self, population, source: SpeciesField | None = None, out: torch.Tensor | None = None) -> SolveReport:
-        """Deposit (if owner), combine, solve to steady state, sample: the per-cell-step update."""
+    def update(self, population, source: SpeciesField | None = None, out: torch.Tensor | None = None,
+               defer: bool = False):
+        """Deposit (if owner), combine, solve to steady state, sample: the per-cell-step update
+        (with ``defer``, the solve's report as a PendingSolve)."""
         self.deposit_uptake(population)
-        report = self.solve_steady_state(source)
+        report = self.solve_steady_state(source, defer=defer)
         self.sample_at_cells(population, out)
         return report

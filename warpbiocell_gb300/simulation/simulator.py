@@ -49,10 +49,10 @@ class StepReport:
 def cell_step(population, grid, lifecycle: LifecycleParams, contact: ContactParams, stepping: TimeStepping,
               oxygen=None, region=None, network=None) -> StepReport:
     """Advance the population by ``stepping.dt_cells``."""
-    report = StepReport(0)
-    if oxygen is not None:
-        fld = oxygen.update(population)
-        report = StepReport(0, fld.sweeps, fld.residual, fld.converged)
+    # The field solves are launched without waiting for their reports: the stream runs on into
+    # the network and the lifecycle, and the reports are read once the division count (the
+    # step's one synchronisation) has been read.
+    pending = oxygen.update(population, defer=True) if oxygen is not None else None
     if network is not None:
         network.step(population, stepping.dt_cells)
     count_before = population.count
@@ -60,4 +60,7 @@ def cell_step(population, grid, lifecycle: LifecycleParams, contact: ContactPara
     if network is not None and n_daughters:
         network.inherit(population, count_before)
     relax_contacts(population, grid, contact, stepping.dt_mechanics, stepping.mechanics_substeps, region)
-    return StepReport(n_daughters, report.field_sweeps, report.field_residual, report.field_converged)
+    if pending is None:
+        return StepReport(n_daughters)
+    fld = pending.result()
+    return StepReport(n_daughters, fld.sweeps, fld.residual, fld.converged)
