@@ -297,6 +297,26 @@ def test_warm_start_needs_one_check_and_uniform_stays_uniform():
     np.testing.assert_array_equal(flat.numpy(), 40.0)
 
 
+def test_deferred_solve_equals_waiting_solve():
+    """A solve whose report is read later (wbc_sor_solve_deferred, as a cell step launches its
+    field solves) gives the same field bits and report as the solve that waits for it, also when
+    a second deferred solve of the same field is started before the first is read."""
+    geom = GridGeometry.centered_cube(400.0, 20.0)
+    x, y, z = np.meshgrid(*geom.node_coordinates(), indexing="ij")
+    density = _t(np.where(x**2 + y**2 + z**2 < 150.0**2, 2.4e-4, 0.0).astype(np.float32))
+    settings = SolverSettings(omega=1.8, tolerance=1e-6, check_every=10)
+    waits = OxygenField(geom, OxygenParams(), settings, device=DEV)
+    defers = OxygenField(geom, OxygenParams(), settings, device=DEV)
+    for f in (waits, defers):
+        f.density.copy_(density)
+    want = [waits.solve_steady_state(), waits.solve_steady_state()]
+    first = defers.solve_steady_state(defer=True)
+    second = defers.solve_steady_state(defer=True)  # reads the first before reusing its record
+    got = [first.result(), second.result()]
+    assert got == want and defers.last_report == want[1]
+    np.testing.assert_array_equal(defers.numpy(), waits.numpy())
+
+
 # ---- mechanics ------------------------------------------------------------------------------------------------
 def test_neighbor_counts_match_brute_force_and_positions_match_oracle(golden):
     g = golden("contact")
