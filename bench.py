@@ -879,15 +879,21 @@ def run_batched(args, rank: int = 0, world: int = 1) -> dict:
     time.sleep(0.3)
     plain_cells, plain_ms = timed(lambda: run_plain(args.steps), "sequential_steps")
 
-    # The same 15 runs as one batch: the first warm-up step outside the graph, then capture.
+    # The same 15 runs as one batch: the first warm-up steps outside the graph, the solve plan
+    # re-made from the mean sweep counts of those after the first (which starts from the initial
+    # field), then capture.
     members = [build_member(sp, P, dev) for sp in specs]
     batch = SpheroidBatch(members, stepping)
-    batch.step(1)
-    torch.cuda.synchronize()
-    batch.rebalance()  # the first step's sweep counts weigh the work list
+    plan_steps = max(1, min(args.batch_plan_steps, args.warmup))
+    history = []
+    for k in range(plan_steps):
+        batch.step(1)
+        if k > 0 or plan_steps == 1:
+            history.append([r.sweeps for r in batch.reports()])
+    batch.rebalance([sum(col) / len(col) for col in zip(*history)])
     batch.capture()
-    if args.warmup > 1:
-        batch.step(args.warmup - 1)
+    if args.warmup > plan_steps:
+        batch.step(args.warmup - plan_steps)
     _, batch_ms = timed(lambda: batch.step(args.steps), "timed_steps")
     clocks = sampler.stop()
     counts = batch.sync()
@@ -1115,6 +1121,9 @@ def main() -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--skip-cpu", action="store_true", help="skip the CPU baseline sample and parity check")
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
+    ap.add_argument("--batch-plan-steps", type=int, default=4,
+                    help="batched sweep: warm-up steps before the solve plan is re-made from their mean sweep counts "
+                         "(the first step's excepted; at most --warmup)")
     ap.add_argument("--sor-tuning", default="",
                     help="tiles,strips for the resident solver instead of the autotuner's pick")
     ap.add_argument("--no-extras", action="store_true",

@@ -37,6 +37,7 @@
 // Every wait is bounded in time (kWaitLimitNs of the GPU's global timer, 2 s); on timeout the CTA
 // raises an abort flag, every CTA leaves, and the host gets WBC_ERR_TIMEOUT.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -941,8 +942,18 @@ static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 // not valid for the grid (an empty strip or tile) or the largest tile does not fit in smem_limit.
 // `score` (may be NULL): the largest tile's columns, then its bounding box, for choosing among
 // partitions.
+// Time model of one sweep of a tile in the batched solver, in ns (a fit to per-item run times
+// traced in batched solves of 55^3-119^3 grids on 5-76 tiles each, on the GB300, within 5% rms):
+// the relaxation of the tile's owned nodes, its halo (the bounding box's perimeter columns, whose
+// pulls and mirrors scale with it) and a fixed cost per sweep (the halo exchanges' round trips and
+// the closing barriers). An item's tiles advance together, so its largest tile sets the pace.
+constexpr double kNsPerNode = 0.393, kNsPerHaloNode = 0.235, kNsPerSweep = 3140.0;
+__host__ __device__ inline double tile_sweep_ns(int owned_columns, int perimeter_columns, int nz) {
+    return kNsPerNode * owned_columns * nz + kNsPerHaloNode * perimeter_columns * nz + kNsPerSweep;
+}
+
 static bool tiling_for(const wbc_sor_params& p, int tiles, int strips, size_t smem_limit, SorTiling* out,
-                       long* score = nullptr) {
+                       long* score = nullptr, double* sweep_ns = nullptr) {
     if (tiles < 1 || tiles > kMaxCtas || strips < 1 || strips > p.ny || strips > tiles) return false;
     const int M = (p.nz + 1) / 2;
     if (M > kMaxEntries || p.nx > 32767 || p.ny > 32767) return false;
@@ -985,6 +996,7 @@ static bool tiling_for(const wbc_sor_params& p, int tiles, int strips, size_t sm
     if (t.smem > smem_limit) return false;
     *out = t;
     if (score) *score = static_cast<long>(max_owned) * 100000 + max_box;
+    if (sweep_ns) *sweep_ns = tile_sweep_ns(max_owned, max_perimeter, p.nz);
     return true;
 }
 
@@ -1003,6 +1015,29 @@ static bool choose_tiling(const wbc_sor_params& p, int tiles, size_t smem_limit,
         if (!found || score < best) {
             found = true;
             best = score;
+            *out = t;
+        }
+    }
+    return found;
+}
+
+// The tiling of `tiles` tiles with the smallest modelled sweep time, over strip counts around the
+// square shape (long thin tiles have long halos: at 101^3 on 34 tiles, 17 strips ran a sweep in
+// 20.7 us against 15.8 us modelled for 4 strips); false if none fits in shared memory.
+static bool compact_tiling(const wbc_sor_params& p, int tiles, size_t smem_limit, SorTiling* out, double* sweep_ns) {
+    tiles = std::min({tiles, kMaxCtas, p.nx * p.ny});
+    if (tiles < 1) return false;
+    const double square = std::sqrt(static_cast<double>(tiles) * p.ny / p.nx);
+    const int lo = std::max(1, static_cast<int>(square / 2.0));
+    const int hi = std::min({p.ny, tiles, static_cast<int>(2.0 * square) + 2});
+    bool found = false;
+    for (int strips = lo; strips <= hi; ++strips) {
+        SorTiling t{};
+        double ns = 0.0;
+        if (!tiling_for(p, tiles, strips, smem_limit, &t, nullptr, &ns)) continue;
+        if (!found || ns < *sweep_ns) {
+            found = true;
+            *sweep_ns = ns;
             *out = t;
         }
     }
@@ -1169,6 +1204,140 @@ static SorBatchLayout sor_batch_layout(int n) {
 
 using namespace wbc;
 
+// The batched solve's plan: the order of the items in the work list and each item's tiling, on G
+// CTAs with `limit` bytes of shared memory each; false if some grid does not fit. `work` is the
+// expected work per item (nodes x sweeps when `weighted`, else nodes).
+//
+// Waves: groups of items that run at the same time, each item on its own tiles, the next wave's
+// tiles claimed as CTAs free up. The items are taken in order of sweep count (work / nodes; 1
+// without weights), most first, and cut into contiguous waves by dynamic programming over the cut
+// points, minimising the sum of the waves' durations under the time model of tile_sweep_ns (an
+// item's duration: its sweeps x the modelled sweep time of its tiling). Within a wave the tile
+// counts give every item the same duration, each with at least the fewest tiles that fit in shared
+// memory, and CTAs left over go to the slowest items. Grouping items of similar sweep counts
+// matters: a tile pays a fixed cost every sweep besides the relaxation of its nodes, so CTAs in
+// proportion to work alone leave the items with more sweeps ending last while the wave's other
+// CTAs wait in the next wave's first barrier. Every tiling is the compact one for its tile count.
+static bool plan_batch(int n, const wbc_sor_batch_item* items, const std::vector<double>& work, bool weighted, int G,
+                       size_t limit, std::vector<int32_t>& order, std::vector<SorTiling>& tiling) {
+    // per distinct grid: the tile counts along which the modelled sweep time falls (the Pareto
+    // front of count against time, from the fewest tiles that fit), with their tilings
+    struct Front {
+        int nx, ny, nz;
+        std::vector<int> tiles;
+        std::vector<double> ns;
+        std::vector<SorTiling> tiling;
+    };
+    std::vector<Front> fronts;
+    std::vector<int> front_of(n);
+    std::vector<double> sweeps(n);
+    for (int b = 0; b < n; ++b) {
+        const wbc_sor_params& p = items[b].params;
+        sweeps[b] = weighted ? work[b] / (static_cast<double>(p.nx) * p.ny * p.nz) : 1.0;
+        int f = 0;
+        while (f < static_cast<int>(fronts.size()) &&
+               !(fronts[f].nx == p.nx && fronts[f].ny == p.ny && fronts[f].nz == p.nz))
+            ++f;
+        if (f == static_cast<int>(fronts.size())) {
+            Front fr{p.nx, p.ny, p.nz, {}, {}, {}};
+            for (int T = 1; T <= G; ++T) {
+                SorTiling t{};
+                double ns = 0.0;
+                if (!compact_tiling(p, T, limit, &t, &ns)) continue;
+                if (t.tiles != T) break;  // fewer columns than tiles
+                if (fr.ns.empty() || ns < fr.ns.back()) {
+                    fr.tiles.push_back(T);
+                    fr.ns.push_back(ns);
+                    fr.tiling.push_back(t);
+                }
+            }
+            if (fr.tiles.empty()) return false;
+            fronts.push_back(fr);
+        }
+        front_of[b] = f;
+    }
+    order.resize(n);
+    for (int b = 0; b < n; ++b) order[b] = b;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        if (sweeps[x] != sweeps[y]) return sweeps[x] > sweeps[y];
+        return work[x] > work[y];
+    });
+    // an item's choice is an index into its front; duration falls with the index
+    auto duration = [&](int b, int k) { return sweeps[b] * fronts[front_of[b]].ns[k]; };
+    auto count = [&](int b, int k) { return fronts[front_of[b]].tiles[k]; };
+    auto last = [&](int b) { return static_cast<int>(fronts[front_of[b]].tiles.size()) - 1; };
+    // the first index with duration <= D, or -1
+    auto within = [&](int b, double D) {
+        int lo = 0, hi = last(b);
+        if (duration(b, hi) > D) return -1;
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            if (duration(b, mid) <= D)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        return lo;
+    };
+    // equal-duration choices for the items order[lo, hi) on G CTAs; their duration, or -1
+    auto wave_plan = [&](int lo, int hi, std::vector<int>* pick) {
+        int need = 0;
+        double D_hi = 0.0, D_lo = 0.0;
+        for (int k = lo; k < hi; ++k) {
+            need += count(order[k], 0);
+            D_hi = std::max(D_hi, duration(order[k], 0));
+        }
+        if (need > G) return -1.0;
+        for (int it = 0; it < 40; ++it) {
+            const double D = 0.5 * (D_lo + D_hi);
+            int total = 0;
+            for (int k = lo; k < hi && total <= G; ++k) {
+                const int q = within(order[k], D);
+                total += q < 0 ? G + 1 : count(order[k], q);
+            }
+            (total <= G ? D_hi : D_lo) = D;
+        }
+        std::vector<int> K(hi - lo);
+        int total = 0;
+        for (int k = lo; k < hi; ++k) total += count(order[k], K[k - lo] = within(order[k], D_hi));
+        while (true) {  // spare CTAs: the slowest item's next choice, while it fits
+            int slow = 0;
+            for (int q = 1; q < hi - lo; ++q)
+                if (duration(order[lo + q], K[q]) > duration(order[lo + slow], K[slow])) slow = q;
+            const int b = order[lo + slow];
+            if (K[slow] == last(b) || total + count(b, K[slow] + 1) - count(b, K[slow]) > G) break;
+            total += count(b, K[slow] + 1) - count(b, K[slow]);
+            ++K[slow];
+        }
+        double D = 0.0;
+        for (int q = 0; q < hi - lo; ++q) D = std::max(D, duration(order[lo + q], K[q]));
+        if (pick) *pick = K;
+        return D;
+    };
+    constexpr int kMaxWave = 48;  // items per wave (bounds the planning time of large batches)
+    std::vector<double> best(n + 1, -1.0);
+    std::vector<int> cut(n + 1, 0);
+    best[0] = 0.0;
+    for (int hi = 1; hi <= n; ++hi) {
+        for (int lo = hi - 1; lo >= std::max(0, hi - kMaxWave); --lo) {
+            const double D = wave_plan(lo, hi, nullptr);
+            if (D < 0.0) break;  // a longer wave does not fit either
+            if (best[lo] >= 0.0 && (best[hi] < 0.0 || best[lo] + D < best[hi])) {
+                best[hi] = best[lo] + D;
+                cut[hi] = lo;
+            }
+        }
+    }
+    if (best[n] < 0.0) return false;
+    tiling.assign(n, SorTiling{});
+    for (int hi = n; hi > 0; hi = cut[hi]) {
+        std::vector<int> K;
+        wave_plan(cut[hi], hi, &K);
+        for (int k = cut[hi]; k < hi; ++k) tiling[k] = fronts[front_of[order[k]]].tiling[K[k - cut[hi]]];
+    }
+    return true;
+}
+
 extern "C" {
 
 size_t wbc_sor_batch_plan_bytes(int32_t n) { return n > 0 ? sor_batch_layout(n).bytes : 0; }
@@ -1189,7 +1358,6 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     // Expected work per item: the caller's weight (e.g. nodes x sweeps of the previous solve), or
     // its node count.
     std::vector<double> work(n);
-    double total_work = 0.0;
     for (int b = 0; b < n; ++b) {
         const wbc_sor_params& p = items[b].params;
         if (p.nx < 3 || p.ny < 3 || p.nz < 3 || !items[b].density || !items[b].field || !items[b].workspace ||
@@ -1199,46 +1367,12 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
             return WBC_ERR_INVALID;
         }
         work[b] = weights ? static_cast<double>(weights[b]) : static_cast<double>(p.nx) * p.ny * p.nz;
-        total_work += work[b];
     }
-    std::vector<int32_t> order(n);
-    for (int b = 0; b < n; ++b) order[b] = b;
-    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
-    // First choice: waves. Heaviest first, items join the current wave while every item of the wave
-    // can be tiled with floor(G x its share of the wave's work) CTAs in shared memory and the
-    // wave's tiles fit on the GPU at once; then a new wave starts. A wave's items start together
-    // and, their CTAs being proportional to their work, end together, so the next wave's tiles are
-    // claimed when a whole wave of CTAs frees up. If some item cannot be tiled that way, each item
-    // gets CTAs in proportion to three times its share of all the work instead, raised until its
-    // tiles fit in shared memory.
-    std::vector<SorTiling> tiling(n);
-    bool waves = true;
-    {
-        auto plan_wave = [&](int lo, int hi, bool commit) {
-            double w = 0.0;
-            for (int k = lo; k < hi; ++k) w += work[order[k]];
-            int tiles = 0;
-            for (int k = lo; k < hi; ++k) {
-                const int b = order[k];
-                const int share = std::max(1, static_cast<int>(G * work[b] / w));
-                SorTiling t{};
-                if (!choose_tiling(items[b].params, share, limit, 0, &t)) return false;
-                tiles += t.tiles;
-                if (commit) tiling[k] = t;
-            }
-            return tiles <= G;
-        };
-        int lo = 0;
-        while (lo < n && waves) {
-            int hi = lo + 1;
-            if (!plan_wave(lo, hi, false)) {
-                waves = false;
-                break;
-            }
-            while (hi < n && plan_wave(lo, hi + 1, false)) ++hi;
-            plan_wave(lo, hi, true);
-            lo = hi;
-        }
+    std::vector<int32_t> order;
+    std::vector<SorTiling> tiling;
+    if (!plan_batch(n, items, work, weights != nullptr, G, limit, order, tiling)) {
+        set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
+        return WBC_ERR_INVALID;
     }
     std::vector<SorArgs> args(n);
     std::vector<int32_t> first(n + 1, 0);
@@ -1248,16 +1382,7 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
         const int b = order[k];
         const wbc_sor_batch_item& it = items[b];
         const wbc_sor_params& p = it.params;
-        SorTiling t = tiling[k];
-        if (!waves) {
-            int share = std::min(G, std::max(1, static_cast<int>(3.0 * G * work[b] / total_work + 0.5)));
-            bool fits = false;
-            for (; share <= G && !fits; ++share) fits = choose_tiling(p, share, limit, 0, &t);
-            if (!fits) {
-                set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
-                return WBC_ERR_INVALID;
-            }
-        }
+        const SorTiling& t = tiling[k];
         SorArgs& a = args[k];
         a.p = p;
         a.t = t;

@@ -97,12 +97,17 @@ class SpheroidBatch:
                   int(self.settings.max_sweeps), float(self.settings.tolerance), _lib.ptr(self._sor_plan),
                   self._sor_plan.numel(), ctypes.byref(self.sor), _lib.stream(self.device))
 
-    def rebalance(self) -> None:
-        """Re-plan the batched solve with each member's last sweep count x grid nodes as its
-        expected work (the heaviest solves start first, with the most CTAs). Drops a captured
-        graph; call :meth:`capture` again."""
-        reports = self.reports()
-        weights = [float(m.oxygen.geometry.node_count) * max(1, r.sweeps) for m, r in zip(self.members, reports)]
+    def rebalance(self, sweeps=None) -> None:
+        """Re-plan the batched solve for each member's expected sweep count: ``sweeps`` (one
+        number per member, e.g. the mean of recent solves) or else the last solve's count. The
+        planner groups members of similar sweep counts into waves and gives each the tiles that
+        make a wave's members end together. Drops a captured graph; call :meth:`capture` again."""
+        if sweeps is None:
+            sweeps = [r.sweeps for r in self.reports()]
+        sweeps = [float(x) for x in sweeps]
+        if len(sweeps) != len(self.members):
+            raise ValueError(f"need {len(self.members)} sweep counts, got {len(sweeps)}")
+        weights = [float(m.oxygen.geometry.node_count) * max(1.0, x) for m, x in zip(self.members, sweeps)]
         self._prepare_solver(weights)
         self._graph = None
 

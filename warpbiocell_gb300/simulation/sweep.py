@@ -373,13 +373,17 @@ def run_batched(configs, run_dirs=None, device=None, log: Callable[[str], None] 
     for k in range(len(exps)):
         record(k, 0.0, 0)
     n_steps = configs[0].n_steps
-    warmed = False
+    # The solve plan is re-made once from the mean sweep counts of steps 2-4 (the first step's
+    # solve starts from the initial steady state and is short); until then steps run uncaptured.
+    plan_after, history = 4, []
     for step in range(1, n_steps + 1):
         batch.step()
-        if not warmed:
-            batch.rebalance()  # the first step's sweep counts weight the solve schedule
-            batch.capture()
-            warmed = True
+        if step <= plan_after:
+            if step > 1:
+                history.append([r.sweeps for r in batch.reports()])
+            if step == plan_after:
+                batch.rebalance([sum(col) / len(col) for col in zip(*history)])
+                batch.capture()
         last = step == n_steps
         due = (step % metrics_every == 0 or last, step % profile_every == 0 or last,
                step % checkpoint_every == 0 or last)
