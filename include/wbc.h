@@ -283,12 +283,13 @@ typedef struct wbc_sor_batch {    /* filled by wbc_sor_batch_prepare            
 } wbc_sor_batch;
 
 size_t wbc_sor_batch_plan_bytes(int32_t n);
-/* Orders the items heaviest first by `weights` (host, one positive value per item, e.g. nodes x
- * sweeps of the previous solve; NULL = node counts) and groups them into waves whose tiles fit on
- * the GPU at once, each item tiled with CTAs in proportion to its weight within its wave (when an
- * item cannot be tiled that way: in proportion to its weight over all items, raised until the
- * tiles fit in shared memory), copies the work list into `plan` (device memory) and fills `out`.
- * Synchronises `stream`; not for use during stream capture. */
+/* Plans the work list from `weights` (host, one positive value per item: nodes x expected sweeps,
+ * e.g. of recent solves; NULL = node counts, i.e. equal sweeps): items ordered by sweep count
+ * (weight / nodes), cut into waves that run together by dynamic programming on a modelled
+ * duration (per tile and sweep: owned nodes, halo nodes and a fixed cost), each item of a wave
+ * given the compact tiling whose tile count makes the wave's items end together; copies the work
+ * list into `plan` (device memory) and fills `out`. WBC_ERR_INVALID if a grid fits no tiling in
+ * shared memory. Synchronises `stream`; not for use during stream capture. */
 int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
                           int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
                           void* stream);
