@@ -15,12 +15,15 @@ from contextlib import contextmanager
 import torch
 
 _enabled = False
+_only: frozenset[str] | None = None
 _events: list[tuple[str, torch.cuda.Event, torch.cuda.Event, int]] = []
 
 
-def enable(on: bool = True) -> None:
-    global _enabled
+def enable(on: bool = True, only=None) -> None:
+    """Start (or stop) recording; ``only``: the stage names to time (default every stage)."""
+    global _enabled, _only
     _enabled = on
+    _only = frozenset(only) if only is not None else None
     _events.clear()
 
 
@@ -31,7 +34,7 @@ def enabled() -> bool:
 @contextmanager
 def stage(name: str, launches: int = 1):
     """Time the enclosed launches as stage ``name`` (``launches`` kernels are attributed to it)."""
-    if not _enabled:
+    if not _enabled or (_only is not None and name not in _only):
         yield
         return
     start = torch.cuda.Event(enable_timing=True)
