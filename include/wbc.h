@@ -293,6 +293,14 @@ size_t wbc_sor_batch_plan_bytes(int32_t n);
 int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
                           int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
                           void* stream);
+/* The plan wbc_sor_batch_prepare makes, computed on the host alone (no device needed): for `ctas`
+ * CTAs with `smem_bytes` of dynamic shared memory each (152 and 231424 on the GB300), the work
+ * list's order of the items (`order`, n item indices) and, per position in it, the item's tile
+ * count, strip count, wave index (`wave`, may be NULL) and modelled sweep time in ns (`sweep_ns`,
+ * may be NULL). For inspection and tests. */
+int wbc_sor_batch_plan_host(int32_t n, const wbc_sor_params* params, const float* weights, int32_t ctas,
+                            int64_t smem_bytes, int32_t* order, int32_t* tiles, int32_t* strips, int32_t* wave,
+                            double* sweep_ns);
 /* Solves every item from its field's current values; nothing is read back (capturable). */
 int wbc_sor_batch_solve(const wbc_sor_batch* b, void* stream);
 /* The items' reports (host array of b->items); synchronises. WBC_ERR_TIMEOUT if a solve timed out. */

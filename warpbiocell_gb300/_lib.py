@@ -241,6 +241,7 @@ SIGNATURES: dict[str, list] = {
     "wbc_sor_autotune": [POINTER(SorParamsC), _I, _P, _P, _P, _P, _P, _P, _P, c_size_t, POINTER(SorTuningC),
                          POINTER(c_float), _P],
     "wbc_sor_batch_plan_bytes": [_I],
+    "wbc_sor_batch_plan_host": [_I, POINTER(SorParamsC), _P, _I, c_int64, _P, _P, _P, _P, _P],
     "wbc_sor_batch_prepare": [_I, POINTER(SorBatchItemC), _P, _I, _I, ctypes.c_double, _P, c_size_t,
                               POINTER(SorBatchC), _P],
     "wbc_sor_batch_solve": [POINTER(SorBatchC), _P],

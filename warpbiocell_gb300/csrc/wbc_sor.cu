@@ -1218,8 +1218,10 @@ using namespace wbc;
 // matters: a tile pays a fixed cost every sweep besides the relaxation of its nodes, so CTAs in
 // proportion to work alone leave the items with more sweeps ending last while the wave's other
 // CTAs wait in the next wave's first barrier. Every tiling is the compact one for its tile count.
-static bool plan_batch(int n, const wbc_sor_batch_item* items, const std::vector<double>& work, bool weighted, int G,
-                       size_t limit, std::vector<int32_t>& order, std::vector<SorTiling>& tiling) {
+static bool plan_batch(const std::vector<wbc_sor_params>& params, const std::vector<double>& work, bool weighted,
+                       int G, size_t limit, std::vector<int32_t>& order, std::vector<SorTiling>& tiling,
+                       std::vector<int32_t>* wave_of = nullptr, std::vector<double>* sweep_ns = nullptr) {
+    const int n = static_cast<int>(params.size());
     // per distinct grid: the tile counts along which the modelled sweep time falls (the Pareto
     // front of count against time, from the fewest tiles that fit), with their tilings
     struct Front {
@@ -1232,7 +1234,7 @@ static bool plan_batch(int n, const wbc_sor_batch_item* items, const std::vector
     std::vector<int> front_of(n);
     std::vector<double> sweeps(n);
     for (int b = 0; b < n; ++b) {
-        const wbc_sor_params& p = items[b].params;
+        const wbc_sor_params& p = params[b];
         sweeps[b] = weighted ? work[b] / (static_cast<double>(p.nx) * p.ny * p.nz) : 1.0;
         int f = 0;
         while (f < static_cast<int>(fronts.size()) &&
@@ -1330,10 +1332,20 @@ static bool plan_batch(int n, const wbc_sor_batch_item* items, const std::vector
     }
     if (best[n] < 0.0) return false;
     tiling.assign(n, SorTiling{});
+    if (wave_of) wave_of->assign(n, 0);
+    if (sweep_ns) sweep_ns->assign(n, 0.0);
+    int waves = 0;
+    for (int hi = n; hi > 0; hi = cut[hi]) ++waves;
     for (int hi = n; hi > 0; hi = cut[hi]) {
         std::vector<int> K;
         wave_plan(cut[hi], hi, &K);
-        for (int k = cut[hi]; k < hi; ++k) tiling[k] = fronts[front_of[order[k]]].tiling[K[k - cut[hi]]];
+        --waves;
+        for (int k = cut[hi]; k < hi; ++k) {
+            const Front& fr = fronts[front_of[order[k]]];
+            tiling[k] = fr.tiling[K[k - cut[hi]]];
+            if (wave_of) (*wave_of)[k] = waves;
+            if (sweep_ns) (*sweep_ns)[k] = fr.ns[K[k - cut[hi]]];
+        }
     }
     return true;
 }
@@ -1341,6 +1353,37 @@ static bool plan_batch(int n, const wbc_sor_batch_item* items, const std::vector
 extern "C" {
 
 size_t wbc_sor_batch_plan_bytes(int32_t n) { return n > 0 ? sor_batch_layout(n).bytes : 0; }
+
+int wbc_sor_batch_plan_host(int32_t n, const wbc_sor_params* params, const float* weights, int32_t ctas,
+                            int64_t smem_bytes, int32_t* order, int32_t* tiles, int32_t* strips, int32_t* wave,
+                            double* sweep_ns) {
+    if (n <= 0 || !params || ctas < 1 || ctas > kMaxCtas || smem_bytes <= 0 || !order || !tiles || !strips)
+        return WBC_ERR_INVALID;
+    std::vector<wbc_sor_params> p(params, params + n);
+    std::vector<double> work(n);
+    for (int b = 0; b < n; ++b) {
+        if (p[b].nx < 3 || p[b].ny < 3 || p[b].nz < 3 || (weights && !(weights[b] > 0.0f))) {
+            set_error_msg("wbc_sor_batch_plan_host: invalid item");
+            return WBC_ERR_INVALID;
+        }
+        work[b] = weights ? static_cast<double>(weights[b]) : static_cast<double>(p[b].nx) * p[b].ny * p[b].nz;
+    }
+    std::vector<int32_t> ord, wv;
+    std::vector<SorTiling> til;
+    std::vector<double> ns;
+    if (!plan_batch(p, work, weights != nullptr, ctas, static_cast<size_t>(smem_bytes), ord, til, &wv, &ns)) {
+        set_error_msg("wbc_sor_batch_plan_host: a grid does not fit the shared-memory resident solver");
+        return WBC_ERR_INVALID;
+    }
+    for (int k = 0; k < n; ++k) {
+        order[k] = ord[k];
+        tiles[k] = til[k].tiles;
+        strips[k] = til[k].strips;
+        if (wave) wave[k] = wv[k];
+        if (sweep_ns) sweep_ns[k] = ns[k];
+    }
+    return WBC_OK;
+}
 
 int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const float* weights, int32_t check_every,
                           int32_t max_sweeps, double tolerance, void* plan, size_t plan_bytes, wbc_sor_batch* out,
@@ -1370,7 +1413,9 @@ int wbc_sor_batch_prepare(int32_t n, const wbc_sor_batch_item* items, const floa
     }
     std::vector<int32_t> order;
     std::vector<SorTiling> tiling;
-    if (!plan_batch(n, items, work, weights != nullptr, G, limit, order, tiling)) {
+    std::vector<wbc_sor_params> params(n);
+    for (int b = 0; b < n; ++b) params[b] = items[b].params;
+    if (!plan_batch(params, work, weights != nullptr, G, limit, order, tiling)) {
         set_error_msg("wbc_sor_batch_prepare: a grid does not fit the shared-memory resident solver");
         return WBC_ERR_INVALID;
     }
