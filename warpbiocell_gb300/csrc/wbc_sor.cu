@@ -319,16 +319,32 @@ __device__ __forceinline__ float neighbour_sum(const Sweep& w, const float* pv, 
     return pv[-w.si] + pv[w.si] + pv[-w.M] + pv[w.M] + vlo + vhi;
 }
 
+// |r| / max(6 u, reference) of an updated node as float bits, r = nb + h prod - (6 + h c) u with
+// c = du / (K + u) at its current value u (field_kernels.py:215-243); the residual pass and the
+// last half-sweep of a chunk (for the colour it updates) share this expression.
+template <bool HAS_PROD>
+__device__ __forceinline__ unsigned int residual_bits(const SorArgs& a, const Sweep& w, float du, float nb, float prod,
+                                                      float o) {
+    const float pr = HAS_PROD ? prod : 0.0f;
+    const float b1 = w.K + o;
+    const float cc = div_rn_fast(du, b1);
+    const float res = nb + w.h * pr - (6.0f + w.h * cc) * o;
+    const float den = fmaxf(6.0f * o, a.p.reference);
+    float val = div_rn_fast(fabsf(res), den);
+    if (!(div_fast_range(du, b1) && div_fast_range(fabsf(res), den))) val = residual_exact(du, b1, nb, pr, w.h, o, den);
+    return __float_as_uint(val);
+}
+
 // One lane-chunk (32 entries from `off` of group d) of colour `colour`: the reference's update
 // (field_kernels.py:185-212) with the Michaelis-Menten uptake linearised at the old value,
 // over-relaxed and clamped at zero. `own` and `oth` point at this lane's entry 0 of the two
 // colour planes. Every lane computes; only nodes with a coefficient are written, and the IEEE
 // division replaces the fast one only where the range tests above do not hold. An edge group also
 // stores every valid entry (unchanged ones too) to the exchange buffer with this half-sweep's tag.
-template <bool HAS_PROD, bool ZCLAMP, bool LINEAR>
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR, bool RESID>
 __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, float* po, const float* pv,
                                             unsigned long long* xp, const int4& d, int off, unsigned mask, float du,
-                                            float prod, int colour, int lane, unsigned int tag) {
+                                            float prod, int colour, int lane, unsigned int tag, unsigned int& rbits) {
     const int kp = ((mask >> lane) & 1) ^ colour;
     int m = 0, last = 0;
     if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
@@ -354,15 +370,17 @@ __device__ __forceinline__ void relax_lanes(const SorArgs& a, const Sweep& w, fl
     const float v = fmaxf(w.one_minus_omega * o + w.omega * gs, 0.0f);
     if (active) *po = v;
     if (group_edge(d) && off + lane < d.w) store_tagged(xp, active ? v : o, tag);
+    if (RESID && active) rbits = max(rbits, residual_bits<HAS_PROD>(a, w, du, nb, prod, v));
 }
 
 // The groups of one colour, a warp per group, edge groups first; the next group's coefficients
 // (and production terms), which live in L2, are loaded before the current group is relaxed.
-template <bool HAS_PROD, bool ZCLAMP, bool LINEAR, bool BRANCH_FREE>
-__device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, int colour, int warp, int nwarps,
-                                             int lane, unsigned int tag) {
+template <bool HAS_PROD, bool ZCLAMP, bool LINEAR, bool BRANCH_FREE, bool RESID = false>
+__device__ __forceinline__ unsigned int relax_colour(const SorArgs& a, const Sweep& w, int colour, int warp,
+                                                     int nwarps, int lane, unsigned int tag) {
+    unsigned int rbits = 0u;
     int q = warp;
-    if (q >= w.n_relax) return;
+    if (q >= w.n_relax) return rbits;
     const float* coeff = a.coeff + colour * w.gplane + lane;
     const float* pc = HAS_PROD ? a.pcopy + colour * w.gplane + lane : nullptr;
     float* own = w.s + colour * w.plane + lane;
@@ -398,8 +416,8 @@ __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, i
 #pragma unroll
         for (int r = 0; r < kSub; ++r)
             if (BRANCH_FREE || r == 0 || d.w > 32 * r)
-                relax_lanes<HAS_PROD, ZCLAMP, LINEAR>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r, mw[r],
-                                                      du[r], pr[r], colour, lane, tag);
+                relax_lanes<HAS_PROD, ZCLAMP, LINEAR, RESID>(a, w, po + 32 * r, pv + 32 * r, xp + 32 * r, d, 32 * r,
+                                                             mw[r], du[r], pr[r], colour, lane, tag, rbits);
         if (!more) break;
         d = dn;
 #pragma unroll
@@ -409,6 +427,7 @@ __device__ __forceinline__ void relax_colour(const SorArgs& a, const Sweep& w, i
         }
         q = qn;
     }
+    return rbits;
 }
 
 // Max-norm residual |r| / max(6 u, reference) of the group's nodes of colour `colour`, with
@@ -433,15 +452,8 @@ __device__ __forceinline__ unsigned int residual_group(const SorArgs& a, const S
         int m = 0, last = 0;
         if (ZCLAMP) lane_entry(w, d, off + lane, kp, a.p.nz, m, last);
         const float o = *po;
-        const float b1 = w.K + o;
-        const float cc = div_rn_fast(du, b1);
         const float nb = neighbour_sum<ZCLAMP>(w, pv, kp, m, last);
-        const float res = nb + w.h * prod - (6.0f + w.h * cc) * o;
-        const float den = fmaxf(6.0f * o, a.p.reference);
-        float val = div_rn_fast(fabsf(res), den);
-        if (active && !(div_fast_range(du, b1) && div_fast_range(fabsf(res), den)))
-            val = residual_exact(du, b1, nb, prod, w.h, o, den);
-        if (active) bits = max(bits, __float_as_uint(val));
+        if (active) bits = max(bits, residual_bits<HAS_PROD>(a, w, du, nb, prod, o));
     }
     return bits;
 }
@@ -737,12 +749,22 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
     float residual = __int_as_float(0x7f800000);
     bool converged = false;
     int chunk_index = 0;
+    constexpr bool kFuseResidual = !LINEAR && !BRANCH_FREE;
     while (ok && sweeps < a.max_sweeps) {
         const int chunk = min(a.check_every, a.max_sweeps - sweeps);
+        unsigned int fused_bits = 0u;
         for (int half = 0; half < 2 * chunk; ++half) {
             const int colour = half & 1;
             const unsigned int tag = static_cast<unsigned int>(2 * sweeps + half + 1);
-            relax_colour<HAS_PROD || LINEAR, ZCLAMP, LINEAR, BRANCH_FREE>(a, w, colour, warp, nwarps, lane, tag);
+            // In the batched kernel the chunk's last half-sweep (colour 1) also forms its nodes'
+            // residuals: their neighbours (colour 0) are final for the chunk, so the residual pass
+            // below needs only colour 0. (In the single-solve kernel a second copy of the
+            // branch-free relaxation in the loop made every half-sweep 12% slower.)
+            if (kFuseResidual && half == 2 * chunk - 1)
+                fused_bits = relax_colour<HAS_PROD, ZCLAMP, false, BRANCH_FREE, true>(a, w, colour, warp, nwarps,
+                                                                                     lane, tag);
+            else
+                relax_colour<HAS_PROD || LINEAR, ZCLAMP, LINEAR, BRANCH_FREE>(a, w, colour, warp, nwarps, lane, tag);
             const bool fine = pull_halo(a, w, colour, tag, warp, nwarps, lane);
             if (__syncthreads_or(!fine)) {
                 if (threadIdx.x == 0) atomicExch(&a.ctl->abort, 1u);
@@ -758,14 +780,14 @@ __device__ __forceinline__ void sor_tile(const SorArgs& a, int tile, int ntiles,
         sweeps += chunk;
         // Max-norm residual of the current field over every updated node (both colours); for a
         // linear solve also the scale it is compared against.
-        unsigned int bits = 0u, sbits = 0u;
+        unsigned int bits = fused_bits, sbits = 0u;
         for (int q = warp; q < w.n_relax; q += nwarps) {
             if (LINEAR) {
                 residual_group_linear<ZCLAMP>(a, w, q, 0, lane, bits, sbits);
                 residual_group_linear<ZCLAMP>(a, w, q, 1, lane, bits, sbits);
             } else {
                 bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 0, lane));
-                bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 1, lane));
+                if (!kFuseResidual) bits = max(bits, residual_group<HAS_PROD, ZCLAMP>(a, w, q, 1, lane));
             }
         }
 #pragma unroll
