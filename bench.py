@@ -1142,7 +1142,7 @@ def main() -> None:
     ap.add_argument("--reference-budget-s", type=float, default=120.0)
     ap.add_argument("--batch-plan-steps", type=int, default=4,
                     help="batched sweep: warm-up steps before the solve plan is re-made from their mean sweep counts "
-                         "(the first step's excepted; at most --warmup)")
+                         "(leaving out the first step's; at most --warmup)")
     ap.add_argument("--sor-tuning", default="",
                     help="tiles,strips for the resident solver instead of the autotuner's pick")
     ap.add_argument("--no-extras", action="store_true",
